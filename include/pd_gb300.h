@@ -1,0 +1,259 @@
+/*
+ * pd_gb300.h -- C ABI of the GB300 (sm_103a) implicit bond-based peridynamics
+ * step: a drop-in for the PD path of SCI-Solver_Peridynamic's PeriCUDAEngine.
+ *
+ * The reference has no plugin or FFI layer; its boundary is the C++ classes
+ * SystemParameter (src/core/parameters.h:146-162) and Simulator
+ * (src/core/simulator.h:32-57).  Each entry point below names the reference
+ * call it replaces.  All calls return a pd_status instead of calling exit()
+ * (the reference's checkCudaErrors / TRUE_OR_DIE, src/core/helper_cuda.h:906-930,
+ * src/core/utilities.h:27-36).  Pointers are host pointers; caller buffers are
+ * copied; the handle owns every device allocation.  One handle per host
+ * thread; calls on one handle are not re-entrant (as Simulator, which keeps
+ * static CG objects, src/core/simulator.cu:745-757).
+ *
+ * Units: positions and lengths are in the simulation's internal units, as the
+ * reference keeps them on the device (src/core/parameters.cu:409-429); the
+ * PD_VAR_POSITION_SCALED export multiplies by scaleFactor as DataIO does
+ * (src/core/memory_manager.cu:274-298).
+ */
+#ifndef PD_GB300_H
+#define PD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PD_GB300_ABI_VERSION 1
+
+typedef enum pd_status {
+    PD_OK = 0,
+    PD_ERR_INVALID_ARGUMENT = 1,
+    PD_ERR_CUDA = 2,               /* a CUDA runtime call failed; see pd_last_error_message */
+    PD_ERR_NOT_READY = 3,          /* pd_make_ready has not run */
+    PD_ERR_BOND_OVERFLOW = 4,      /* a particle has more bonds than max_bonds_per_particle */
+    PD_ERR_NO_DEVICE = 5,
+    PD_ERR_FILE = 6,               /* parameter file could not be opened */
+    PD_ERR_OUT_OF_MEMORY = 7,
+    PD_ERR_STATE = 8               /* call out of order (e.g. set_particles after make_ready) */
+} pd_status;
+
+/* src/core/definitions.h:154-158 */
+typedef enum pd_integrator { PD_IMPLICIT_EULER = 0, PD_NEWMARK_BETA = 1 } pd_integrator;
+
+/* 0..3 are the reference's Activity enum (src/core/parameters.h:137-144).
+ * PD_CLAMPED and PD_PRESCRIBED have no reference counterpart: a clamped
+ * particle keeps velocity 0, a prescribed one keeps the velocity it was given;
+ * both are Dirichlet rows of the implicit solve. */
+typedef enum pd_activity {
+    PD_ACTIVE = 0, PD_SEMI_ACTIVE = 1, PD_INACTIVE = 2, PD_INVISIBLE = 3,
+    PD_CLAMPED = 4, PD_PRESCRIBED = 5
+} pd_activity;
+
+typedef enum pd_precision {
+    PD_PRECISION_MIXED = 0,  /* FP32 forces/SpMV/CG vectors; FP64 stretch test, master state; ~FP64 dots */
+    PD_PRECISION_FP64 = 1    /* every step quantity in FP64 */
+} pd_precision;
+
+/* The PD-path fields of SimulationParameters (src/core/parameters.h:16-88).
+ * pd_params_derive fills the derived ones exactly as
+ * SystemParameter::calculateDependentParameters (src/core/parameters.cu:351-453). */
+typedef struct pd_sim_params {
+    int num_pd_particle;
+    int num_cell_x, num_cell_y, num_cell_z, num_cells;
+    double cell_size;
+    double sph_kernel_coeff;
+    double pd_kernel_coeff;
+    double sph_particle_mass;
+    double pd_particle_mass;
+    double boundary_min_x, boundary_min_y, boundary_min_z;
+    double boundary_max_x, boundary_max_y, boundary_max_z;
+    int pd_max_num_bonds;          /* output of make_ready */
+    int pd_time_step;              /* ticks of the time-step base */
+    double sph_particle_radius;
+    double pd_particle_radius;     /* input: radius_pd_over_sph; after derive: radius (internal units) */
+    double pd_horizon;
+    double pd_C_times_V;
+    double clockScale;
+    double scaleFactor;
+} pd_sim_params;
+
+/* RunningParameters (src/core/parameters.h:90-135). */
+typedef struct pd_run_params {
+    int adaptive_integration;
+    int gpu_device;
+    int step_per_frame;
+    int step_per_state;
+    int start_step;
+    int final_step;
+    int wall_thickness;
+    int tube_radius;
+    float sph_initial_velocity;
+    float mesh_translation_x, mesh_translation_y, mesh_translation_z;
+    float pd_stretch_limit_s0;
+    float pd_initial_velocity;
+    int dump_activity, dump_density, dump_velocity, dump_pd_bond_list_top;
+    int integrator;                /* pd_integrator */
+    char obj_file[512];
+    char saving_path[512];
+} pd_run_params;
+
+/* What the reference hard-codes in src/core/definitions.h, plus the knobs of
+ * this implementation.  pd_solver_options_default gives the reference values. */
+typedef struct pd_solver_options {
+    int precision;                 /* pd_precision; default PD_PRECISION_MIXED */
+    double cg_relative_tolerance;  /* CG_RELATIVE_TOLERANCE (1e-20), definitions.h:135 */
+    int cg_max_iterations;         /* MAX_CG_ITERATION (100000), definitions.h:134 */
+    double time_step_base;         /* SYSTEM_TIMESTEP_BASE (2^-23 s), definitions.h:65 */
+    int time_step_min;             /* TIMESTEP_PD_MIN (100), definitions.h:69 */
+    int max_substep;               /* MAX_SUBSTEP (10), definitions.h:71 */
+    int phase_in_steps;            /* PHASEIN (30), definitions.h:103 */
+    double pd_k;                   /* PD_K (5 * 2.94315e9), definitions.h:87 */
+    double bond_stiffness;         /* > 0 overrides pd_C_times_V * PD_K (no reference counterpart) */
+    double gravity[3];             /* acceleration; reference (0, -9.8, 0), cg_solver.cuh:330 */
+    double restitution;            /* RESTITUTION (0.001), definitions.h:74 */
+    int box_enabled;               /* 1: reflect at boundary_min/max +- radius (reference); 0: no walls */
+    double stretch_a, stretch_b;   /* 10, 9 in (a - b*clockScale)*s0, cg_solver.cuh:326 */
+    double alpha;                  /* alpha_pr (0.25), definitions.h:109 */
+    int max_bonds_per_particle;    /* MAX_PD_BOND_COUNT (528), definitions.h:101 */
+    /* rigid-sphere penalty contact (no reference counterpart) */
+    int sphere_enabled;
+    double sphere_center[3];       /* at simulated time 0 */
+    double sphere_velocity[3];
+    double sphere_radius;
+    double sphere_stiffness;
+    /* performance knobs: 0 = automatic */
+    int lanes_per_particle;        /* 4, 8, 16 or 32 lanes cooperate on one bond row */
+    int cg_check_interval;         /* CG iterations launched between convergence read-backs */
+} pd_solver_options;
+
+/* Export selectors for pd_get. */
+typedef enum pd_variable {
+    PD_VAR_POSITION = 0,           /* double[4n], internal units (w = 0) */
+    PD_VAR_VELOCITY = 1,           /* double[4n] */
+    PD_VAR_ACTIVITY = 2,           /* int32[n] */
+    PD_VAR_BOND_COUNT = 3,         /* int32[n]: live bonds = pd_bond_list_top + 1 */
+    PD_VAR_STRETCH = 4,            /* double[n]: pd_stretch */
+    PD_VAR_ORIGINAL_STRETCH = 5,   /* double[n]: pd_original_stretch (s0_i) */
+    PD_VAR_NEW_STRETCH = 6,        /* double[n]: pd_new_stretch of the last force pass */
+    PD_VAR_FORCE = 7,              /* double[4n]: pd_force of the last force pass */
+    PD_VAR_SOLUTION = 8,           /* double[4n]: pd_system_solution of the last solve */
+    PD_VAR_BOND_ROW_PTR = 9,       /* int64[n+1]: row starts of the bond list below */
+    PD_VAR_BOND_LIST = 10,         /* int32[total]: per particle, live neighbours ascending then broken ones ascending */
+    PD_VAR_POSITION_SCALED = 11,   /* double[4n]: positions * scaleFactor (DataIO convention) */
+    PD_VAR_ORIGINAL_POSITION = 12  /* double[4n]: pd_original_pos */
+} pd_variable;
+
+typedef struct pd_step_stats {
+    int current_step;              /* Simulator::get_current_step */
+    int cg_converged;              /* Simulator::CGConvergence */
+    int last_cg_iterations;
+    double last_cg_residual;       /* ||r|| at exit */
+    double last_cg_tolerance;      /* rel_tol * ||b|| */
+    long long total_cg_iterations;
+    int time_step_ticks;           /* current pd_time_step */
+    int substep;                   /* current_substep_ of the adaptive scheme */
+    int retries_last_step;         /* integrate() calls that rolled back in the last advance */
+    long long bonds_initial;
+    long long bonds_alive;
+    int max_bonds_per_particle;    /* pd_max_num_bonds */
+    double clock_scale;
+    double sim_time;               /* simulated seconds */
+} pd_step_stats;
+
+/* Device time per kernel class, accumulated with CUDA events on the handle's
+ * stream while profiling is on (pd_set_profiling). */
+typedef enum pd_kernel_class {
+    PD_KC_FORCE = 0, PD_KC_SPMV = 1, PD_KC_CG_VECTOR = 2, PD_KC_UPDATE = 3, PD_KC_COUNT = 4
+} pd_kernel_class;
+
+typedef struct pd_kernel_times {
+    long long launches[PD_KC_COUNT];
+    double total_ms[PD_KC_COUNT];
+} pd_kernel_times;
+
+typedef struct pd_handle pd_handle;
+
+/* ---- parameters (SystemParameter, src/core/parameters.cu) ---------------- */
+
+/* SystemParameter::initParameters (parameters.cu:40-86) + RunningParameters() (parameters.h:92-104) */
+pd_status pd_params_default(pd_sim_params* sim, pd_run_params* run);
+/* SystemParameter(const char*) (parameters.cu:21-25, 89-347): key/value file, then derive */
+pd_status pd_params_load(const char* path, pd_sim_params* sim, pd_run_params* run);
+/* SystemParameter::calculateDependentParameters (parameters.cu:351-453) */
+pd_status pd_params_derive(pd_sim_params* sim, pd_run_params* run);
+/* definitions.h constants; no reference call (they are compile-time there) */
+pd_status pd_solver_options_default(pd_solver_options* opt);
+
+/* ---- simulator (Simulator, src/core/simulator.h:32-57) -------------------- */
+
+/* Simulator(int deviceID, SimulationParameters&, RunningParameters&) (simulator.cu:34-53).
+ * opt may be NULL (reference defaults).  The device is run->gpu_device. */
+pd_status pd_create(const pd_sim_params* sim, const pd_run_params* run,
+                    const pd_solver_options* opt, pd_handle** out);
+/* ~Simulator */
+pd_status pd_destroy(pd_handle* h);
+/* Replaces filling get_pd_position/get_pd_velocity/get_pd_activity host arrays
+ * before makeReady (examples/main.cpp:64-66, examples/scene.cpp:360-395).
+ * pos4, vel4: n*4 doubles (x, y, z, w; w is ignored).  activity may be NULL
+ * (all PD_ACTIVE), vel4 may be NULL (zero).  n must equal num_pd_particle. */
+pd_status pd_set_particles(pd_handle* h, const double* pos4, const double* vel4,
+                           const int32_t* activity, int n);
+/* Optional: per-particle stretch limits s0_i instead of getstretch() after
+ * srand(1973) (simulator.cu:802-822, 852-857). */
+pd_status pd_set_stretch_limits(pd_handle* h, const double* s0, int n);
+/* Simulator::makeReady (simulator.cu:56-89): bonds on the GPU (uniform grid +
+ * radix sort + CSR) instead of the host kd-tree (simulator.cu:825-943). */
+pd_status pd_make_ready(pd_handle* h);
+/* nsteps x Simulator::advance (simulator.cu:1159-1217).  Stops early when the
+ * solver has not converged (finished() becomes true). */
+pd_status pd_advance(pd_handle* h, int nsteps);
+/* Simulator::finished (simulator.cu:141-144) */
+pd_status pd_finished(pd_handle* h, int* finished);
+/* Simulator::CGConvergence (simulator.cu:147-150) */
+pd_status pd_cg_converged(pd_handle* h, int* converged);
+/* Simulator::get_current_step (simulator.cu:153-156) */
+pd_status pd_get_current_step(pd_handle* h, int* step);
+/* Replaces get_pd_position/velocity/activity + MemoryManager::downloadFromDevice
+ * (memory_manager.cu:274-298).  bytes must be at least the size of the export. */
+pd_status pd_get(pd_handle* h, pd_variable var, void* dst, size_t bytes);
+/* Size in bytes of an export (the bond list size is known after make_ready). */
+pd_status pd_get_size(pd_handle* h, pd_variable var, size_t* bytes);
+/* CG iterations / residual (simulator.cu:773-790 prints them) and step state */
+pd_status pd_get_stats(pd_handle* h, pd_step_stats* stats);
+/* Resolved solver options and simulation parameters in use (after derive). */
+pd_status pd_get_params(pd_handle* h, pd_sim_params* sim, pd_run_params* run, pd_solver_options* opt);
+
+/* ---- profiling (Monitor, src/core/monitor.cu:53-95) ----------------------- */
+pd_status pd_set_profiling(pd_handle* h, int enabled);
+pd_status pd_get_kernel_times(pd_handle* h, pd_kernel_times* t);
+pd_status pd_reset_kernel_times(pd_handle* h);
+/* Number of kernels this library launched on the handle's stream so far. */
+pd_status pd_get_launch_count(pd_handle* h, long long* launches);
+
+/* ---- errors --------------------------------------------------------------- */
+const char* pd_status_string(pd_status s);
+/* Last error text of a handle (or of the last failed pd_create when h is NULL). */
+const char* pd_last_error_message(pd_handle* h);
+/* ABI version of the loaded library. */
+int pd_abi_version(void);
+
+/* ---- host logic exposed for testing without a GPU ------------------------ */
+
+/* glibc-compatible rand() stream: s0_i = getstretch(s0) after srand(1973)
+ * (simulator.cu:802-822, 852-857), for i = 0..n-1. */
+pd_status pd_sample_stretch_limits(float s0, int n, double* out);
+
+/* One decision of the adaptive time-step scheme of integratePeridynamics*
+ * (simulator.cu:332-401): given has_broken, updates *ticks and *substep and
+ * returns through *rollback whether the step must be rolled back. */
+pd_status pd_adaptive_decide(int has_broken, int ticks_base, int ticks_min, int max_substep,
+                             int* ticks, int* substep, int* rollback);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PD_GB300_H */

@@ -1,0 +1,355 @@
+"""GB300 implicit bond-based peridynamics step -- Python host mirror.
+
+A drop-in for the PD path of SCI-Solver_Peridynamic's PeriCUDAEngine.  The
+classes here mirror the reference's host interface over the C ABI of
+``libpd_gb300.so`` (``include/pd_gb300.h``):
+
+  SystemParameter   src/core/parameters.h:146-162 (file -> SimulationParameters,
+                    RunningParameters)
+  Simulator         src/core/simulator.h:32-57 (makeReady, advance, finished,
+                    CGConvergence, get_current_step, get_pd_position/velocity/
+                    activity host arrays)
+
+The compute path is the CUDA library; there is no CPU fallback: every call
+that needs the device raises ``PdError`` when the library or the GPU is
+missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG_DIR, "libpd_gb300.so")
+
+# pd_status
+PD_OK = 0
+STATUS_NAMES = {0: "PD_OK", 1: "PD_ERR_INVALID_ARGUMENT", 2: "PD_ERR_CUDA", 3: "PD_ERR_NOT_READY",
+                4: "PD_ERR_BOND_OVERFLOW", 5: "PD_ERR_NO_DEVICE", 6: "PD_ERR_FILE", 7: "PD_ERR_OUT_OF_MEMORY",
+                8: "PD_ERR_STATE"}
+# pd_integrator
+IMPLICIT_EULER, NEWMARK_BETA = 0, 1
+# pd_activity
+ACTIVE, SEMI_ACTIVE, INACTIVE, INVISIBLE, CLAMPED, PRESCRIBED = range(6)
+# pd_precision
+PRECISION_MIXED, PRECISION_FP64 = 0, 1
+# pd_variable
+(VAR_POSITION, VAR_VELOCITY, VAR_ACTIVITY, VAR_BOND_COUNT, VAR_STRETCH, VAR_ORIGINAL_STRETCH,
+ VAR_NEW_STRETCH, VAR_FORCE, VAR_SOLUTION, VAR_BOND_ROW_PTR, VAR_BOND_LIST, VAR_POSITION_SCALED,
+ VAR_ORIGINAL_POSITION) = range(13)
+# pd_kernel_class
+KC_FORCE, KC_SPMV, KC_CG_VECTOR, KC_UPDATE = range(4)
+KC_NAMES = ("force", "spmv", "cg_vector", "update")
+
+
+class PdError(RuntimeError):
+    def __init__(self, status, message=""):
+        self.status = status
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+
+
+class SimulationParameters(C.Structure):
+    """pd_sim_params: PD fields of SimulationParameters (src/core/parameters.h:16-88)."""
+    _fields_ = [
+        ("num_pd_particle", C.c_int), ("num_cell_x", C.c_int), ("num_cell_y", C.c_int),
+        ("num_cell_z", C.c_int), ("num_cells", C.c_int), ("cell_size", C.c_double),
+        ("sph_kernel_coeff", C.c_double), ("pd_kernel_coeff", C.c_double),
+        ("sph_particle_mass", C.c_double), ("pd_particle_mass", C.c_double),
+        ("boundary_min_x", C.c_double), ("boundary_min_y", C.c_double), ("boundary_min_z", C.c_double),
+        ("boundary_max_x", C.c_double), ("boundary_max_y", C.c_double), ("boundary_max_z", C.c_double),
+        ("pd_max_num_bonds", C.c_int), ("pd_time_step", C.c_int),
+        ("sph_particle_radius", C.c_double), ("pd_particle_radius", C.c_double),
+        ("pd_horizon", C.c_double), ("pd_C_times_V", C.c_double), ("clockScale", C.c_double),
+        ("scaleFactor", C.c_double),
+    ]
+
+
+class RunningParameters(C.Structure):
+    """pd_run_params: RunningParameters (src/core/parameters.h:90-135)."""
+    _fields_ = [
+        ("adaptive_integration", C.c_int), ("gpu_device", C.c_int), ("step_per_frame", C.c_int),
+        ("step_per_state", C.c_int), ("start_step", C.c_int), ("final_step", C.c_int),
+        ("wall_thickness", C.c_int), ("tube_radius", C.c_int), ("sph_initial_velocity", C.c_float),
+        ("mesh_translation_x", C.c_float), ("mesh_translation_y", C.c_float),
+        ("mesh_translation_z", C.c_float), ("pd_stretch_limit_s0", C.c_float),
+        ("pd_initial_velocity", C.c_float), ("dump_activity", C.c_int), ("dump_density", C.c_int),
+        ("dump_velocity", C.c_int), ("dump_pd_bond_list_top", C.c_int), ("integrator", C.c_int),
+        ("obj_file", C.c_char * 512), ("saving_path", C.c_char * 512),
+    ]
+
+
+class SolverOptions(C.Structure):
+    """pd_solver_options: the reference's definitions.h constants plus this library's knobs."""
+    _fields_ = [
+        ("precision", C.c_int), ("cg_relative_tolerance", C.c_double), ("cg_max_iterations", C.c_int),
+        ("time_step_base", C.c_double), ("time_step_min", C.c_int), ("max_substep", C.c_int),
+        ("phase_in_steps", C.c_int), ("pd_k", C.c_double), ("bond_stiffness", C.c_double),
+        ("gravity", C.c_double * 3), ("restitution", C.c_double), ("box_enabled", C.c_int),
+        ("stretch_a", C.c_double), ("stretch_b", C.c_double), ("alpha", C.c_double),
+        ("max_bonds_per_particle", C.c_int), ("sphere_enabled", C.c_int),
+        ("sphere_center", C.c_double * 3), ("sphere_velocity", C.c_double * 3),
+        ("sphere_radius", C.c_double), ("sphere_stiffness", C.c_double),
+        ("lanes_per_particle", C.c_int), ("cg_check_interval", C.c_int),
+    ]
+
+
+class StepStats(C.Structure):
+    _fields_ = [
+        ("current_step", C.c_int), ("cg_converged", C.c_int), ("last_cg_iterations", C.c_int),
+        ("last_cg_residual", C.c_double), ("last_cg_tolerance", C.c_double),
+        ("total_cg_iterations", C.c_longlong), ("time_step_ticks", C.c_int), ("substep", C.c_int),
+        ("retries_last_step", C.c_int), ("bonds_initial", C.c_longlong), ("bonds_alive", C.c_longlong),
+        ("max_bonds_per_particle", C.c_int), ("clock_scale", C.c_double), ("sim_time", C.c_double),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class KernelTimes(C.Structure):
+    _fields_ = [("launches", C.c_longlong * 4), ("total_ms", C.c_double * 4)]
+
+
+_lib = None
+
+
+def library(build_if_missing: bool = True):
+    """Load libpd_gb300.so (building it first if needed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_missing:
+        from importlib import import_module
+        build_mod = import_module(__name__ + ".build")
+        build_mod.build()
+    if not os.path.exists(LIB_PATH):
+        raise PdError(2, f"{LIB_PATH} is missing; run build.py")
+    lib = C.CDLL(LIB_PATH)
+    P = C.POINTER
+    st = C.c_int
+    vp = C.c_void_p
+    sig = {
+        "pd_params_default": (st, [P(SimulationParameters), P(RunningParameters)]),
+        "pd_params_load": (st, [C.c_char_p, P(SimulationParameters), P(RunningParameters)]),
+        "pd_params_derive": (st, [P(SimulationParameters), P(RunningParameters)]),
+        "pd_solver_options_default": (st, [P(SolverOptions)]),
+        "pd_create": (st, [P(SimulationParameters), P(RunningParameters), P(SolverOptions), P(vp)]),
+        "pd_destroy": (st, [vp]),
+        "pd_set_particles": (st, [vp, P(C.c_double), P(C.c_double), P(C.c_int32), C.c_int]),
+        "pd_set_stretch_limits": (st, [vp, P(C.c_double), C.c_int]),
+        "pd_make_ready": (st, [vp]),
+        "pd_advance": (st, [vp, C.c_int]),
+        "pd_finished": (st, [vp, P(C.c_int)]),
+        "pd_cg_converged": (st, [vp, P(C.c_int)]),
+        "pd_get_current_step": (st, [vp, P(C.c_int)]),
+        "pd_get": (st, [vp, C.c_int, vp, C.c_size_t]),
+        "pd_get_size": (st, [vp, C.c_int, P(C.c_size_t)]),
+        "pd_get_stats": (st, [vp, P(StepStats)]),
+        "pd_get_params": (st, [vp, P(SimulationParameters), P(RunningParameters), P(SolverOptions)]),
+        "pd_set_profiling": (st, [vp, C.c_int]),
+        "pd_get_kernel_times": (st, [vp, P(KernelTimes)]),
+        "pd_reset_kernel_times": (st, [vp]),
+        "pd_get_launch_count": (st, [vp, P(C.c_longlong)]),
+        "pd_status_string": (C.c_char_p, [C.c_int]),
+        "pd_last_error_message": (C.c_char_p, [vp]),
+        "pd_abi_version": (C.c_int, []),
+        "pd_sample_stretch_limits": (st, [C.c_float, C.c_int, P(C.c_double)]),
+        "pd_adaptive_decide": (st, [C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_int), P(C.c_int), P(C.c_int)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _check(status, handle=None):
+    if status != PD_OK:
+        lib = library(False)
+        msg = lib.pd_last_error_message(handle)
+        raise PdError(status, msg.decode() if msg else "")
+
+
+def default_options() -> SolverOptions:
+    o = SolverOptions()
+    _check(library().pd_solver_options_default(C.byref(o)))
+    return o
+
+
+def sample_stretch_limits(s0: float, n: int) -> np.ndarray:
+    out = np.zeros(n, np.float64)
+    _check(library().pd_sample_stretch_limits(C.c_float(s0), n, out.ctypes.data_as(C.POINTER(C.c_double))))
+    return out
+
+
+def adaptive_decide(has_broken, ticks, substep, ticks_base=128, ticks_min=100, max_substep=10):
+    t, s, rb = C.c_int(ticks), C.c_int(substep), C.c_int(0)
+    _check(library().pd_adaptive_decide(int(has_broken), ticks_base, ticks_min, max_substep,
+                                        C.byref(t), C.byref(s), C.byref(rb)))
+    return t.value, s.value, bool(rb.value)
+
+
+class SystemParameter:
+    """SystemParameter (src/core/parameters.h:146-162)."""
+
+    def __init__(self, param_file: str | None = None):
+        self._sim = SimulationParameters()
+        self._run = RunningParameters()
+        lib = library()
+        if param_file is None:
+            _check(lib.pd_params_default(C.byref(self._sim), C.byref(self._run)))
+        else:
+            _check(lib.pd_params_load(param_file.encode(), C.byref(self._sim), C.byref(self._run)))
+
+    def derive(self):
+        """calculateDependentParameters, for parameters set in code."""
+        _check(library().pd_params_derive(C.byref(self._sim), C.byref(self._run)))
+
+    def getSimulationParameters(self) -> SimulationParameters:
+        return self._sim
+
+    def getRunningParameters(self) -> RunningParameters:
+        return self._run
+
+
+class Simulator:
+    """Simulator (src/core/simulator.h:32-57) over the C ABI.
+
+    As in the reference, the caller fills the host arrays returned by
+    get_pd_position / get_pd_velocity / get_pd_activity before makeReady().
+    """
+
+    def __init__(self, deviceID: int, simParams: SimulationParameters, runningParams: RunningParameters,
+                 options: SolverOptions | None = None):
+        self.lib = library()
+        self.sim = simParams
+        self.run = runningParams
+        self.run.gpu_device = deviceID
+        self.options = options if options is not None else default_options()
+        self.n = int(simParams.num_pd_particle)
+        h = C.c_void_p()
+        _check(self.lib.pd_create(C.byref(self.sim), C.byref(self.run), C.byref(self.options), C.byref(h)))
+        self.h = h
+        self._pos = np.zeros((self.n, 4), np.float64)
+        self._vel = np.zeros((self.n, 4), np.float64)
+        self._act = np.zeros(self.n, np.int32)
+        self._s0 = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pd_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # host arrays filled by the caller before makeReady (examples/main.cpp:64-66)
+    def get_pd_position(self) -> np.ndarray:
+        return self._pos
+
+    def get_pd_velocity(self) -> np.ndarray:
+        return self._vel
+
+    def get_pd_activity(self) -> np.ndarray:
+        return self._act
+
+    def set_stretch_limits(self, s0):
+        self._s0 = np.ascontiguousarray(s0, np.float64)
+
+    def makeReady(self):
+        dp = C.POINTER(C.c_double)
+        pos = np.ascontiguousarray(self._pos, np.float64)
+        vel = np.ascontiguousarray(self._vel, np.float64)
+        act = np.ascontiguousarray(self._act, np.int32)
+        _check(self.lib.pd_set_particles(self.h, pos.ctypes.data_as(dp), vel.ctypes.data_as(dp),
+                                         act.ctypes.data_as(C.POINTER(C.c_int32)), self.n), self.h)
+        if self._s0 is not None:
+            _check(self.lib.pd_set_stretch_limits(self.h, self._s0.ctypes.data_as(dp), self.n), self.h)
+        _check(self.lib.pd_make_ready(self.h), self.h)
+
+    def advance(self, nsteps: int = 1):
+        _check(self.lib.pd_advance(self.h, int(nsteps)), self.h)
+
+    def finished(self) -> bool:
+        v = C.c_int()
+        _check(self.lib.pd_finished(self.h, C.byref(v)), self.h)
+        return bool(v.value)
+
+    def CGConvergence(self) -> bool:
+        v = C.c_int()
+        _check(self.lib.pd_cg_converged(self.h, C.byref(v)), self.h)
+        return bool(v.value)
+
+    def get_current_step(self) -> int:
+        v = C.c_int()
+        _check(self.lib.pd_get_current_step(self.h, C.byref(v)), self.h)
+        return v.value
+
+    # exports (MemoryManager::downloadFromDevice equivalents)
+    def get(self, var: int) -> np.ndarray:
+        size = C.c_size_t()
+        _check(self.lib.pd_get_size(self.h, var, C.byref(size)), self.h)
+        if var in (VAR_ACTIVITY, VAR_BOND_COUNT, VAR_BOND_LIST):
+            out = np.zeros(size.value // 4, np.int32)
+        elif var == VAR_BOND_ROW_PTR:
+            out = np.zeros(size.value // 8, np.int64)
+        else:
+            out = np.zeros(size.value // 8, np.float64)
+        _check(self.lib.pd_get(self.h, var, out.ctypes.data_as(C.c_void_p), size.value), self.h)
+        if var in (VAR_POSITION, VAR_VELOCITY, VAR_FORCE, VAR_SOLUTION, VAR_POSITION_SCALED, VAR_ORIGINAL_POSITION):
+            out = out.reshape(self.n, 4)
+        return out
+
+    def downloadFromDevice(self, var: int) -> np.ndarray:
+        """Refresh the host array like MemoryManager::downloadFromDevice
+        (positions are multiplied by scaleFactor, memory_manager.cu:274-298)."""
+        if var == VAR_POSITION:
+            self._pos[:] = self.get(VAR_POSITION_SCALED)
+            return self._pos
+        if var == VAR_VELOCITY:
+            self._vel[:] = self.get(VAR_VELOCITY)
+            return self._vel
+        return self.get(var)
+
+    def bond_rows(self):
+        """Per particle (caller order): sorted live neighbours, sorted broken ones."""
+        rp = self.get(VAR_BOND_ROW_PTR)
+        bl = self.get(VAR_BOND_LIST)
+        cnt = self.get(VAR_BOND_COUNT)
+        return rp, bl, cnt
+
+    def alive_sets(self):
+        rp, bl, cnt = self.bond_rows()
+        return [bl[rp[i]:rp[i] + cnt[i]] for i in range(self.n)]
+
+    def stats(self) -> StepStats:
+        s = StepStats()
+        _check(self.lib.pd_get_stats(self.h, C.byref(s)), self.h)
+        return s
+
+    def params(self):
+        s, r, o = SimulationParameters(), RunningParameters(), SolverOptions()
+        _check(self.lib.pd_get_params(self.h, C.byref(s), C.byref(r), C.byref(o)), self.h)
+        return s, r, o
+
+    def set_profiling(self, on: bool):
+        _check(self.lib.pd_set_profiling(self.h, 1 if on else 0), self.h)
+
+    def kernel_times(self):
+        t = KernelTimes()
+        _check(self.lib.pd_get_kernel_times(self.h, C.byref(t)), self.h)
+        return {KC_NAMES[k]: (t.launches[k], t.total_ms[k]) for k in range(4)}
+
+    def reset_kernel_times(self):
+        _check(self.lib.pd_reset_kernel_times(self.h), self.h)
+
+    def launch_count(self) -> int:
+        v = C.c_longlong()
+        _check(self.lib.pd_get_launch_count(self.h, C.byref(v)), self.h)
+        return v.value

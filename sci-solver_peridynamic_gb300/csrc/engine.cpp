@@ -1,0 +1,659 @@
+// engine.cpp -- host driver of the GB300 PD step.
+//
+// Mirrors Simulator (src/core/simulator.cu): makeReady (:56-89), advance
+// (:1159-1182), integratePeridynamicsImplicitEuler/NewmarkBeta (:297-652)
+// including the adaptive time-step rollback (:332-401, :506-572), and
+// solveLinearSystem (:735-799).  Differences by design:
+//  * bonds are built on the GPU (bonds.cu) instead of the host kd-tree;
+//  * particles live in cell-sorted slots; exports map back to caller order;
+//  * the CG runs on the device: its scalars never leave the GPU inside an
+//    iteration; the host reads one small record every few iterations;
+//  * errors are returned as pd_status instead of exit().
+#include "engine.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace pdgb {
+
+#define CK(call, what)                                   \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+template <typename T>
+static cudaError_t dalloc(T** p, size_t count)
+{
+    *p = nullptr;
+    if (count == 0) count = 1;
+    return cudaMalloc((void**)p, sizeof(T) * count);
+}
+
+Engine::Engine(const pd_sim_params& sim, const pd_run_params& run, const pd_solver_options& opt)
+    : sim_(sim), run_(run), opt_(opt)
+{
+    fp64_ = opt_.precision == PD_PRECISION_FP64;
+    device_ = run_.gpu_device;
+    n_ = sim_.num_pd_particle;
+    ticks_ = sim_.pd_time_step;
+    clock_scale_ = opt_.phase_in_steps > 0 ? sim_.clockScale : 1.0;
+    // the reference evaluates pd_C_times_V * PD_K inside the kernel (cg_solver.cuh:299,325)
+    bond_coeff_ = opt_.bond_stiffness > 0 ? opt_.bond_stiffness : sim_.pd_C_times_V * opt_.pd_k;
+}
+
+Engine::~Engine()
+{
+    if (device_ >= 0) cudaSetDevice(device_);
+    free_all();
+    for (cudaEvent_t e : event_pool_) cudaEventDestroy(e);
+    for (Mark& m : marks_) {
+        cudaEventDestroy(m.a);
+        cudaEventDestroy(m.b);
+    }
+    if (h_sc_) cudaFreeHost(h_sc_);
+    if (h_flags_) cudaFreeHost(h_flags_);
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+pd_status Engine::cuda_fail(cudaError_t e, const char* what)
+{
+    err_ = std::string(what) + ": " + cudaGetErrorString(e);
+    cudaGetLastError();
+    if (e == cudaErrorMemoryAllocation) return PD_ERR_OUT_OF_MEMORY;
+    if (e == cudaErrorNoDevice || e == cudaErrorInvalidDevice || e == cudaErrorInsufficientDriver)
+        return PD_ERR_NO_DEVICE;
+    return PD_ERR_CUDA;
+}
+
+pd_status Engine::init_device()
+{
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        err_ = "no CUDA device";
+        cudaGetLastError();
+        return PD_ERR_NO_DEVICE;
+    }
+    if (device_ < 0 || device_ >= count) {
+        err_ = "gpu_device out of range";
+        return PD_ERR_NO_DEVICE;
+    }
+    CK(cudaSetDevice(device_), "cudaSetDevice");
+    CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+    CK(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, device_), "device attribute");
+    CK(cudaMallocHost((void**)&h_sc_, sizeof(CgScalars)), "cudaMallocHost");
+    CK(cudaMallocHost((void**)&h_flags_, sizeof(int) * 4), "cudaMallocHost");
+    std::memset(h_sc_, 0, sizeof(CgScalars));
+    return PD_OK;
+}
+
+pd_status Engine::set_particles(const double* pos4, const double* vel4, const int32_t* act, int n)
+{
+    if (n != n_ || n < 0 || (n > 0 && !pos4)) {
+        err_ = "set_particles: n must equal num_pd_particle";
+        return PD_ERR_INVALID_ARGUMENT;
+    }
+    h_pos_.assign(pos4, pos4 + 4 * (size_t)n);
+    if (vel4) h_vel_.assign(vel4, vel4 + 4 * (size_t)n);
+    else h_vel_.assign(4 * (size_t)n, 0.0);
+    if (act) {
+        h_act_.assign(act, act + n);
+        for (int i = 0; i < n; ++i)
+            if (h_act_[i] < 0 || h_act_[i] > PD_PRESCRIBED) {
+                err_ = "set_particles: activity code out of range";
+                return PD_ERR_INVALID_ARGUMENT;
+            }
+    } else {
+        h_act_.assign(n, PD_ACTIVE);
+    }
+    for (int i = 0; i < 4 * n; ++i)
+        if (!std::isfinite(h_pos_[i]) || !std::isfinite(h_vel_[i])) {
+            err_ = "set_particles: non-finite position or velocity";
+            return PD_ERR_INVALID_ARGUMENT;
+        }
+    particles_set_ = true;
+    ready_ = false;
+    return PD_OK;
+}
+
+pd_status Engine::set_stretch(const double* s0, int n)
+{
+    if (n != n_ || (n > 0 && !s0)) return PD_ERR_INVALID_ARGUMENT;
+    h_s0_.assign(s0, s0 + n);
+    stretch_set_ = true;
+    ready_ = false;
+    return PD_OK;
+}
+
+void Engine::free_all()
+{
+    void* ptrs[] = {S_.act, S_.x64, S_.v64, S_.X64, S_.x64_bk, S_.v64_bk, S_.st, S_.ost, S_.nst, S_.row_ptr,
+                    S_.cnt, S_.cnt_bk, S_.col, S_.X32, S_.u32, S_.jac, S_.jdiag, S_.force, S_.rhs, S_.sol,
+                    S_.r, S_.p, S_.y, S_.sc, S_.partials, S_.counters, S_.flags, d_perm_};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    S_ = DeviceState{};
+    d_perm_ = nullptr;
+}
+
+pd_status Engine::allocate()
+{
+    const size_t n = (size_t)n_;
+    const size_t r4 = fp64_ ? sizeof(dbl4) : sizeof(float4);
+    S_.n = n_;
+    CK(dalloc(&S_.act, n), "alloc act");
+    CK(dalloc(&S_.x64, n), "alloc x");
+    CK(dalloc(&S_.v64, n), "alloc v");
+    CK(dalloc(&S_.X64, n), "alloc X");
+    CK(dalloc(&S_.x64_bk, n), "alloc x backup");
+    CK(dalloc(&S_.v64_bk, n), "alloc v backup");
+    CK(dalloc(&S_.st, n), "alloc stretch");
+    CK(dalloc(&S_.ost, n), "alloc original stretch");
+    CK(dalloc(&S_.nst, n), "alloc new stretch");
+    CK(dalloc(&S_.row_ptr, n + 1), "alloc row_ptr");
+    CK(dalloc(&S_.cnt, n), "alloc cnt");
+    CK(dalloc(&S_.cnt_bk, n), "alloc cnt backup");
+    CK(dalloc(&S_.X32, n), "alloc X32");
+    CK(dalloc(&S_.u32, n), "alloc u32");
+    void** vecs[] = {&S_.force, &S_.rhs, &S_.sol, &S_.r, &S_.p, &S_.y};
+    for (void** v : vecs) {
+        CK(cudaMalloc(v, r4 * (n ? n : 1)), "alloc vector");
+        CK(cudaMemsetAsync(*v, 0, r4 * (n ? n : 1), stream_), "memset vector");
+    }
+    if (fp64_) CK(dalloc(&S_.jdiag, 6 * n), "alloc jdiag");
+    CK(dalloc(&S_.sc, 1), "alloc scalars");
+    CK(dalloc(&S_.partials, (size_t)kMaxPartials), "alloc partials");
+    CK(dalloc(&S_.counters, 8), "alloc counters");
+    CK(dalloc(&S_.flags, 4), "alloc flags");
+    CK(cudaMemsetAsync(S_.counters, 0, sizeof(unsigned) * 8, stream_), "memset counters");
+    CK(cudaMemsetAsync(S_.flags, 0, sizeof(int) * 4, stream_), "memset flags");
+    CK(cudaMemsetAsync(S_.u32, 0, sizeof(float4) * (n ? n : 1), stream_), "memset u32");
+    return PD_OK;
+}
+
+pd_status Engine::make_ready()
+{
+    if (!particles_set_) {
+        err_ = "make_ready: particles not set";
+        return PD_ERR_NOT_READY;
+    }
+    CK(cudaSetDevice(device_), "cudaSetDevice");
+    ready_ = false;
+    free_all();
+    pd_status s = allocate();
+    if (s != PD_OK) return s;
+    const int n = n_;
+    const size_t N = (size_t)n;
+
+    struct Tmp {   // staging buffers in caller order, freed on every return path
+        dbl4* pos = nullptr;
+        double* s0 = nullptr;
+        int* act = nullptr;
+        ~Tmp() { cudaFree(pos); cudaFree(s0); cudaFree(act); }
+    } tmp;
+    CK(dalloc(&tmp.pos, N), "alloc tmp");
+    CK(dalloc(&tmp.s0, N), "alloc tmp");
+    CK(dalloc(&tmp.act, N), "alloc tmp");
+    dbl4* d_tmp4 = tmp.pos;
+    double* d_tmp1 = tmp.s0;
+    int* d_tmpi = tmp.act;
+
+    // bonds (replaces initPeridynamicsBonds' kd-tree, simulator.cu:825-943)
+    if (n > 0) CK(cudaMemcpyAsync(d_tmp4, h_pos_.data(), sizeof(dbl4) * N, cudaMemcpyHostToDevice, stream_), "upload pos");
+    BondBuildOut out{};
+    out.row_ptr = S_.row_ptr;
+    out.cnt = S_.cnt;
+    CK(build_bonds(d_tmp4, n, sim_.pd_horizon, opt_.max_bonds_per_particle, S_.x64, S_.X32, origin_, &out, stream_),
+       "build_bonds");
+    d_perm_ = out.perm;
+    S_.col = out.col;
+    if (out.overflow) {
+        err_ = out.overflow == 2 ? "bond list exceeds 2^31 slots"
+                                 : "a particle has more bonds than max_bonds_per_particle";
+        sim_.pd_max_num_bonds = out.max_bonds;
+        return PD_ERR_BOND_OVERFLOW;
+    }
+    if (n == 0) {
+        CK(dalloc(&d_perm_, 1), "alloc perm");
+        CK(dalloc(&S_.col, 8), "alloc col");
+    }
+    total_slots_ = out.total;
+    bonds_initial_ = out.bonds;
+    sim_.pd_max_num_bonds = out.max_bonds;
+    if (n > 0) {
+        CK(cudaMemcpyAsync(S_.X64, S_.x64, sizeof(dbl4) * N, cudaMemcpyDeviceToDevice, stream_), "copy X");
+        CK(cudaMemcpyAsync(d_tmp4, h_vel_.data(), sizeof(dbl4) * N, cudaMemcpyHostToDevice, stream_), "upload v");
+        gather_double4(d_tmp4, d_perm_, S_.v64, n, stream_);
+        CK(cudaMemcpyAsync(d_tmpi, h_act_.data(), sizeof(int) * N, cudaMemcpyHostToDevice, stream_), "upload act");
+        gather_int_to_u8(d_tmpi, d_perm_, S_.act, n, stream_);
+        // s0_i = getstretch(s0) after srand(1973), in caller order (simulator.cu:852-857)
+        std::vector<double> s0 = h_s0_;
+        if (!stretch_set_) {
+            s0.assign(N, 0.0);
+            pd_sample_stretch_limits(run_.pd_stretch_limit_s0, n, s0.data());
+        }
+        CK(cudaMemcpyAsync(d_tmp1, s0.data(), sizeof(double) * N, cudaMemcpyHostToDevice, stream_), "upload s0");
+        gather_double(d_tmp1, d_perm_, S_.ost, n, stream_);
+        CK(cudaMemcpyAsync(S_.st, S_.ost, sizeof(double) * N, cudaMemcpyDeviceToDevice, stream_), "copy st");
+        CK(cudaMemcpyAsync(S_.nst, S_.ost, sizeof(double) * N, cudaMemcpyDeviceToDevice, stream_), "copy nst");
+        CK(cudaMemcpyAsync(S_.cnt_bk, S_.cnt, sizeof(int) * N, cudaMemcpyDeviceToDevice, stream_), "backup cnt");
+        CK(cudaMemcpyAsync(S_.x64_bk, S_.x64, sizeof(dbl4) * N, cudaMemcpyDeviceToDevice, stream_), "backup x");
+        CK(cudaMemcpyAsync(S_.v64_bk, S_.v64, sizeof(dbl4) * N, cudaMemcpyDeviceToDevice, stream_), "backup v");
+        launches_ += 3;
+    }
+    if (fp64_) {
+        CK(dalloc(&S_.jac, 6 * (size_t)std::max<long long>(total_slots_, 1)), "alloc jac");
+    }
+    // CG scalars (initPDSolutions zeroed the solution, cg_solver.cuh:184-194)
+    std::memset(h_sc_, 0, sizeof(CgScalars));
+    h_sc_->rel_tol = opt_.cg_relative_tolerance;
+    h_sc_->max_iter = opt_.cg_max_iterations;
+    CK(cudaMemcpyAsync(S_.sc, h_sc_, sizeof(CgScalars), cudaMemcpyHostToDevice, stream_), "upload scalars");
+    // host copies of the slot permutation and the initial row lengths
+    perm_.assign(N, 0);
+    inv_.assign(N, 0);
+    cnt_init_.assign(N, 0);
+    if (n > 0) {
+        CK(cudaMemcpyAsync(perm_.data(), d_perm_, sizeof(int) * N, cudaMemcpyDeviceToHost, stream_), "download perm");
+        CK(cudaMemcpyAsync(cnt_init_.data(), S_.cnt, sizeof(int) * N, cudaMemcpyDeviceToHost, stream_), "download cnt");
+    }
+    CK(cudaStreamSynchronize(stream_), "make_ready sync");
+    for (int i = 0; i < n; ++i) inv_[perm_[i]] = i;
+    // launch geometry
+    int lanes = opt_.lanes_per_particle;
+    if (lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32) lanes = 8;
+    L_.lanes = lanes;
+    const int bpsm = row_kernel_blocks_per_sm(fp64_, lanes);
+    const long long need_rows = ((long long)n + (kBlock / lanes) - 1) / (kBlock / lanes);
+    L_.grid_bonds = (int)std::max<long long>(1, std::min<long long>({need_rows, (long long)sm_count_ * bpsm, (long long)kMaxPartials}));
+    const long long need_vec = ((long long)n + kBlock - 1) / kBlock;
+    L_.grid_vec = (int)std::max<long long>(1, std::min<long long>({need_vec, (long long)sm_count_ * 8, (long long)kMaxPartials}));
+    // step state
+    step_ = 0;
+    substep_ = 0;
+    ticks_ = sim_.pd_time_step;
+    clock_scale_ = opt_.phase_in_steps > 0 ? 0.0 : 1.0;
+    sim_time_ = 0.0;
+    cg_converged_ = true;
+    last_iters_ = 0;
+    total_iters_ = 0;
+    predicted_iters_ = 0;
+    ready_ = true;
+    return PD_OK;
+}
+
+StepParams Engine::step_params() const
+{
+    StepParams P{};
+    P.n = n_;
+    P.integrator = run_.integrator;
+    P.ticks = ticks_;
+    P.box_enabled = opt_.box_enabled;
+    P.sphere_on = opt_.sphere_enabled;
+    P.cs = clock_scale_;
+    P.bond_coeff = bond_coeff_;
+    P.horizon = sim_.pd_horizon;
+    P.radius = sim_.pd_particle_radius;
+    P.vs_threshold = sim_.pd_horizon - sim_.pd_particle_radius;
+    P.mass = sim_.pd_particle_mass;
+    P.dt_base = opt_.time_step_base;
+    P.h = ticks_ * opt_.time_step_base;
+    P.t2 = run_.integrator == PD_IMPLICIT_EULER ? P.h * P.h : (P.h * P.h) / 4.0;
+    for (int k = 0; k < 3; ++k) P.gravity[k] = opt_.gravity[k];
+    P.stretch_a = opt_.stretch_a;
+    P.stretch_b = opt_.stretch_b;
+    P.alpha = opt_.alpha;
+    P.bmin[0] = sim_.boundary_min_x; P.bmin[1] = sim_.boundary_min_y; P.bmin[2] = sim_.boundary_min_z;
+    P.bmax[0] = sim_.boundary_max_x; P.bmax[1] = sim_.boundary_max_y; P.bmax[2] = sim_.boundary_max_z;
+    P.restitution = opt_.restitution;
+    for (int k = 0; k < 3; ++k) {
+        P.sphere_c[k] = opt_.sphere_center[k] + opt_.sphere_velocity[k] * sim_time_;
+        P.sphere_c_local[k] = P.sphere_c[k] - origin_[k];
+    }
+    P.sphere_r = opt_.sphere_radius;
+    P.sphere_k = opt_.sphere_stiffness;
+    return P;
+}
+
+bool Engine::finished() const { return step_ > run_.final_step || !cg_converged_; }
+
+pd_status Engine::advance(int nsteps)
+{
+    if (!ready_) {
+        err_ = "advance: make_ready has not run";
+        return PD_ERR_NOT_READY;
+    }
+    if (nsteps < 0) return PD_ERR_INVALID_ARGUMENT;
+    CK(cudaSetDevice(device_), "cudaSetDevice");
+    for (int k = 0; k < nsteps; ++k) {
+        if (!cg_converged_) break;
+        ++step_;
+        if (step_ <= opt_.phase_in_steps) clock_scale_ = (double)step_ / (double)opt_.phase_in_steps;
+        retries_ = 0;
+        for (;;) {
+            bool advanced = false;
+            pd_status s = integrate(&advanced);
+            if (s != PD_OK) return s;
+            if (advanced) break;
+            if (++retries_ > 64) {
+                err_ = "adaptive time step: too many rollbacks";
+                return PD_ERR_STATE;
+            }
+        }
+    }
+    return PD_OK;
+}
+
+pd_status Engine::integrate(bool* advanced)
+{
+    *advanced = false;
+    const StepParams P = step_params();
+    const size_t N = (size_t)n_;
+    CK(cudaMemsetAsync(S_.flags, 0, sizeof(int) * 2, stream_), "memset flags");
+    mark_begin(PD_KC_FORCE, -1);
+    launch_force(fp64_, P, S_, L_, stream_);
+    mark_end();
+    ++launches_;
+    const bool adaptive = run_.integrator == PD_NEWMARK_BETA || run_.adaptive_integration != 0;
+    if (adaptive) {
+        CK(cudaMemcpyAsync(h_flags_, S_.flags, sizeof(int) * 2, cudaMemcpyDeviceToHost, stream_), "read flag");
+        CK(cudaStreamSynchronize(stream_), "step sync");
+        int rollback = 0;
+        pd_adaptive_decide(h_flags_[0], sim_.pd_time_step, opt_.time_step_min, opt_.max_substep, &ticks_, &substep_,
+                           &rollback);
+        if (rollback) {
+            // restoreBondListTopIndex / restorePDPosition / restorePDVelocity (memory_manager.cu:500-550)
+            CK(cudaMemcpyAsync(S_.cnt, S_.cnt_bk, sizeof(int) * N, cudaMemcpyDeviceToDevice, stream_), "restore cnt");
+            CK(cudaMemcpyAsync(S_.x64, S_.x64_bk, sizeof(dbl4) * N, cudaMemcpyDeviceToDevice, stream_), "restore x");
+            CK(cudaMemcpyAsync(S_.v64, S_.v64_bk, sizeof(dbl4) * N, cudaMemcpyDeviceToDevice, stream_), "restore v");
+            launch_refresh(fp64_, P, S_, L_, stream_);
+            ++launches_;
+            return PD_OK;
+        }
+        CK(cudaMemcpyAsync(S_.cnt_bk, S_.cnt, sizeof(int) * N, cudaMemcpyDeviceToDevice, stream_), "backup cnt");
+        CK(cudaMemcpyAsync(S_.x64_bk, S_.x64, sizeof(dbl4) * N, cudaMemcpyDeviceToDevice, stream_), "backup x");
+        CK(cudaMemcpyAsync(S_.v64_bk, S_.v64, sizeof(dbl4) * N, cudaMemcpyDeviceToDevice, stream_), "backup v");
+    }
+    pd_status s = solve(P);
+    if (s != PD_OK) return s;
+    mark_begin(PD_KC_UPDATE, -1);
+    launch_update(fp64_, P, S_, L_, stream_);
+    mark_end();
+    ++launches_;
+    CK(cudaGetLastError(), "step launch");
+    sim_time_ += P.h;
+    *advanced = true;
+    return PD_OK;
+}
+
+pd_status Engine::solve(const StepParams& P)
+{
+    launch_cg_init(fp64_, P, S_, L_, stream_);
+    launch_spmv(fp64_, false, P, S_, L_, stream_);
+    launch_cg_residual(fp64_, P, S_, L_, stream_);
+    launches_ += 3;
+    const int check = opt_.cg_check_interval > 0 ? opt_.cg_check_interval : 8;
+    int batch = predicted_iters_ > 0 ? predicted_iters_ : check;
+    int launched = 0;
+    for (;;) {
+        for (int k = 0; k < batch; ++k) {
+            mark_begin(PD_KC_SPMV, launched);
+            launch_spmv(fp64_, true, P, S_, L_, stream_);
+            mark_end();
+            mark_begin(PD_KC_CG_VECTOR, launched);
+            launch_cg_axpy(fp64_, P, S_, L_, stream_);
+            launch_cg_xpby(fp64_, P, S_, L_, stream_);
+            mark_end();
+            ++launched;
+        }
+        launches_ += 3LL * batch;
+        CK(cudaGetLastError(), "cg launch");
+        CK(cudaMemcpyAsync(h_sc_, S_.sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, stream_), "read cg scalars");
+        CK(cudaStreamSynchronize(stream_), "cg sync");
+        if (h_sc_->done) break;
+        if (launched > opt_.cg_max_iterations + 2 * check) {
+            err_ = "cg: iteration count not advancing";
+            return PD_ERR_STATE;
+        }
+        batch = std::max(check, launched / 8);
+    }
+    last_iters_ = h_sc_->iter;
+    last_res_ = h_sc_->rnorm;
+    last_tol_ = h_sc_->tol;
+    total_iters_ += last_iters_;
+    predicted_iters_ = std::max(1, last_iters_);
+    flush_marks(last_iters_);
+    if (!h_sc_->converged) cg_converged_ = false;
+    return PD_OK;
+}
+
+// ---- profiling -------------------------------------------------------------------
+cudaEvent_t Engine::take_event()
+{
+    if (!event_pool_.empty()) {
+        cudaEvent_t e = event_pool_.back();
+        event_pool_.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+void Engine::mark_begin(int kc, int iter)
+{
+    if (!profiling_) return;
+    Mark m{kc, iter, take_event(), take_event()};
+    cudaEventRecord(m.a, stream_);
+    marks_.push_back(m);
+    open_mark_ = (int)marks_.size() - 1;
+}
+
+void Engine::mark_end()
+{
+    if (!profiling_ || open_mark_ < 0) return;
+    cudaEventRecord(marks_[open_mark_].b, stream_);
+    open_mark_ = -1;
+}
+
+// Accumulates completed marks.  SpMV / CG-vector marks of iterations at or
+// beyond `live_iters` were launches that returned immediately after
+// convergence and are dropped.  live_iters < 0 keeps all.
+void Engine::flush_marks(int live_iters)
+{
+    if (marks_.empty()) return;
+    cudaStreamSynchronize(stream_);
+    for (Mark& m : marks_) {
+        const bool dead = live_iters >= 0 && m.iter >= live_iters &&
+                          (m.kc == PD_KC_SPMV || m.kc == PD_KC_CG_VECTOR);
+        if (!dead) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, m.a, m.b) == cudaSuccess) {
+                kc_ms_[m.kc] += ms;
+                kc_launches_[m.kc] += (m.kc == PD_KC_CG_VECTOR) ? 2 : 1;
+            }
+        }
+        event_pool_.push_back(m.a);
+        event_pool_.push_back(m.b);
+    }
+    marks_.clear();
+    open_mark_ = -1;
+}
+
+pd_status Engine::kernel_times(pd_kernel_times* t)
+{
+    // CG marks were filtered when their solve ended; what is left is complete work
+    flush_marks(-1);
+    for (int k = 0; k < PD_KC_COUNT; ++k) {
+        t->launches[k] = kc_launches_[k];
+        t->total_ms[k] = kc_ms_[k];
+    }
+    return PD_OK;
+}
+
+void Engine::reset_kernel_times()
+{
+    flush_marks(-1);
+    for (int k = 0; k < PD_KC_COUNT; ++k) {
+        kc_launches_[k] = 0;
+        kc_ms_[k] = 0.0;
+    }
+}
+
+// ---- exports -----------------------------------------------------------------------
+template <typename T>
+pd_status Engine::download_scatter(const T* dev, T* host_out, size_t per, size_t count)
+{
+    std::vector<T> tmp(per * count);
+    if (count) CK(cudaMemcpyAsync(tmp.data(), dev, sizeof(T) * per * count, cudaMemcpyDeviceToHost, stream_), "download");
+    CK(cudaStreamSynchronize(stream_), "download sync");
+    for (size_t i = 0; i < count; ++i)
+        for (size_t j = 0; j < per; ++j) host_out[(size_t)perm_[i] * per + j] = tmp[i * per + j];
+    return PD_OK;
+}
+
+pd_status Engine::export_vec4(const void* dev, bool is_float, double* dst)
+{
+    const size_t N = (size_t)n_;
+    if (is_float) {
+        std::vector<float> tmp(4 * N);
+        if (N) CK(cudaMemcpyAsync(tmp.data(), dev, sizeof(float) * 4 * N, cudaMemcpyDeviceToHost, stream_), "download");
+        CK(cudaStreamSynchronize(stream_), "download sync");
+        for (size_t i = 0; i < N; ++i) {
+            double* o = dst + 4 * (size_t)perm_[i];
+            o[0] = tmp[4 * i]; o[1] = tmp[4 * i + 1]; o[2] = tmp[4 * i + 2]; o[3] = 0.0;
+        }
+        return PD_OK;
+    }
+    pd_status s = download_scatter((const double*)dev, dst, 4, N);
+    if (s != PD_OK) return s;
+    for (size_t i = 0; i < N; ++i) dst[4 * i + 3] = 0.0;
+    return PD_OK;
+}
+
+pd_status Engine::export_bonds(int64_t* rp_out, int32_t* list_out)
+{
+    const size_t N = (size_t)n_;
+    std::vector<int> rp(N + 1), cnt(N), col((size_t)std::max<long long>(total_slots_, 1));
+    CK(cudaMemcpyAsync(rp.data(), S_.row_ptr, sizeof(int) * (N + 1), cudaMemcpyDeviceToHost, stream_), "download rp");
+    if (N) CK(cudaMemcpyAsync(cnt.data(), S_.cnt, sizeof(int) * N, cudaMemcpyDeviceToHost, stream_), "download cnt");
+    if (total_slots_ > 0)
+        CK(cudaMemcpyAsync(col.data(), S_.col, sizeof(int) * (size_t)total_slots_, cudaMemcpyDeviceToHost, stream_),
+           "download col");
+    CK(cudaStreamSynchronize(stream_), "download sync");
+    int64_t pos = 0;
+    if (rp_out) rp_out[0] = 0;
+    for (size_t o = 0; o < N; ++o) {
+        const int s = inv_[o];
+        const int base = rp[s], live = cnt[s], all = cnt_init_[s];
+        if (list_out) {
+            int32_t* row = list_out + pos;
+            for (int j = 0; j < all; ++j) row[j] = perm_[col[base + j]];
+            std::sort(row, row + live);
+            std::sort(row + live, row + all);
+        }
+        pos += all;
+        if (rp_out) rp_out[o + 1] = pos;
+    }
+    return PD_OK;
+}
+
+pd_status Engine::get_size(pd_variable var, size_t* bytes) const
+{
+    const size_t N = (size_t)n_;
+    switch (var) {
+    case PD_VAR_POSITION: case PD_VAR_VELOCITY: case PD_VAR_FORCE: case PD_VAR_SOLUTION:
+    case PD_VAR_POSITION_SCALED: case PD_VAR_ORIGINAL_POSITION:
+        *bytes = 4 * N * sizeof(double); return PD_OK;
+    case PD_VAR_ACTIVITY: case PD_VAR_BOND_COUNT: *bytes = N * sizeof(int32_t); return PD_OK;
+    case PD_VAR_STRETCH: case PD_VAR_ORIGINAL_STRETCH: case PD_VAR_NEW_STRETCH: *bytes = N * sizeof(double); return PD_OK;
+    case PD_VAR_BOND_ROW_PTR: *bytes = (N + 1) * sizeof(int64_t); return PD_OK;
+    case PD_VAR_BOND_LIST: *bytes = (size_t)bonds_initial_ * sizeof(int32_t); return PD_OK;
+    }
+    return PD_ERR_INVALID_ARGUMENT;
+}
+
+pd_status Engine::get(pd_variable var, void* dst, size_t bytes)
+{
+    size_t need = 0;
+    if (get_size(var, &need) != PD_OK) return PD_ERR_INVALID_ARGUMENT;
+    if (!dst && need > 0) return PD_ERR_INVALID_ARGUMENT;
+    if (bytes < need) {
+        err_ = "pd_get: destination too small";
+        return PD_ERR_INVALID_ARGUMENT;
+    }
+    if (var == PD_VAR_ACTIVITY) {
+        if (!particles_set_) return PD_ERR_NOT_READY;
+        std::memcpy(dst, h_act_.data(), need);
+        return PD_OK;
+    }
+    if (!ready_) {
+        err_ = "pd_get: make_ready has not run";
+        return PD_ERR_NOT_READY;
+    }
+    CK(cudaSetDevice(device_), "cudaSetDevice");
+    const size_t N = (size_t)n_;
+    switch (var) {
+    case PD_VAR_POSITION:
+    case PD_VAR_POSITION_SCALED: {
+        pd_status s = download_scatter((const double*)S_.x64, (double*)dst, 4, N);
+        if (s != PD_OK) return s;
+        if (var == PD_VAR_POSITION_SCALED)
+            for (size_t i = 0; i < N; ++i)
+                for (int k = 0; k < 3; ++k) ((double*)dst)[4 * i + k] *= sim_.scaleFactor;
+        return PD_OK;
+    }
+    case PD_VAR_ORIGINAL_POSITION: return download_scatter((const double*)S_.X64, (double*)dst, 4, N);
+    case PD_VAR_VELOCITY: return download_scatter((const double*)S_.v64, (double*)dst, 4, N);
+    case PD_VAR_FORCE: return export_vec4(S_.force, !fp64_, (double*)dst);
+    case PD_VAR_SOLUTION: return export_vec4(S_.sol, !fp64_, (double*)dst);
+    case PD_VAR_BOND_COUNT: return download_scatter(S_.cnt, (int*)dst, 1, N);
+    case PD_VAR_STRETCH: return download_scatter(S_.st, (double*)dst, 1, N);
+    case PD_VAR_ORIGINAL_STRETCH: return download_scatter(S_.ost, (double*)dst, 1, N);
+    case PD_VAR_NEW_STRETCH: return download_scatter(S_.nst, (double*)dst, 1, N);
+    case PD_VAR_BOND_ROW_PTR: return export_bonds((int64_t*)dst, nullptr);
+    case PD_VAR_BOND_LIST: return export_bonds(nullptr, (int32_t*)dst);
+    default: return PD_ERR_INVALID_ARGUMENT;
+    }
+}
+
+pd_status Engine::stats(pd_step_stats* s) const
+{
+    std::memset(s, 0, sizeof(*s));
+    s->current_step = step_;
+    s->cg_converged = cg_converged_ ? 1 : 0;
+    s->last_cg_iterations = last_iters_;
+    s->last_cg_residual = last_res_;
+    s->last_cg_tolerance = last_tol_;
+    s->total_cg_iterations = total_iters_;
+    s->time_step_ticks = ticks_;
+    s->substep = substep_;
+    s->retries_last_step = retries_;
+    s->bonds_initial = bonds_initial_;
+    s->max_bonds_per_particle = sim_.pd_max_num_bonds;
+    s->clock_scale = clock_scale_;
+    s->sim_time = sim_time_;
+    s->bonds_alive = bonds_initial_;
+    if (ready_ && n_ > 0) {
+        std::vector<int> c((size_t)n_);
+        cudaSetDevice(device_);
+        if (cudaMemcpyAsync(c.data(), S_.cnt, sizeof(int) * (size_t)n_, cudaMemcpyDeviceToHost, stream_) == cudaSuccess &&
+            cudaStreamSynchronize(stream_) == cudaSuccess) {
+            long long a = 0;
+            for (int v : c) a += v;
+            s->bonds_alive = a;
+        }
+    }
+    return PD_OK;
+}
+
+void Engine::params(pd_sim_params* s, pd_run_params* r, pd_solver_options* o) const
+{
+    if (s) *s = sim_;
+    if (r) *r = run_;
+    if (o) *o = opt_;
+}
+
+}  // namespace pdgb

@@ -1,0 +1,106 @@
+// engine.h -- host driver of the GB300 PD step (the Simulator of the reference).
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "pd_gb300.h"
+#include "pd_kernels.h"
+
+namespace pdgb {
+
+class Engine {
+public:
+    Engine(const pd_sim_params& sim, const pd_run_params& run, const pd_solver_options& opt);
+    ~Engine();
+
+    pd_status init_device();
+    pd_status set_particles(const double* pos4, const double* vel4, const int32_t* act, int n);
+    pd_status set_stretch(const double* s0, int n);
+    pd_status make_ready();
+    pd_status advance(int nsteps);
+    bool finished() const;
+    bool cg_converged() const { return cg_converged_; }
+    int current_step() const { return step_; }
+    pd_status get(pd_variable var, void* dst, size_t bytes);
+    pd_status get_size(pd_variable var, size_t* bytes) const;
+    pd_status stats(pd_step_stats* s) const;
+    void params(pd_sim_params* s, pd_run_params* r, pd_solver_options* o) const;
+    void set_profiling(bool on) { profiling_ = on; }
+    pd_status kernel_times(pd_kernel_times* t);
+    void reset_kernel_times();
+    long long launches() const { return launches_; }
+    const std::string& error() const { return err_; }
+
+private:
+    pd_status cuda_fail(cudaError_t e, const char* what);
+    pd_status allocate();
+    void free_all();
+    StepParams step_params() const;
+    pd_status integrate(bool* advanced);
+    pd_status solve(const StepParams& P);
+    template <typename T>
+    pd_status download_scatter(const T* dev, T* host_out, size_t count_per, size_t elem_count);
+    pd_status export_vec4(const void* dev, bool real_is_float, double* dst);
+    pd_status export_bonds(int64_t* row_ptr_out, int32_t* list_out);
+    // profiling
+    struct Mark {
+        int kc;
+        int iter;   // CG iteration index for SpMV marks, -1 otherwise
+        cudaEvent_t a, b;
+    };
+    void mark_begin(int kc, int iter);
+    void mark_end();
+    void flush_marks(int live_iters);
+    cudaEvent_t take_event();
+
+    pd_sim_params sim_;
+    pd_run_params run_;
+    pd_solver_options opt_;
+    bool fp64_ = false;
+    int device_ = 0;
+    cudaStream_t stream_ = nullptr;
+    int sm_count_ = 0;
+    int n_ = 0;
+    bool particles_set_ = false;
+    bool stretch_set_ = false;
+    bool ready_ = false;
+    std::vector<double> h_pos_, h_vel_, h_s0_;
+    std::vector<int32_t> h_act_;
+    std::vector<int> perm_, inv_, cnt_init_;
+    double origin_[3] = {0, 0, 0};
+    double bond_coeff_ = 0;
+    long long total_slots_ = 0;
+    long long bonds_initial_ = 0;
+    DeviceState S_{};
+    int* d_perm_ = nullptr;
+    CgScalars* h_sc_ = nullptr;   // pinned
+    int* h_flags_ = nullptr;      // pinned
+    LaunchCfg L_{};
+    // step state (Simulator members)
+    int step_ = 0;
+    int substep_ = 0;
+    int ticks_ = 0;
+    double clock_scale_ = 0;
+    double sim_time_ = 0;
+    bool cg_converged_ = true;
+    int last_iters_ = 0;
+    double last_res_ = 0;
+    double last_tol_ = 0;
+    long long total_iters_ = 0;
+    int retries_ = 0;
+    int predicted_iters_ = 0;
+    // profiling
+    bool profiling_ = false;
+    std::vector<cudaEvent_t> event_pool_;
+    std::vector<Mark> marks_;
+    int open_mark_ = -1;
+    long long kc_launches_[PD_KC_COUNT] = {0, 0, 0, 0};
+    double kc_ms_[PD_KC_COUNT] = {0, 0, 0, 0};
+    long long launches_ = 0;
+    std::string err_;
+};
+
+}  // namespace pdgb

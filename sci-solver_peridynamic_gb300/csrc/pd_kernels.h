@@ -1,0 +1,149 @@
+// pd_kernels.h -- host-visible interface between the engine and the CUDA kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pdgb {
+
+constexpr int kBlock = 256;          // threads per block of the per-particle kernels
+constexpr int kMaxPartials = 4096;   // upper bound on blocks of a reducing launch
+
+// 32-byte aligned FP64 4-vector (CUDA 13 deprecates the unaligned double4).
+struct __align__(32) dbl4 {
+    double x, y, z, w;
+};
+__host__ __device__ inline dbl4 make_dbl4(double x, double y, double z, double w)
+{
+    dbl4 v;
+    v.x = x; v.y = y; v.z = z; v.w = w;
+    return v;
+}
+
+// Activity byte: low 3 bits = pd_activity, bit 3 = in contact with the sphere
+// during the current step (set by the force pass, read by the SpMV).
+constexpr uint8_t kActMask = 7;
+constexpr uint8_t kActContact = 8;
+
+// Scalars of the device-resident CG (one instance per handle, device memory).
+struct CgScalars {
+    double bnorm2;     // ||P b||^2 over free rows
+    double tol;        // rel_tol * ||P b||
+    double rz;         // <r, r>
+    double pAp;        // <p, A p>
+    double alpha;
+    double beta;
+    double rnorm;      // sqrt(rz) at the last check
+    double rel_tol;
+    int iter;
+    int done;
+    int converged;
+    int max_iter;
+};
+
+// Per-step constants, passed by value to the step kernels.
+struct StepParams {
+    int n;
+    int integrator;            // 0 implicit Euler, 1 Newmark-beta
+    int ticks;                 // pd_time_step
+    int box_enabled;
+    int sphere_on;
+    double cs;                 // clockScale
+    double bond_coeff;         // c: pd_C_times_V * PD_K or override
+    double horizon, radius;
+    double vs_threshold;       // horizon - radius
+    double mass;
+    double dt_base;
+    double h;                  // ticks * dt_base
+    double t2;                 // h^2 (IE) or h^2/4 (Newmark)
+    double gravity[3];
+    double stretch_a, stretch_b, alpha;
+    double bmin[3], bmax[3];
+    double restitution;
+    double sphere_c[3];        // centre at the start of this step (absolute coordinates)
+    double sphere_c_local[3];  // same, relative to the FP32 coordinate origin
+    double sphere_r, sphere_k;
+};
+
+// Device pointers of one handle (particles in cell-sorted order).
+struct DeviceState {
+    int n;
+    uint8_t* act;
+    dbl4* x64;      // positions (FP64 master)
+    dbl4* v64;      // velocities (FP64 master)
+    dbl4* X64;      // original positions
+    dbl4* x64_bk;
+    dbl4* v64_bk;
+    double* st;        // pd_stretch
+    double* ost;       // pd_original_stretch
+    double* nst;       // pd_new_stretch
+    int* row_ptr;      // CSR row starts (32-byte aligned rows), n+1
+    int* cnt;          // live bonds per particle (pd_bond_list_top + 1)
+    int* cnt_bk;
+    int* col;          // neighbour slots
+    float4* X32;       // original positions relative to origin (mixed)
+    float4* u32;       // displacement x - X (mixed)
+    double* jac;       // FP64 mode: symmetric bond Jacobians, 6 per bond slot
+    double* jdiag;     // FP64 mode: 6 per particle (sum of bond Jacobians + contact)
+    void* force;       // Real4 per particle: pd_force
+    void* rhs;         // Real4: b
+    void* sol;         // Real4: x (pd_system_solution)
+    void* r;           // Real4
+    void* p;           // Real4
+    void* y;           // Real4
+    CgScalars* sc;
+    double* partials;
+    unsigned int* counters;  // 8 reduction counters
+    int* flags;              // [0] has_broken, [1] broken bonds this pass, [2] overflow
+};
+
+// ---- step kernels (step.cu) --------------------------------------------------
+struct LaunchCfg {
+    int lanes;          // lanes per particle (4, 8, 16, 32)
+    int grid_bonds;     // blocks for row kernels (force, SpMV)
+    int grid_vec;       // blocks for per-particle vector kernels
+};
+
+void launch_force(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
+void launch_cg_init(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
+// y = A(x) (dot = false) or y = A(p) with <p,y> reduced into alpha (dot = true)
+void launch_spmv(bool fp64, bool dot, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
+void launch_cg_residual(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
+void launch_cg_axpy(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
+void launch_cg_xpby(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
+void launch_update(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
+void launch_refresh(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
+// Max resident blocks per SM of the row kernels for a lane count (for grid sizing).
+int row_kernel_blocks_per_sm(bool fp64, int lanes);
+
+// ---- bond construction kernels (bonds.cu) --------------------------------------
+struct BondBuildOut {
+    int* perm;        // slot -> original index (device, n)
+    int* row_ptr;     // device, n+1
+    int* col;         // device, allocated by the builder (cudaMalloc), caller frees
+    int* cnt;         // device, n
+    long long total;  // padded bond slots
+    long long bonds;  // live bonds
+    int max_bonds;    // largest row
+    int overflow;     // 1 if some row exceeded max_bonds
+};
+
+// Sorts particles by Morton cell key and builds the CSR bond list over the
+// exact predicate sqrt((a-b).(a-b)) < horizon.  pos_orig: n dbl4 in caller
+// order (device).  Writes the sorted positions to pos_sorted (n dbl4).
+// x32_sorted receives FP32 positions relative to origin (the box centre).
+cudaError_t build_bonds(const dbl4* pos_orig, int n, double horizon, int max_bonds,
+                        dbl4* pos_sorted, float4* x32_sorted, double origin[3], BondBuildOut* out,
+                        cudaStream_t st);
+
+// out[i] = in[perm[i]] for 4-double, 1-double, int32 and uint8 records
+void gather_double4(const dbl4* in, const int* perm, dbl4* out, int n, cudaStream_t st);
+void gather_double(const double* in, const int* perm, double* out, int n, cudaStream_t st);
+void gather_int_to_u8(const int* in, const int* perm, uint8_t* out, int n, cudaStream_t st);
+// out[perm[i]] = in[i]
+void scatter_double4(const dbl4* in, const int* perm, dbl4* out, int n, cudaStream_t st);
+// FP32 copies relative to an origin
+void make_local32(const dbl4* X, double ox, double oy, double oz, float4* X32, float4* u32, int n,
+                  cudaStream_t st);
+
+}  // namespace pdgb

@@ -1,0 +1,678 @@
+// step.cu -- the implicit PD step on sm_103a.
+//
+// One step (reference: Simulator::integratePeridynamicsImplicitEuler /
+// NewmarkBeta, src/core/simulator.cu:297-652) is
+//   k_force      bond stretch, breakage, force, right-hand side      (cg_solver.cuh:200-339,
+//                                                                     implicit_euler.cuh:62-86,
+//                                                                     newmark_beta.cuh:62-86)
+//   k_cg_init / k_spmv / k_cg_residual                               CG set-up
+//   { k_spmv(dot) ; k_cg_axpy ; k_cg_xpby } x iterations              CUSP krylov::cg restated
+//   k_update     position / velocity update + box reflection        (implicit_euler.cuh:90-176,
+//                                                                     newmark_beta.cuh:89-199)
+// The reference assembles A = M + beta h^2 K as 3x3 blocks in a 528-slot
+// bond-major array (cg_solver.cuh:307, implicit_euler.cuh:19-59); here the
+// mixed-precision path never forms A: k_spmv recomputes each bond's Jacobian
+// from the positions inside the product.  The FP64 path stores the six
+// independent entries of each symmetric bond Jacobian.
+//
+// Rows of G lanes ("lanes per particle") walk a particle's CSR row; the
+// per-particle sums are shuffled within the group.
+#include <type_traits>
+
+#include "pd_device.cuh"
+#include "pd_kernels.h"
+
+namespace pdgb {
+
+// ---- FP64 operations the compiler must not contract ---------------------------
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ double dsqrt(double a) { return __dsqrt_rn(a); }
+
+// Bond geometry exactly as calculatePDForceDerivative evaluates it
+// (cg_solver.cuh:254-260): eij = x_q - x_p, dij = sqrt(x*x + y*y + z*z),
+// d0 = length(X_p - X_q), drdivd = dij / d0 - 1.
+struct BondEval {
+    double ex, ey, ez, dij, d0, s;
+};
+
+__device__ __forceinline__ BondEval eval_bond(const dbl4& xp, const dbl4& Xp, const dbl4& xq,
+                                              const dbl4& Xq)
+{
+    BondEval b;
+    b.ex = dsub(xq.x, xp.x);
+    b.ey = dsub(xq.y, xp.y);
+    b.ez = dsub(xq.z, xp.z);
+    b.dij = dsqrt(dadd(dadd(dmul(b.ex, b.ex), dmul(b.ey, b.ey)), dmul(b.ez, b.ez)));
+    const double ox = dsub(Xp.x, Xq.x), oy = dsub(Xp.y, Xq.y), oz = dsub(Xp.z, Xq.z);
+    b.d0 = dsqrt(dadd(dadd(dmul(ox, ox), dmul(oy, oy)), dmul(oz, oz)));
+    b.s = dsub(ddiv(b.dij, b.d0), 1.0);
+    return b;
+}
+
+// fmaxf(stretch_p, stretch_q) of cg_solver.cuh:264: both limits rounded to float.
+__device__ __forceinline__ double break_threshold(float thp, double stq)
+{
+    const float thq = (float)stq;
+    return (double)(thp > thq ? thp : thq);
+}
+
+// ---- force / breakage / right-hand side ----------------------------------------
+template <int G, bool FP64>
+__global__ void __launch_bounds__(kBlock) k_force(StepParams P, DeviceState S)
+{
+    using Real = typename std::conditional<FP64, double, float>::type;
+    using V4 = typename Vec4<Real>::type;
+    const unsigned gmask = group_mask<G>();
+    const int lane = threadIdx.x & (G - 1);
+    constexpr int gpb = kBlock / G;
+    const int stride = gridDim.x * gpb;
+    V4* force = (V4*)S.force;
+    V4* rhs = (V4*)S.rhs;
+    for (int p = blockIdx.x * gpb + threadIdx.x / G; p < P.n; p += stride) {
+        const int a = S.act[p] & kActMask;
+        if (a == ACT_INVISIBLE) continue;
+        const dbl4 xp = S.x64[p];
+        const dbl4 Xp = S.X64[p];
+        const float thp = (float)S.st[p];
+        const int rs = S.row_ptr[p];
+        const int c = S.cnt[p];
+        Real fx = 0, fy = 0, fz = 0;
+        double j0 = 0, j1 = 0, j2 = 0, j3 = 0, j4 = 0, j5 = 0;   // FP64: diagonal block sum
+        double smin = 0.0;
+        int nb = 0;
+        for (int j = lane; j < c; j += G) {
+            const int q = S.col[rs + j];
+            const dbl4 xq = S.x64[q];
+            const dbl4 Xq = S.X64[q];
+            const BondEval b = eval_bond(xp, Xp, xq, Xq);
+            if (b.s > break_threshold(thp, S.st[q])) {
+                ++nb;
+                continue;
+            }
+            smin = b.s < smin ? b.s : smin;
+            if (FP64) {
+                // reference formulas: eij /= fmaxf(dij, SMALL) (float-rounded), vscale,
+                // J = (c/d0) [ (1 - d0/dij) I + (d0/dij) e e^T ]   (cg_solver.cuh:256-303)
+                const double D = (double)fmaxf((float)b.dij, (float)1e-10);
+                const double ex = ddiv(b.ex, D), ey = ddiv(b.ey, D), ez = ddiv(b.ez, D);
+                double vscale = 1.0;
+                if (b.d0 > P.vs_threshold) vscale = dadd(0.5, ddiv(ddiv(dsub(P.horizon, b.d0), 2.0), P.radius));
+                const double kk = dmul(b.s, vscale);
+                fx = dadd(fx, dmul(kk, ex));
+                fy = dadd(fy, dmul(kk, ey));
+                fz = dadd(fz, dmul(kk, ez));
+                const double r = ddiv(b.d0, b.dij);
+                const double dg = dsub(1.0, r);
+                const double cc = ddiv(P.bond_coeff, b.d0);
+                const double jxx = dmul(dadd(dg, dmul(dmul(ex, ex), r)), cc);
+                const double jyy = dmul(dadd(dg, dmul(dmul(ey, ey), r)), cc);
+                const double jzz = dmul(dadd(dg, dmul(dmul(ez, ez), r)), cc);
+                const double jxy = dmul(dmul(dmul(ex, ey), r), cc);
+                const double jxz = dmul(dmul(dmul(ex, ez), r), cc);
+                const double jyz = dmul(dmul(dmul(ey, ez), r), cc);
+                double* J = S.jac + 6ll * (rs + j);
+                J[0] = jxx; J[1] = jyy; J[2] = jzz; J[3] = jxy; J[4] = jxz; J[5] = jyz;
+                j0 += jxx; j1 += jyy; j2 += jzz; j3 += jxy; j4 += jxz; j5 += jyz;
+            } else {
+                const float inv = 1.0f / (float)b.dij;
+                const float d0f = (float)b.d0;
+                float vs = 1.0f;
+                if (b.d0 > P.vs_threshold) vs = 0.5f + ((float)P.horizon - d0f) * 0.5f / (float)P.radius;
+                const float kk = (float)b.s * vs * inv;
+                fx = fmaf(kk, (float)b.ex, (float)fx);
+                fy = fmaf(kk, (float)b.ey, (float)fy);
+                fz = fmaf(kk, (float)b.ez, (float)fz);
+            }
+        }
+        fx = group_sum<G>(fx, gmask);
+        fy = group_sum<G>(fy, gmask);
+        fz = group_sum<G>(fz, gmask);
+        smin = group_min<G>(smin, gmask);
+        nb = group_sum<G>(nb, gmask);
+        if (FP64) {
+            j0 = group_sum<G>(j0, gmask); j1 = group_sum<G>(j1, gmask); j2 = group_sum<G>(j2, gmask);
+            j3 = group_sum<G>(j3, gmask); j4 = group_sum<G>(j4, gmask); j5 = group_sum<G>(j5, gmask);
+        }
+        if (nb > 0) {
+            // Rare path: partition the row as the reference does (swap the broken
+            // bond with the last live one and retest the swapped-in bond,
+            // cg_solver.cuh:264-275), so live bonds occupy the first cnt slots.
+            int top = c - 1;
+            if (lane == 0) {
+                int bond = 0;
+                while (bond <= top) {
+                    const int q = S.col[rs + bond];
+                    const BondEval b = eval_bond(xp, Xp, S.x64[q], S.X64[q]);
+                    if (b.s > break_threshold(thp, S.st[q])) {
+                        S.col[rs + bond] = S.col[rs + top];
+                        S.col[rs + top] = q;
+                        --top;
+                        continue;
+                    }
+                    ++bond;
+                }
+                S.cnt[p] = top + 1;
+                S.flags[0] = 1;
+                atomicAdd(&S.flags[1], nb);
+            }
+            __syncwarp(gmask);
+            if (FP64) {
+                // bond slots moved: store each live bond's Jacobian at its new slot
+                top = __shfl_sync(gmask, top, 0, G);
+                for (int j = lane; j <= top; j += G) {
+                    const int q = S.col[rs + j];
+                    const BondEval b = eval_bond(xp, Xp, S.x64[q], S.X64[q]);
+                    const double D = (double)fmaxf((float)b.dij, (float)1e-10);
+                    const double ex = ddiv(b.ex, D), ey = ddiv(b.ey, D), ez = ddiv(b.ez, D);
+                    const double r = ddiv(b.d0, b.dij);
+                    const double dg = dsub(1.0, r);
+                    const double cc = ddiv(P.bond_coeff, b.d0);
+                    double* J = S.jac + 6ll * (rs + j);
+                    J[0] = dmul(dadd(dg, dmul(dmul(ex, ex), r)), cc);
+                    J[1] = dmul(dadd(dg, dmul(dmul(ey, ey), r)), cc);
+                    J[2] = dmul(dadd(dg, dmul(dmul(ez, ez), r)), cc);
+                    J[3] = dmul(dmul(dmul(ex, ey), r), cc);
+                    J[4] = dmul(dmul(dmul(ex, ez), r), cc);
+                    J[5] = dmul(dmul(dmul(ey, ez), r), cc);
+                }
+            }
+        }
+        if (lane == 0) {
+            // force *= C*V*PD_K; new stretch limit; gravity (cg_solver.cuh:325-331)
+            double f0 = (double)fx * P.bond_coeff, f1 = (double)fy * P.bond_coeff, f2 = (double)fz * P.bond_coeff;
+            if (FP64) {
+                f0 = dmul((double)fx, P.bond_coeff);
+                f1 = dmul((double)fy, P.bond_coeff);
+                f2 = dmul((double)fz, P.bond_coeff);
+            }
+            const double ss0 = dmul(dsub(P.stretch_a, dmul(P.stretch_b, P.cs)), S.ost[p]);
+            S.nst[p] = dsub(ss0, dmul(P.alpha, smin));
+            if (P.gravity[0] != 0.0) f0 = dsub(f0, dmul(dmul(P.cs, -P.gravity[0]), P.mass));
+            if (P.gravity[1] != 0.0) f1 = dsub(f1, dmul(dmul(P.cs, -P.gravity[1]), P.mass));
+            if (P.gravity[2] != 0.0) f2 = dsub(f2, dmul(dmul(P.cs, -P.gravity[2]), P.mass));
+            // rigid-sphere penalty contact at the start-of-step position (extension)
+            uint8_t actb = (uint8_t)a;
+            if (P.sphere_on) {
+                const double dx = xp.x - P.sphere_c[0], dy = xp.y - P.sphere_c[1], dz = xp.z - P.sphere_c[2];
+                const double d = sqrt(dx * dx + dy * dy + dz * dz);
+                const double pen = (P.sphere_r + P.radius) - d;
+                if (pen > 0.0 && d > 0.0) {
+                    const double nx = dx / d, ny = dy / d, nz = dz / d;
+                    f0 += P.sphere_k * pen * nx;
+                    f1 += P.sphere_k * pen * ny;
+                    f2 += P.sphere_k * pen * nz;
+                    actb |= kActContact;
+                    if (FP64) {
+                        j0 += P.sphere_k * nx * nx; j1 += P.sphere_k * ny * ny; j2 += P.sphere_k * nz * nz;
+                        j3 += P.sphere_k * nx * ny; j4 += P.sphere_k * nx * nz; j5 += P.sphere_k * ny * nz;
+                    }
+                }
+            }
+            S.act[p] = actb;
+            force[p] = make_v4<V4>(f0, f1, f2);
+            if (FP64) {
+                double* D = S.jdiag + 6ll * p;
+                D[0] = j0; D[1] = j1; D[2] = j2; D[3] = j3; D[4] = j4; D[5] = j5;
+            }
+            // right-hand side (fillVectorB*): b = m v + h f, or b = h (m v + (h/2) f)
+            const dbl4 v = S.v64[p];
+            double b0, b1, b2;
+            if (P.integrator == 0) {
+                b0 = dadd(dmul(P.mass, v.x), dmul(P.h, f0));
+                b1 = dadd(dmul(P.mass, v.y), dmul(P.h, f1));
+                b2 = dadd(dmul(P.mass, v.z), dmul(P.h, f2));
+            } else {
+                const double hh = dmul(0.5, P.h);
+                b0 = dmul(P.h, dadd(dmul(P.mass, v.x), dmul(hh, f0)));
+                b1 = dmul(P.h, dadd(dmul(P.mass, v.y), dmul(hh, f1)));
+                b2 = dmul(P.h, dadd(dmul(P.mass, v.z), dmul(hh, f2)));
+            }
+            rhs[p] = make_v4<V4>(b0, b1, b2);
+        }
+    }
+}
+
+// ---- A u: mass + (beta h^2) stiffness, Dirichlet rows projected out --------------
+// Mixed precision: per bond, with xi0 = X_q - X_p, delta = u_q - u_p (u = x - X),
+// xi = xi0 + delta, the bond Jacobian applied to w = u_p - u_q is
+//   c [ (1/d0 - 1/d) w + (xi . w) xi / d^3 ]
+// which equals (c/d0)[(1 - d0/d) I + (d0/d) e e^T] w of cg_solver.cuh:292-299.
+template <int G, bool FP64, bool DOT>
+__global__ void __launch_bounds__(kBlock) k_spmv(StepParams P, DeviceState S, const void* __restrict__ in_,
+                                                  void* __restrict__ out_, ReduceSlot slot)
+{
+    using Real = typename std::conditional<FP64, double, float>::type;
+    using V4 = typename Vec4<Real>::type;
+    using Acc = typename DotAccFor<Real>::type;
+    if (DOT && ((volatile CgScalars*)S.sc)->done) return;
+    const V4* __restrict__ in = (const V4*)in_;
+    V4* __restrict__ out = (V4*)out_;
+    const unsigned gmask = group_mask<G>();
+    const int lane = threadIdx.x & (G - 1);
+    constexpr int gpb = kBlock / G;
+    const int stride = gridDim.x * gpb;
+    Acc acc;
+    const Real c = (Real)P.bond_coeff;
+    const Real t2 = (Real)P.t2;
+    const Real m = (Real)P.mass;
+    // every group runs the same number of loop trips so that whole blocks reach the reduction
+    const int trips = (P.n + stride - 1) / stride;
+    for (int t = 0; t < trips; ++t) {
+        const int p = t * stride + blockIdx.x * gpb + threadIdx.x / G;
+        if (p >= P.n) continue;
+        const uint8_t ab = S.act[p];
+        if (is_dirichlet(ab & kActMask)) {
+            if (lane == 0) out[p] = make_v4<V4>(0.0, 0.0, 0.0);
+            continue;
+        }
+        const V4 w = in[p];
+        const int rs = S.row_ptr[p];
+        const int cn = S.cnt[p];
+        Real ax = 0, ay = 0, az = 0;
+        if (FP64) {
+            for (int j = lane; j < cn; j += G) {
+                const int q = S.col[rs + j];
+                const V4 wq = in[q];
+                const double* J = S.jac + 6ll * (rs + j);
+                ax += J[0] * wq.x + J[3] * wq.y + J[4] * wq.z;
+                ay += J[3] * wq.x + J[1] * wq.y + J[5] * wq.z;
+                az += J[4] * wq.x + J[5] * wq.y + J[2] * wq.z;
+            }
+        } else {
+            const float4 Xp = S.X32[p];
+            const float4 Up = S.u32[p];
+            for (int j = lane; j < cn; j += G) {
+                const int q = S.col[rs + j];
+                const float4 Xq = S.X32[q];
+                const float4 Uq = S.u32[q];
+                const V4 wq = in[q];
+                const float x0 = Xq.x - Xp.x, y0 = Xq.y - Xp.y, z0 = Xq.z - Xp.z;
+                const float xs = x0 + (Uq.x - Up.x), ys = y0 + (Uq.y - Up.y), zs = z0 + (Uq.z - Up.z);
+                const float inv_d0 = rsqrtf(fmaf(x0, x0, fmaf(y0, y0, z0 * z0)));
+                const float inv_d = rsqrtf(fmaf(xs, xs, fmaf(ys, ys, zs * zs)));
+                const float wx = (float)w.x - (float)wq.x, wy = (float)w.y - (float)wq.y, wz = (float)w.z - (float)wq.z;
+                const float a1 = inv_d0 - inv_d;
+                const float g = fmaf(xs, wx, fmaf(ys, wy, zs * wz)) * (inv_d * inv_d * inv_d);
+                ax = fmaf(a1, wx, fmaf(g, xs, (float)ax));
+                ay = fmaf(a1, wy, fmaf(g, ys, (float)ay));
+                az = fmaf(a1, wz, fmaf(g, zs, (float)az));
+            }
+        }
+        ax = group_sum<G>(ax, gmask);
+        ay = group_sum<G>(ay, gmask);
+        az = group_sum<G>(az, gmask);
+        if (lane == 0) {
+            Real kx, ky, kz;
+            if (FP64) {
+                const double* D = S.jdiag + 6ll * p;
+                kx = D[0] * w.x + D[3] * w.y + D[4] * w.z - ax;
+                ky = D[3] * w.x + D[1] * w.y + D[5] * w.z - ay;
+                kz = D[4] * w.x + D[5] * w.y + D[2] * w.z - az;
+            } else {
+                kx = c * ax; ky = c * ay; kz = c * az;
+                if (ab & kActContact) {
+                    const float4 Xp = S.X32[p];
+                    const float4 Up = S.u32[p];
+                    const float dx = Xp.x + Up.x - (float)P.sphere_c_local[0];
+                    const float dy = Xp.y + Up.y - (float)P.sphere_c_local[1];
+                    const float dz = Xp.z + Up.z - (float)P.sphere_c_local[2];
+                    const float inv = rsqrtf(dx * dx + dy * dy + dz * dz);
+                    const float nx = dx * inv, ny = dy * inv, nz = dz * inv;
+                    const float kn = (float)P.sphere_k * (nx * (float)w.x + ny * (float)w.y + nz * (float)w.z);
+                    kx += kn * nx; ky += kn * ny; kz += kn * nz;
+                }
+            }
+            const Real yx = m * (Real)w.x + t2 * kx;
+            const Real yy = m * (Real)w.y + t2 * ky;
+            const Real yz = m * (Real)w.z + t2 * kz;
+            V4 yv;
+            yv.x = yx; yv.y = yy; yv.z = yz; yv.w = 0;
+            out[p] = yv;
+            if (DOT) {
+                acc.fma(w.x, yx);
+                acc.fma(w.y, yy);
+                acc.fma(w.z, yz);
+            }
+        }
+    }
+    if (DOT) {
+        CgScalars* sc = S.sc;
+        block_reduce_finish(acc, slot, [sc](double pAp) {
+            sc->pAp = pAp;
+            sc->alpha = sc->rz / pAp;
+        });
+    }
+}
+
+// ---- CG vector kernels (CUSP krylov::cg, identity preconditioner) ----------------
+// Dirichlet values: clamped and invisible particles 0, prescribed particles their
+// velocity (implicit Euler) or h * velocity (Newmark); ||b|| over free rows.
+template <bool FP64>
+__global__ void __launch_bounds__(kBlock) k_cg_init(StepParams P, DeviceState S, ReduceSlot slot)
+{
+    using Real = typename std::conditional<FP64, double, float>::type;
+    using V4 = typename Vec4<Real>::type;
+    using Acc = typename DotAccFor<Real>::type;
+    V4* x = (V4*)S.sol;
+    const V4* b = (const V4*)S.rhs;
+    Acc acc;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
+        const int a = S.act[i] & kActMask;
+        if (is_dirichlet(a)) {
+            double ux = 0, uy = 0, uz = 0;
+            if (a == ACT_PRESCRIBED) {
+                const dbl4 v = S.v64[i];
+                const double s = P.integrator == 0 ? 1.0 : P.h;
+                ux = v.x * s; uy = v.y * s; uz = v.z * s;
+            }
+            x[i] = make_v4<V4>(ux, uy, uz);
+        } else {
+            const V4 bv = b[i];
+            acc.fma(bv.x, bv.x);
+            acc.fma(bv.y, bv.y);
+            acc.fma(bv.z, bv.z);
+        }
+    }
+    CgScalars* sc = S.sc;
+    block_reduce_finish(acc, slot, [sc](double bb) {
+        sc->bnorm2 = bb;
+        sc->tol = 0.0 + sc->rel_tol * sqrt(bb);
+        sc->iter = 0;
+        sc->done = 0;
+        sc->converged = 0;
+    });
+}
+
+// r = b - A x0 (free rows), p = r, rz = <r,r>; convergence test before the first iteration
+template <bool FP64>
+__global__ void __launch_bounds__(kBlock) k_cg_residual(StepParams P, DeviceState S, ReduceSlot slot)
+{
+    using Real = typename std::conditional<FP64, double, float>::type;
+    using V4 = typename Vec4<Real>::type;
+    using Acc = typename DotAccFor<Real>::type;
+    const V4* b = (const V4*)S.rhs;
+    const V4* y = (const V4*)S.y;
+    V4* r = (V4*)S.r;
+    V4* pv = (V4*)S.p;
+    Acc acc;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
+        V4 rv;
+        if (is_dirichlet(S.act[i] & kActMask)) {
+            rv.x = 0; rv.y = 0; rv.z = 0; rv.w = 0;
+        } else {
+            const V4 bv = b[i], yv = y[i];
+            rv.x = bv.x - yv.x; rv.y = bv.y - yv.y; rv.z = bv.z - yv.z; rv.w = 0;
+            acc.fma(rv.x, rv.x);
+            acc.fma(rv.y, rv.y);
+            acc.fma(rv.z, rv.z);
+        }
+        r[i] = rv;
+        pv[i] = rv;
+    }
+    CgScalars* sc = S.sc;
+    block_reduce_finish(acc, slot, [sc](double rr) {
+        sc->rz = rr;
+        sc->rnorm = sqrt(rr);
+        if (sc->rnorm <= sc->tol) {
+            sc->done = 1;
+            sc->converged = 1;
+        } else if (sc->iter >= sc->max_iter) {
+            sc->done = 1;
+        }
+    });
+}
+
+// x += alpha p ; r -= alpha A p ; rz' = <r,r> ; beta = rz'/rz ; test
+template <bool FP64>
+__global__ void __launch_bounds__(kBlock) k_cg_axpy(StepParams P, DeviceState S, ReduceSlot slot)
+{
+    using Real = typename std::conditional<FP64, double, float>::type;
+    using V4 = typename Vec4<Real>::type;
+    using Acc = typename DotAccFor<Real>::type;
+    CgScalars* sc = S.sc;
+    if (((volatile CgScalars*)sc)->done) return;
+    const Real alpha = (Real)sc->alpha;
+    V4* x = (V4*)S.sol;
+    V4* r = (V4*)S.r;
+    const V4* pv = (const V4*)S.p;
+    const V4* y = (const V4*)S.y;
+    Acc acc;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
+        const V4 pi = pv[i], yi = y[i];
+        V4 xi = x[i], ri = r[i];
+        xi.x += alpha * pi.x; xi.y += alpha * pi.y; xi.z += alpha * pi.z;
+        ri.x -= alpha * yi.x; ri.y -= alpha * yi.y; ri.z -= alpha * yi.z;
+        x[i] = xi;
+        r[i] = ri;
+        acc.fma(ri.x, ri.x);
+        acc.fma(ri.y, ri.y);
+        acc.fma(ri.z, ri.z);
+    }
+    block_reduce_finish(acc, slot, [sc](double rr) {
+        const double rz_old = sc->rz;
+        sc->rz = rr;
+        sc->beta = rr / rz_old;
+        sc->iter += 1;
+        sc->rnorm = sqrt(rr);
+        if (sc->rnorm <= sc->tol) {
+            sc->done = 1;
+            sc->converged = 1;
+        } else if (sc->iter >= sc->max_iter) {
+            sc->done = 1;
+        }
+    });
+}
+
+// p = r + beta p
+template <bool FP64>
+__global__ void __launch_bounds__(kBlock) k_cg_xpby(StepParams P, DeviceState S)
+{
+    using Real = typename std::conditional<FP64, double, float>::type;
+    using V4 = typename Vec4<Real>::type;
+    const CgScalars* sc = S.sc;
+    if (((volatile const CgScalars*)sc)->done) return;
+    const Real beta = (Real)sc->beta;
+    const V4* r = (const V4*)S.r;
+    V4* pv = (V4*)S.p;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
+        const V4 ri = r[i];
+        V4 pi = pv[i];
+        pi.x = ri.x + beta * pi.x;
+        pi.y = ri.y + beta * pi.y;
+        pi.z = ri.z + beta * pi.z;
+        pv[i] = pi;
+    }
+}
+
+// ---- position / velocity update ------------------------------------------------
+// box reflection of updatePDPosition* (implicit_euler.cuh:116-168), FP64, same order
+__device__ __forceinline__ void reflect(const StepParams& P, double& np, double& nv, int k)
+{
+    const double mn = dadd(P.bmin[k], P.radius);
+    const double mx = dsub(P.bmax[k], P.radius);
+    if (np > mx) {
+        nv = dmul(nv, -P.restitution);
+        np = dsub(mx, dmul(P.restitution, dsub(np, mx)));
+    }
+    if (np < mn) {
+        nv = dmul(nv, -P.restitution);
+        np = dadd(mn, dmul(P.restitution, dsub(mn, np)));
+    }
+}
+
+template <bool FP64>
+__global__ void __launch_bounds__(kBlock) k_update(StepParams P, DeviceState S)
+{
+    using Real = typename std::conditional<FP64, double, float>::type;
+    using V4 = typename Vec4<Real>::type;
+    const V4* sol = (const V4*)S.sol;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
+        S.st[i] = S.nst[i];   // updatePDStretchNeighborList (simulator.cuh:2601-2620)
+        const int a = S.act[i] & kActMask;
+        const dbl4 x = S.x64[i];
+        dbl4 v = S.v64[i];
+        if (a == ACT_INVISIBLE) {
+            if (P.integrator == 0) S.v64[i] = make_dbl4(0.0, 0.0, 0.0, 0.0);
+            continue;
+        }
+        double nv[3], np[3];
+        const double xs[3] = {x.x, x.y, x.z};
+        const double vs[3] = {v.x, v.y, v.z};
+        if (P.integrator == 0) {
+            // transferData(PD_VELOCITY <- PD_SYSTEM_SOLUTION); x += v * base * ticks
+            if (a == ACT_PRESCRIBED) {
+                nv[0] = vs[0]; nv[1] = vs[1]; nv[2] = vs[2];
+            } else if (a == ACT_CLAMPED) {
+                nv[0] = nv[1] = nv[2] = 0.0;
+            } else {
+                const V4 s = sol[i];
+                nv[0] = (double)s.x; nv[1] = (double)s.y; nv[2] = (double)s.z;
+            }
+            for (int k = 0; k < 3; ++k) np[k] = dadd(xs[k], dmul(dmul(nv[k], P.dt_base), (double)P.ticks));
+        } else {
+            // v = 2/h dx - v ; x += dx
+            double dx[3];
+            if (a == ACT_PRESCRIBED) {
+                for (int k = 0; k < 3; ++k) { dx[k] = dmul(P.h, vs[k]); nv[k] = vs[k]; }
+            } else if (a == ACT_CLAMPED) {
+                for (int k = 0; k < 3; ++k) { dx[k] = 0.0; nv[k] = 0.0; }
+            } else {
+                const V4 s = sol[i];
+                dx[0] = (double)s.x; dx[1] = (double)s.y; dx[2] = (double)s.z;
+                const double two_h = ddiv(2.0, P.h);
+                for (int k = 0; k < 3; ++k) nv[k] = dsub(dmul(two_h, dx[k]), vs[k]);
+            }
+            for (int k = 0; k < 3; ++k) np[k] = dadd(xs[k], dx[k]);
+        }
+        if (P.box_enabled)
+            for (int k = 0; k < 3; ++k) reflect(P, np[k], nv[k], k);
+        S.x64[i] = make_dbl4(np[0], np[1], np[2], 0.0);
+        S.v64[i] = make_dbl4(nv[0], nv[1], nv[2], 0.0);
+        if (!FP64) {
+            const dbl4 X = S.X64[i];
+            S.u32[i] = make_float4((float)(np[0] - X.x), (float)(np[1] - X.y), (float)(np[2] - X.z), 0.f);
+        }
+    }
+}
+
+// FP32 displacement from the FP64 master positions (after a rollback restore)
+__global__ void __launch_bounds__(kBlock) k_refresh(StepParams P, DeviceState S)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
+        const dbl4 x = S.x64[i], X = S.X64[i];
+        S.u32[i] = make_float4((float)(x.x - X.x), (float)(x.y - X.y), (float)(x.z - X.z), 0.f);
+        S.act[i] &= kActMask;
+    }
+}
+
+// ---- launchers ------------------------------------------------------------------
+static ReduceSlot slot_of(const DeviceState& S, int k) { return ReduceSlot{S.partials, S.counters + k}; }
+
+template <int G>
+static void force_g(bool fp64, const StepParams& P, const DeviceState& S, int grid, cudaStream_t st)
+{
+    if (fp64) k_force<G, true><<<grid, kBlock, 0, st>>>(P, S);
+    else k_force<G, false><<<grid, kBlock, 0, st>>>(P, S);
+}
+
+void launch_force(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st)
+{
+    switch (L.lanes) {
+    case 4: force_g<4>(fp64, P, S, L.grid_bonds, st); break;
+    case 16: force_g<16>(fp64, P, S, L.grid_bonds, st); break;
+    case 32: force_g<32>(fp64, P, S, L.grid_bonds, st); break;
+    default: force_g<8>(fp64, P, S, L.grid_bonds, st); break;
+    }
+}
+
+template <int G, bool DOT>
+static void spmv_g(bool fp64, const StepParams& P, const DeviceState& S, int grid, cudaStream_t st)
+{
+    const void* in = DOT ? S.p : S.sol;
+    void* out = S.y;
+    if (fp64) k_spmv<G, true, DOT><<<grid, kBlock, 0, st>>>(P, S, in, out, slot_of(S, 1));
+    else k_spmv<G, false, DOT><<<grid, kBlock, 0, st>>>(P, S, in, out, slot_of(S, 1));
+}
+
+template <bool DOT>
+static void spmv_d(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st)
+{
+    switch (L.lanes) {
+    case 4: spmv_g<4, DOT>(fp64, P, S, L.grid_bonds, st); break;
+    case 16: spmv_g<16, DOT>(fp64, P, S, L.grid_bonds, st); break;
+    case 32: spmv_g<32, DOT>(fp64, P, S, L.grid_bonds, st); break;
+    default: spmv_g<8, DOT>(fp64, P, S, L.grid_bonds, st); break;
+    }
+}
+
+void launch_spmv(bool fp64, bool dot, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st)
+{
+    if (dot) spmv_d<true>(fp64, P, S, L, st);
+    else spmv_d<false>(fp64, P, S, L, st);
+}
+
+void launch_cg_init(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st)
+{
+    if (fp64) k_cg_init<true><<<L.grid_vec, kBlock, 0, st>>>(P, S, slot_of(S, 0));
+    else k_cg_init<false><<<L.grid_vec, kBlock, 0, st>>>(P, S, slot_of(S, 0));
+}
+
+void launch_cg_residual(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st)
+{
+    if (fp64) k_cg_residual<true><<<L.grid_vec, kBlock, 0, st>>>(P, S, slot_of(S, 2));
+    else k_cg_residual<false><<<L.grid_vec, kBlock, 0, st>>>(P, S, slot_of(S, 2));
+}
+
+void launch_cg_axpy(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st)
+{
+    if (fp64) k_cg_axpy<true><<<L.grid_vec, kBlock, 0, st>>>(P, S, slot_of(S, 3));
+    else k_cg_axpy<false><<<L.grid_vec, kBlock, 0, st>>>(P, S, slot_of(S, 3));
+}
+
+void launch_cg_xpby(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st)
+{
+    if (fp64) k_cg_xpby<true><<<L.grid_vec, kBlock, 0, st>>>(P, S);
+    else k_cg_xpby<false><<<L.grid_vec, kBlock, 0, st>>>(P, S);
+}
+
+void launch_update(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st)
+{
+    if (fp64) k_update<true><<<L.grid_vec, kBlock, 0, st>>>(P, S);
+    else k_update<false><<<L.grid_vec, kBlock, 0, st>>>(P, S);
+}
+
+void launch_refresh(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st)
+{
+    (void)fp64;
+    k_refresh<<<L.grid_vec, kBlock, 0, st>>>(P, S);
+}
+
+template <int G>
+static int blocks_g(bool fp64)
+{
+    int a = 0, b = 0;
+    if (fp64) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_spmv<G, true, true>, kBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_force<G, true>, kBlock, 0);
+    } else {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_spmv<G, false, true>, kBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_force<G, false>, kBlock, 0);
+    }
+    const int m = a < b ? a : b;
+    return m > 0 ? m : 1;
+}
+
+int row_kernel_blocks_per_sm(bool fp64, int lanes)
+{
+    switch (lanes) {
+    case 4: return blocks_g<4>(fp64);
+    case 16: return blocks_g<16>(fp64);
+    case 32: return blocks_g<32>(fp64);
+    default: return blocks_g<8>(fp64);
+    }
+}
+
+}  // namespace pdgb

@@ -1,0 +1,62 @@
+"""Test helpers: map a scene onto the oracle's resolved parameters and compare runs."""
+import numpy as np
+
+from oracle import oracle as O
+
+
+def oracle_params(scene):
+    sim, run, opt = scene.sim, scene.run, scene.opt
+    p = O.default_params()
+    p.n = scene.n
+    p.integrator = run.integrator
+    p.adaptive = run.adaptive_integration
+    p.horizon = sim.pd_horizon
+    p.radius = sim.pd_particle_radius
+    p.bond_coeff = opt.bond_stiffness if opt.bond_stiffness > 0 else sim.pd_C_times_V * opt.pd_k
+    p.mass = sim.pd_particle_mass
+    p.dt_base = opt.time_step_base
+    p.dt_ticks = sim.pd_time_step
+    p.dt_ticks_min = opt.time_step_min
+    p.max_substep = opt.max_substep
+    p.phase_in = opt.phase_in_steps
+    p.stretch_a, p.stretch_b, p.alpha = opt.stretch_a, opt.stretch_b, opt.alpha
+    for k in range(3):
+        p.gravity[k] = opt.gravity[k]
+    if opt.box_enabled:
+        lo = (sim.boundary_min_x, sim.boundary_min_y, sim.boundary_min_z)
+        hi = (sim.boundary_max_x, sim.boundary_max_y, sim.boundary_max_z)
+    else:
+        lo, hi = (-1e300,) * 3, (1e300,) * 3
+    for k in range(3):
+        p.box_min[k], p.box_max[k] = lo[k], hi[k]
+    p.restitution = opt.restitution
+    p.cg_rel_tol = opt.cg_relative_tolerance
+    p.cg_max_iter = opt.cg_max_iterations
+    p.max_bonds = opt.max_bonds_per_particle
+    p.s0 = float(np.float32(run.pd_stretch_limit_s0))
+    p.sphere_on = opt.sphere_enabled
+    for k in range(3):
+        p.sphere_c0[k] = opt.sphere_center[k]
+        p.sphere_v[k] = opt.sphere_velocity[k]
+    p.sphere_radius = opt.sphere_radius
+    p.sphere_k = opt.sphere_stiffness
+    return p
+
+
+def make_oracle(scene):
+    o = O.OracleSim(oracle_params(scene))
+    o.set_particles(scene.pos, scene.vel, scene.act)
+    o.make_ready()
+    return o
+
+
+def same_sets(a, b):
+    return len(a) == len(b) and all(np.array_equal(np.asarray(x), np.asarray(y)) for x, y in zip(a, b))
+
+
+def rel_err(x, ref):
+    """max |x - ref| / max |ref| over xyz."""
+    x = np.asarray(x)[:, :3]
+    ref = np.asarray(ref)[:, :3]
+    scale = max(np.abs(ref).max(), 1e-300)
+    return float(np.abs(x - ref).max() / scale)
