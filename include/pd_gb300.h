@@ -233,6 +233,11 @@ pd_status pd_get_kernel_times(pd_handle* h, pd_kernel_times* t);
 pd_status pd_reset_kernel_times(pd_handle* h);
 /* Number of kernels this library launched on the handle's stream so far. */
 pd_status pd_get_launch_count(pd_handle* h, long long* launches);
+/* The cudaStream_t (as void*) every call of this handle runs on, e.g. to
+ * record CUDA events around pd_advance. */
+pd_status pd_get_stream(pd_handle* h, void** stream);
+/* Waits until all work of the handle has finished on the device. */
+pd_status pd_synchronize(pd_handle* h);
 
 /* ---- errors --------------------------------------------------------------- */
 const char* pd_status_string(pd_status s);

@@ -152,6 +152,8 @@ def library(build_if_missing: bool = True):
         "pd_get_kernel_times": (st, [vp, P(KernelTimes)]),
         "pd_reset_kernel_times": (st, [vp]),
         "pd_get_launch_count": (st, [vp, P(C.c_longlong)]),
+        "pd_get_stream": (st, [vp, P(vp)]),
+        "pd_synchronize": (st, [vp]),
         "pd_status_string": (C.c_char_p, [C.c_int]),
         "pd_last_error_message": (C.c_char_p, [vp]),
         "pd_abi_version": (C.c_int, []),
@@ -348,6 +350,15 @@ class Simulator:
 
     def reset_kernel_times(self):
         _check(self.lib.pd_reset_kernel_times(self.h), self.h)
+
+    def stream_handle(self) -> int:
+        """cudaStream_t of this simulator, as an integer (for CUDA events)."""
+        v = C.c_void_p()
+        _check(self.lib.pd_get_stream(self.h, C.byref(v)), self.h)
+        return v.value or 0
+
+    def synchronize(self):
+        _check(self.lib.pd_synchronize(self.h), self.h)
 
     def launch_count(self) -> int:
         v = C.c_longlong()

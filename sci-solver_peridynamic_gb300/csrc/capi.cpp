@@ -199,4 +199,18 @@ pd_status pd_get_launch_count(pd_handle* h, long long* launches)
     return PD_OK;
 }
 
+pd_status pd_get_stream(pd_handle* h, void** stream)
+{
+    ENG(h);
+    if (!stream) return PD_ERR_INVALID_ARGUMENT;
+    *stream = (void*)h->eng->stream();
+    return PD_OK;
+}
+
+pd_status pd_synchronize(pd_handle* h)
+{
+    ENG(h);
+    return h->eng->synchronize();
+}
+
 }  // extern "C"

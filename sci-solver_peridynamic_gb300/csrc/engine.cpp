@@ -317,6 +317,13 @@ StepParams Engine::step_params() const
     return P;
 }
 
+pd_status Engine::synchronize()
+{
+    CK(cudaSetDevice(device_), "cudaSetDevice");
+    CK(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+    return PD_OK;
+}
+
 bool Engine::finished() const { return step_ > run_.final_step || !cg_converged_; }
 
 pd_status Engine::advance(int nsteps)

@@ -32,6 +32,8 @@ public:
     pd_status kernel_times(pd_kernel_times* t);
     void reset_kernel_times();
     long long launches() const { return launches_; }
+    cudaStream_t stream() const { return stream_; }
+    pd_status synchronize();
     const std::string& error() const { return err_; }
 
 private:

@@ -146,10 +146,12 @@ def cube_lattice(n_side=16, spacing=0.02, seed=0, jitter=0.05, coeff=5.0, s0=0.0
 
 def ellipsoid_impact(target_n=1_000_000, semi_axes=(0.5, 0.35, 0.3), seed=0, jitter=0.05, coeff=5.0, s0=0.015,
                      dt=5e-5, cg_tol=1e-6, precision=PRECISION_MIXED, steps=200, sphere_radius=0.1,
-                     sphere_speed=10.0, spacing=None):
+                     sphere_speed=10.0, spacing=None, gap=1.0):
     """Jittered lattice filling an ellipsoid, struck along -x by a rigid
     sphere (penalty contact), Newmark-beta dt = 5e-5, CG rel. tol 1e-6.
-    The spacing is chosen so the particle count is ~target_n."""
+    The spacing is chosen so the particle count is ~target_n.  The sphere
+    starts `gap` spacings beyond the outermost particle (gap <= 0: in
+    contact from the first step)."""
     a, b, c = semi_axes
     if spacing is None:
         spacing = (4.0 / 3.0 * math.pi * a * b * c / target_n) ** (1.0 / 3.0)
@@ -176,7 +178,7 @@ def ellipsoid_impact(target_n=1_000_000, semi_axes=(0.5, 0.35, 0.3), seed=0, jit
     opt.box_enabled = 0
     opt.sphere_enabled = 1
     opt.sphere_radius = sphere_radius
-    opt.sphere_center[:] = (pos[:, 0].max() + sphere_radius + spacing, 0.0, 0.0)
+    opt.sphere_center[:] = (pos[:, 0].max() + sphere_radius + gap * spacing, 0.0, 0.0)
     opt.sphere_velocity[:] = (-sphere_speed, 0.0, 0.0)
     opt.sphere_stiffness = 10.0 * cstiff / spacing
     return Scene("ellipsoid_impact", sim, run, opt, pos, vel, act, steps,

@@ -50,10 +50,11 @@ def test_bonds_cube_lattice(pdgb, scenes):
     assert same_sets(sim.alive_sets(), ora.alive_sets())
 
 
-@pytest.mark.parametrize("coeff,interior", [(4.001, 26), (5.001, 80), (6.001, 92)])
+@pytest.mark.parametrize("coeff,interior", [(3.999, 26), (4.001, 32), (5.001, 80), (5.999, 92), (6.001, 122)])
 def test_bond_count_known_answer(pdgb, scenes, coeff, interior):
-    """Unjittered lattice: interior particles have 26 / 80 / 92 bonds for
-    horizons of 2 / 2.5 / 3 spacings."""
+    """Unjittered lattice, horizon = coeff * spacing / 2: an interior particle
+    bonds every lattice vector v with |v| < coeff/2 spacings (|v|^2 in
+    {1,2,3} -> 26, +{4} -> 32, +{5,6} -> 80, +{8} -> 92, +{9} -> 122)."""
     sc = scenes.reference_block(n_side=9, pd_kernel_coeff=coeff, jitter=0.0)
     sim = scenes.make_simulator(sc)
     sim.makeReady()
@@ -92,8 +93,11 @@ def test_cube_lattice_mixed_100_steps(pdgb, scenes):
     sc = scenes.cube_lattice()
     sim, ora = _run_pair(pdgb, scenes, sc, 100, check_every=20)
     assert rel_err(sim.get(pdgb.VAR_POSITION), ora.position) < MIXED_TOL
+    # implicit Euler damps the impact out: the block is at rest after 100 steps,
+    # so velocity errors are measured against the initial speed (5 m/s)
     v, vo = sim.get(pdgb.VAR_VELOCITY), ora.velocity
-    assert np.abs(v - vo)[:, :3].max() / np.abs(vo).max() < 1e-3
+    vscale = max(np.abs(vo).max(), np.abs(sc.vel).max())
+    assert np.abs(v - vo)[:, :3].max() / vscale < MIXED_TOL
     assert sim.CGConvergence()
 
 
