@@ -144,7 +144,8 @@ typedef enum pd_variable {
     PD_VAR_BOND_ROW_PTR = 9,       /* int64[n+1]: row starts of the bond list below */
     PD_VAR_BOND_LIST = 10,         /* int32[total]: per particle, live neighbours ascending then broken ones ascending */
     PD_VAR_POSITION_SCALED = 11,   /* double[4n]: positions * scaleFactor (DataIO convention) */
-    PD_VAR_ORIGINAL_POSITION = 12  /* double[4n]: pd_original_pos */
+    PD_VAR_ORIGINAL_POSITION = 12, /* double[4n]: pd_original_pos */
+    PD_VAR_SLOT_PERMUTATION = 13   /* int32[n]: caller index of each device slot (operator view order) */
 } pd_variable;
 
 typedef struct pd_step_stats {
@@ -174,6 +175,36 @@ typedef struct pd_kernel_times {
     long long launches[PD_KC_COUNT];
     double total_ms[PD_KC_COUNT];
 } pd_kernel_times;
+
+/* Device-side view of a handle's current linear system A = M + beta h^2 K
+ * (beta = 1 implicit Euler, 1/4 Newmark), for applying the matrix-free
+ * operator outside pd_advance: the role of the reference's
+ * PeridynamicsMatrix linear operator (src/core/cg_solver.cuh:386-428).
+ * Pointers are device pointers into the handle's state, valid until the next
+ * pd_make_ready or pd_destroy.  Vectors are in slot order (perm[slot] = caller
+ * index), 4 components per particle (float in mixed precision, double in
+ * FP64 mode; w ignored).  Dirichlet rows (clamped, prescribed, invisible)
+ * map to 0. */
+typedef struct pd_operator_view {
+    int n;                         /* particles */
+    int precision;                 /* pd_precision of the vectors */
+    int lanes_per_particle;        /* 4, 8, 16 or 32 */
+    int blocks;                    /* thread blocks of a launch; 0 = automatic */
+    const uint8_t* activity;       /* n: low 3 bits pd_activity, bit 3 = in sphere contact */
+    const int32_t* row_ptr;        /* n + 1 */
+    const int32_t* bond_count;     /* n: live bonds per row */
+    const int32_t* bond_slot;      /* neighbour slots of each row */
+    const int32_t* perm;           /* n: slot -> caller index */
+    const void* ref_pos;           /* mixed: float4 original positions minus origin */
+    const void* disp;              /* mixed: float4 displacement x - X */
+    const double* jac;             /* FP64: 6 entries per bond slot (xx yy zz xy xz yz) */
+    const double* jac_diag;        /* FP64: 6 entries per particle */
+    double mass;
+    double t2;                     /* beta h^2 */
+    double bond_coeff;
+    double sphere_center_local[3]; /* sphere centre minus origin (mixed contact rows) */
+    double sphere_stiffness;
+} pd_operator_view;
 
 typedef struct pd_handle pd_handle;
 
@@ -226,6 +257,17 @@ pd_status pd_get_size(pd_handle* h, pd_variable var, size_t* bytes);
 pd_status pd_get_stats(pd_handle* h, pd_step_stats* stats);
 /* Resolved solver options and simulation parameters in use (after derive). */
 pd_status pd_get_params(pd_handle* h, pd_sim_params* sim, pd_run_params* run, pd_solver_options* opt);
+
+/* ---- the system operator (PeridynamicsMatrix, src/core/cg_solver.cuh:386-428) */
+
+/* Fills a view of the operator of the current step (after pd_make_ready; the
+ * time step and contact state of the latest pd_advance). */
+pd_status pd_get_operator_view(pd_handle* h, pd_operator_view* view);
+/* y = A x on device vectors (PeridynamicsMatrix::operator(), which launches
+ * computeAx, cg_solver.cuh:343-383, 414-427); *d_dot (device double, may be
+ * NULL) receives <x, A x>.  Runs on the handle's stream with the handle's
+ * scratch; returns after enqueueing. */
+pd_status pd_apply_operator(pd_handle* h, const void* d_x, void* d_y, double* d_dot);
 
 /* ---- profiling (Monitor, src/core/monitor.cu:53-95) ----------------------- */
 pd_status pd_set_profiling(pd_handle* h, int enabled);

@@ -38,7 +38,7 @@ PRECISION_MIXED, PRECISION_FP64 = 0, 1
 # pd_variable
 (VAR_POSITION, VAR_VELOCITY, VAR_ACTIVITY, VAR_BOND_COUNT, VAR_STRETCH, VAR_ORIGINAL_STRETCH,
  VAR_NEW_STRETCH, VAR_FORCE, VAR_SOLUTION, VAR_BOND_ROW_PTR, VAR_BOND_LIST, VAR_POSITION_SCALED,
- VAR_ORIGINAL_POSITION) = range(13)
+ VAR_ORIGINAL_POSITION, VAR_SLOT_PERMUTATION) = range(14)
 # pd_kernel_class
 KC_FORCE, KC_SPMV, KC_CG_VECTOR, KC_UPDATE = range(4)
 KC_NAMES = ("force", "spmv", "cg_vector", "update")
@@ -108,6 +108,17 @@ class StepStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class OperatorView(C.Structure):
+    """pd_operator_view: device-side view of the current system operator."""
+    _fields_ = [
+        ("n", C.c_int), ("precision", C.c_int), ("lanes_per_particle", C.c_int), ("blocks", C.c_int),
+        ("activity", C.c_void_p), ("row_ptr", C.c_void_p), ("bond_count", C.c_void_p),
+        ("bond_slot", C.c_void_p), ("perm", C.c_void_p), ("ref_pos", C.c_void_p), ("disp", C.c_void_p),
+        ("jac", C.c_void_p), ("jac_diag", C.c_void_p), ("mass", C.c_double), ("t2", C.c_double),
+        ("bond_coeff", C.c_double), ("sphere_center_local", C.c_double * 3), ("sphere_stiffness", C.c_double),
+    ]
+
+
 class KernelTimes(C.Structure):
     _fields_ = [("launches", C.c_longlong * 4), ("total_ms", C.c_double * 4)]
 
@@ -153,6 +164,8 @@ def library(build_if_missing: bool = True):
         "pd_reset_kernel_times": (st, [vp]),
         "pd_get_launch_count": (st, [vp, P(C.c_longlong)]),
         "pd_get_stream": (st, [vp, P(vp)]),
+        "pd_get_operator_view": (st, [vp, P(OperatorView)]),
+        "pd_apply_operator": (st, [vp, vp, vp, vp]),
         "pd_synchronize": (st, [vp]),
         "pd_status_string": (C.c_char_p, [C.c_int]),
         "pd_last_error_message": (C.c_char_p, [vp]),
@@ -297,7 +310,7 @@ class Simulator:
     def get(self, var: int) -> np.ndarray:
         size = C.c_size_t()
         _check(self.lib.pd_get_size(self.h, var, C.byref(size)), self.h)
-        if var in (VAR_ACTIVITY, VAR_BOND_COUNT, VAR_BOND_LIST):
+        if var in (VAR_ACTIVITY, VAR_BOND_COUNT, VAR_BOND_LIST, VAR_SLOT_PERMUTATION):
             out = np.zeros(size.value // 4, np.int32)
         elif var == VAR_BOND_ROW_PTR:
             out = np.zeros(size.value // 8, np.int64)
@@ -350,6 +363,16 @@ class Simulator:
 
     def reset_kernel_times(self):
         _check(self.lib.pd_reset_kernel_times(self.h), self.h)
+
+    def operator_view(self) -> OperatorView:
+        v = OperatorView()
+        _check(self.lib.pd_get_operator_view(self.h, C.byref(v)), self.h)
+        return v
+
+    def apply_operator(self, d_x: int, d_y: int, d_dot: int | None = None):
+        """y = A x on device vectors given as raw device pointers (slot order)."""
+        _check(self.lib.pd_apply_operator(self.h, C.c_void_p(d_x), C.c_void_p(d_y),
+                                          C.c_void_p(d_dot) if d_dot else None), self.h)
 
     def stream_handle(self) -> int:
         """cudaStream_t of this simulator, as an integer (for CUDA events)."""

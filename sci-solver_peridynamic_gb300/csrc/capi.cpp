@@ -199,6 +199,19 @@ pd_status pd_get_launch_count(pd_handle* h, long long* launches)
     return PD_OK;
 }
 
+pd_status pd_get_operator_view(pd_handle* h, pd_operator_view* view)
+{
+    ENG(h);
+    if (!view) return PD_ERR_INVALID_ARGUMENT;
+    return h->eng->operator_view(view);
+}
+
+pd_status pd_apply_operator(pd_handle* h, const void* d_x, void* d_y, double* d_dot)
+{
+    ENG(h);
+    return h->eng->apply_operator(d_x, d_y, d_dot);
+}
+
 pd_status pd_get_stream(pd_handle* h, void** stream)
 {
     ENG(h);

@@ -280,6 +280,7 @@ pd_status Engine::make_ready()
     last_iters_ = 0;
     total_iters_ = 0;
     predicted_iters_ = 0;
+    last_params_ = step_params();
     ready_ = true;
     return PD_OK;
 }
@@ -324,6 +325,48 @@ pd_status Engine::synchronize()
     return PD_OK;
 }
 
+pd_status Engine::operator_view(pd_operator_view* v) const
+{
+    if (!ready_) return PD_ERR_NOT_READY;
+    std::memset(v, 0, sizeof(*v));
+    const StepParams& P = last_params_;
+    v->n = n_;
+    v->precision = fp64_ ? PD_PRECISION_FP64 : PD_PRECISION_MIXED;
+    v->lanes_per_particle = L_.lanes;
+    v->blocks = L_.grid_bonds;
+    v->activity = S_.act;
+    v->row_ptr = S_.row_ptr;
+    v->bond_count = S_.cnt;
+    v->bond_slot = S_.col;
+    v->perm = d_perm_;
+    v->ref_pos = S_.X32;
+    v->disp = S_.u32;
+    v->jac = S_.jac;
+    v->jac_diag = S_.jdiag;
+    v->mass = P.mass;
+    v->t2 = P.t2;
+    v->bond_coeff = P.bond_coeff;
+    for (int k = 0; k < 3; ++k) v->sphere_center_local[k] = P.sphere_c_local[k];
+    v->sphere_stiffness = P.sphere_k;
+    return PD_OK;
+}
+
+pd_status Engine::apply_operator(const void* d_x, void* d_y, double* d_dot)
+{
+    if (!ready_) {
+        err_ = "apply_operator: make_ready has not run";
+        return PD_ERR_NOT_READY;
+    }
+    if ((!d_x || !d_y) && n_ > 0) return PD_ERR_INVALID_ARGUMENT;
+    CK(cudaSetDevice(device_), "cudaSetDevice");
+    // counter 4 of the handle's reduction scratch is reserved for this call
+    ReduceSlot slot{S_.partials, S_.counters + 4};
+    launch_operator(fp64_, last_params_, S_, L_.lanes, L_.grid_bonds, d_x, d_y, slot, d_dot, stream_);
+    ++launches_;
+    CK(cudaGetLastError(), "apply_operator launch");
+    return PD_OK;
+}
+
 bool Engine::finished() const { return step_ > run_.final_step || !cg_converged_; }
 
 pd_status Engine::advance(int nsteps)
@@ -356,11 +399,11 @@ pd_status Engine::advance(int nsteps)
 pd_status Engine::integrate(bool* advanced)
 {
     *advanced = false;
-    const StepParams P = step_params();
+    const StepParams Pf = step_params();   // force pass: does not depend on the time step
     const size_t N = (size_t)n_;
     CK(cudaMemsetAsync(S_.flags, 0, sizeof(int) * 2, stream_), "memset flags");
     mark_begin(PD_KC_FORCE, -1);
-    launch_force(fp64_, P, S_, L_, stream_);
+    launch_force(fp64_, Pf, S_, L_, stream_);
     mark_end();
     ++launches_;
     const bool adaptive = run_.integrator == PD_NEWMARK_BETA || run_.adaptive_integration != 0;
@@ -375,7 +418,7 @@ pd_status Engine::integrate(bool* advanced)
             CK(cudaMemcpyAsync(S_.cnt, S_.cnt_bk, sizeof(int) * N, cudaMemcpyDeviceToDevice, stream_), "restore cnt");
             CK(cudaMemcpyAsync(S_.x64, S_.x64_bk, sizeof(dbl4) * N, cudaMemcpyDeviceToDevice, stream_), "restore x");
             CK(cudaMemcpyAsync(S_.v64, S_.v64_bk, sizeof(dbl4) * N, cudaMemcpyDeviceToDevice, stream_), "restore v");
-            launch_refresh(fp64_, P, S_, L_, stream_);
+            launch_refresh(fp64_, Pf, S_, L_, stream_);
             ++launches_;
             return PD_OK;
         }
@@ -383,6 +426,10 @@ pd_status Engine::integrate(bool* advanced)
         CK(cudaMemcpyAsync(S_.x64_bk, S_.x64, sizeof(dbl4) * N, cudaMemcpyDeviceToDevice, stream_), "backup x");
         CK(cudaMemcpyAsync(S_.v64_bk, S_.v64, sizeof(dbl4) * N, cudaMemcpyDeviceToDevice, stream_), "backup v");
     }
+    // the assembly, solve and update of this step use the time step as the
+    // adaptive decision left it (the reference doubles it in place)
+    const StepParams P = step_params();
+    last_params_ = P;
     pd_status s = solve(P);
     if (s != PD_OK) return s;
     mark_begin(PD_KC_UPDATE, -1);
@@ -574,7 +621,8 @@ pd_status Engine::get_size(pd_variable var, size_t* bytes) const
     case PD_VAR_POSITION: case PD_VAR_VELOCITY: case PD_VAR_FORCE: case PD_VAR_SOLUTION:
     case PD_VAR_POSITION_SCALED: case PD_VAR_ORIGINAL_POSITION:
         *bytes = 4 * N * sizeof(double); return PD_OK;
-    case PD_VAR_ACTIVITY: case PD_VAR_BOND_COUNT: *bytes = N * sizeof(int32_t); return PD_OK;
+    case PD_VAR_ACTIVITY: case PD_VAR_BOND_COUNT: case PD_VAR_SLOT_PERMUTATION:
+        *bytes = N * sizeof(int32_t); return PD_OK;
     case PD_VAR_STRETCH: case PD_VAR_ORIGINAL_STRETCH: case PD_VAR_NEW_STRETCH: *bytes = N * sizeof(double); return PD_OK;
     case PD_VAR_BOND_ROW_PTR: *bytes = (N + 1) * sizeof(int64_t); return PD_OK;
     case PD_VAR_BOND_LIST: *bytes = (size_t)bonds_initial_ * sizeof(int32_t); return PD_OK;
@@ -622,6 +670,9 @@ pd_status Engine::get(pd_variable var, void* dst, size_t bytes)
     case PD_VAR_NEW_STRETCH: return download_scatter(S_.nst, (double*)dst, 1, N);
     case PD_VAR_BOND_ROW_PTR: return export_bonds((int64_t*)dst, nullptr);
     case PD_VAR_BOND_LIST: return export_bonds(nullptr, (int32_t*)dst);
+    case PD_VAR_SLOT_PERMUTATION:
+        std::memcpy(dst, perm_.data(), N * sizeof(int32_t));
+        return PD_OK;
     default: return PD_ERR_INVALID_ARGUMENT;
     }
 }

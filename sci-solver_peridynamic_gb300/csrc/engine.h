@@ -34,6 +34,8 @@ public:
     long long launches() const { return launches_; }
     cudaStream_t stream() const { return stream_; }
     pd_status synchronize();
+    pd_status operator_view(pd_operator_view* v) const;
+    pd_status apply_operator(const void* d_x, void* d_y, double* d_dot);
     const std::string& error() const { return err_; }
 
 private:
@@ -81,6 +83,7 @@ private:
     CgScalars* h_sc_ = nullptr;   // pinned
     int* h_flags_ = nullptr;      // pinned
     LaunchCfg L_{};
+    StepParams last_params_{};   // constants of the latest step (the operator's time step)
     // step state (Simulator members)
     int step_ = 0;
     int substep_ = 0;

@@ -145,11 +145,6 @@ __device__ __forceinline__ double warp_total(DotAcc64 a)
 // Every block contributes one FP64 partial; the last block to arrive sums the
 // partials in index order (deterministic for a fixed grid) and runs `fin`
 // on thread 0.  Must be reached by every thread of the block.
-struct ReduceSlot {
-    double* partials;       // >= gridDim.x entries
-    unsigned int* counter;  // zero before the launch; reset by the finisher
-};
-
 template <typename Acc, typename Fin>
 __device__ __forceinline__ void block_reduce_finish(Acc acc, ReduceSlot slot, Fin fin)
 {

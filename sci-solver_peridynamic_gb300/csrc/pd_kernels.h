@@ -41,6 +41,13 @@ struct CgScalars {
     int max_iter;
 };
 
+// Partial-sum scratch of a reducing launch: one double per block and an
+// arrival counter that is zero before the launch (the last block resets it).
+struct ReduceSlot {
+    double* partials;
+    unsigned int* counter;
+};
+
 // Per-step constants, passed by value to the step kernels.
 struct StepParams {
     int n;
@@ -108,6 +115,10 @@ void launch_force(bool fp64, const StepParams& P, const DeviceState& S, const La
 void launch_cg_init(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
 // y = A(x) (dot = false) or y = A(p) with <p,y> reduced into alpha (dot = true)
 void launch_spmv(bool fp64, bool dot, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
+// y = A(in) with the reduction slot given by the caller; dot_out (device,
+// may be null) receives <in, A in>.  Used by the operator entry points.
+void launch_operator(bool fp64, const StepParams& P, const DeviceState& S, int lanes, int grid, const void* in,
+                     void* out, ReduceSlot slot, double* dot_out, cudaStream_t st);
 void launch_cg_residual(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
 void launch_cg_axpy(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
 void launch_cg_xpby(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);

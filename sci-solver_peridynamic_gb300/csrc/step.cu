@@ -70,12 +70,14 @@ __global__ void __launch_bounds__(kBlock) k_force(StepParams P, DeviceState S)
     constexpr int gpb = kBlock / G;
     const int stride = gridDim.x * gpb;
     V4* force = (V4*)S.force;
-    V4* rhs = (V4*)S.rhs;
     for (int p = blockIdx.x * gpb + threadIdx.x / G; p < P.n; p += stride) {
         const int a = S.act[p] & kActMask;
-        if (a == ACT_INVISIBLE) continue;
         const dbl4 xp = S.x64[p];
         const dbl4 Xp = S.X64[p];
+        // FP32 displacement of this step's linear system (read by k_spmv)
+        if (!FP64 && lane == 0)
+            S.u32[p] = make_float4((float)(xp.x - Xp.x), (float)(xp.y - Xp.y), (float)(xp.z - Xp.z), 0.f);
+        if (a == ACT_INVISIBLE) continue;
         const float thp = (float)S.st[p];
         const int rs = S.row_ptr[p];
         const int c = S.cnt[p];
@@ -217,20 +219,6 @@ __global__ void __launch_bounds__(kBlock) k_force(StepParams P, DeviceState S)
                 double* D = S.jdiag + 6ll * p;
                 D[0] = j0; D[1] = j1; D[2] = j2; D[3] = j3; D[4] = j4; D[5] = j5;
             }
-            // right-hand side (fillVectorB*): b = m v + h f, or b = h (m v + (h/2) f)
-            const dbl4 v = S.v64[p];
-            double b0, b1, b2;
-            if (P.integrator == 0) {
-                b0 = dadd(dmul(P.mass, v.x), dmul(P.h, f0));
-                b1 = dadd(dmul(P.mass, v.y), dmul(P.h, f1));
-                b2 = dadd(dmul(P.mass, v.z), dmul(P.h, f2));
-            } else {
-                const double hh = dmul(0.5, P.h);
-                b0 = dmul(P.h, dadd(dmul(P.mass, v.x), dmul(hh, f0)));
-                b1 = dmul(P.h, dadd(dmul(P.mass, v.y), dmul(hh, f1)));
-                b2 = dmul(P.h, dadd(dmul(P.mass, v.z), dmul(hh, f2)));
-            }
-            rhs[p] = make_v4<V4>(b0, b1, b2);
         }
     }
 }
@@ -240,14 +228,18 @@ __global__ void __launch_bounds__(kBlock) k_force(StepParams P, DeviceState S)
 // xi = xi0 + delta, the bond Jacobian applied to w = u_p - u_q is
 //   c [ (1/d0 - 1/d) w + (xi . w) xi / d^3 ]
 // which equals (c/d0)[(1 - d0/d) I + (d0/d) e e^T] w of cg_solver.cuh:292-299.
+// DOT: reduce <in, A in>; with `cg` set (CG iteration) the result becomes
+// alpha = rz / <p, A p> and the launch is skipped once the CG has finished;
+// with `dot_out` set the result is also stored there.
 template <int G, bool FP64, bool DOT>
 __global__ void __launch_bounds__(kBlock) k_spmv(StepParams P, DeviceState S, const void* __restrict__ in_,
-                                                  void* __restrict__ out_, ReduceSlot slot)
+                                                  void* __restrict__ out_, ReduceSlot slot, CgScalars* cg,
+                                                  double* dot_out)
 {
     using Real = typename std::conditional<FP64, double, float>::type;
     using V4 = typename Vec4<Real>::type;
     using Acc = typename DotAccFor<Real>::type;
-    if (DOT && ((volatile CgScalars*)S.sc)->done) return;
+    if (DOT && cg && ((volatile CgScalars*)cg)->done) return;
     const V4* __restrict__ in = (const V4*)in_;
     V4* __restrict__ out = (V4*)out_;
     const unsigned gmask = group_mask<G>();
@@ -339,15 +331,21 @@ __global__ void __launch_bounds__(kBlock) k_spmv(StepParams P, DeviceState S, co
         }
     }
     if (DOT) {
-        CgScalars* sc = S.sc;
-        block_reduce_finish(acc, slot, [sc](double pAp) {
-            sc->pAp = pAp;
-            sc->alpha = sc->rz / pAp;
+        block_reduce_finish(acc, slot, [cg, dot_out](double pAp) {
+            if (cg) {
+                cg->pAp = pAp;
+                cg->alpha = cg->rz / pAp;
+            }
+            if (dot_out) *dot_out = pAp;
         });
     }
 }
 
 // ---- CG vector kernels (CUSP krylov::cg, identity preconditioner) ----------------
+// Right-hand side with this step's final time step (the adaptive scheme may
+// have changed it after the force pass, simulator.cu:540-572, before
+// fillVectorB*): b = m v + h f (implicit_euler.cuh:83-84) or
+// b = h (m v + (h/2) f) (newmark_beta.cuh:264-265).
 // Dirichlet values: clamped and invisible particles 0, prescribed particles their
 // velocity (implicit Euler) or h * velocity (Newmark); ||b|| over free rows.
 template <bool FP64>
@@ -357,10 +355,27 @@ __global__ void __launch_bounds__(kBlock) k_cg_init(StepParams P, DeviceState S,
     using V4 = typename Vec4<Real>::type;
     using Acc = typename DotAccFor<Real>::type;
     V4* x = (V4*)S.sol;
-    const V4* b = (const V4*)S.rhs;
+    V4* b = (V4*)S.rhs;
+    const V4* force = (const V4*)S.force;
     Acc acc;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
         const int a = S.act[i] & kActMask;
+        {
+            const dbl4 v = S.v64[i];
+            const V4 f = force[i];
+            double b0, b1, b2;
+            if (P.integrator == 0) {
+                b0 = dadd(dmul(P.mass, v.x), dmul(P.h, (double)f.x));
+                b1 = dadd(dmul(P.mass, v.y), dmul(P.h, (double)f.y));
+                b2 = dadd(dmul(P.mass, v.z), dmul(P.h, (double)f.z));
+            } else {
+                const double hh = dmul(0.5, P.h);
+                b0 = dmul(P.h, dadd(dmul(P.mass, v.x), dmul(hh, (double)f.x)));
+                b1 = dmul(P.h, dadd(dmul(P.mass, v.y), dmul(hh, (double)f.y)));
+                b2 = dmul(P.h, dadd(dmul(P.mass, v.z), dmul(hh, (double)f.z)));
+            }
+            b[i] = make_v4<V4>(b0, b1, b2);
+        }
         if (is_dirichlet(a)) {
             double ux = 0, uy = 0, uz = 0;
             if (a == ACT_PRESCRIBED) {
@@ -551,10 +566,6 @@ __global__ void __launch_bounds__(kBlock) k_update(StepParams P, DeviceState S)
             for (int k = 0; k < 3; ++k) reflect(P, np[k], nv[k], k);
         S.x64[i] = make_dbl4(np[0], np[1], np[2], 0.0);
         S.v64[i] = make_dbl4(nv[0], nv[1], nv[2], 0.0);
-        if (!FP64) {
-            const dbl4 X = S.X64[i];
-            S.u32[i] = make_float4((float)(np[0] - X.x), (float)(np[1] - X.y), (float)(np[2] - X.z), 0.f);
-        }
     }
 }
 
@@ -589,29 +600,36 @@ void launch_force(bool fp64, const StepParams& P, const DeviceState& S, const La
 }
 
 template <int G, bool DOT>
-static void spmv_g(bool fp64, const StepParams& P, const DeviceState& S, int grid, cudaStream_t st)
+static void spmv_g(bool fp64, const StepParams& P, const DeviceState& S, int grid, const void* in, void* out,
+                   ReduceSlot slot, CgScalars* cg, double* dot_out, cudaStream_t st)
 {
-    const void* in = DOT ? S.p : S.sol;
-    void* out = S.y;
-    if (fp64) k_spmv<G, true, DOT><<<grid, kBlock, 0, st>>>(P, S, in, out, slot_of(S, 1));
-    else k_spmv<G, false, DOT><<<grid, kBlock, 0, st>>>(P, S, in, out, slot_of(S, 1));
+    if (fp64) k_spmv<G, true, DOT><<<grid, kBlock, 0, st>>>(P, S, in, out, slot, cg, dot_out);
+    else k_spmv<G, false, DOT><<<grid, kBlock, 0, st>>>(P, S, in, out, slot, cg, dot_out);
 }
 
 template <bool DOT>
-static void spmv_d(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st)
+static void spmv_d(bool fp64, const StepParams& P, const DeviceState& S, int lanes, int grid, const void* in,
+                   void* out, ReduceSlot slot, CgScalars* cg, double* dot_out, cudaStream_t st)
 {
-    switch (L.lanes) {
-    case 4: spmv_g<4, DOT>(fp64, P, S, L.grid_bonds, st); break;
-    case 16: spmv_g<16, DOT>(fp64, P, S, L.grid_bonds, st); break;
-    case 32: spmv_g<32, DOT>(fp64, P, S, L.grid_bonds, st); break;
-    default: spmv_g<8, DOT>(fp64, P, S, L.grid_bonds, st); break;
+    switch (lanes) {
+    case 4: spmv_g<4, DOT>(fp64, P, S, grid, in, out, slot, cg, dot_out, st); break;
+    case 16: spmv_g<16, DOT>(fp64, P, S, grid, in, out, slot, cg, dot_out, st); break;
+    case 32: spmv_g<32, DOT>(fp64, P, S, grid, in, out, slot, cg, dot_out, st); break;
+    default: spmv_g<8, DOT>(fp64, P, S, grid, in, out, slot, cg, dot_out, st); break;
     }
 }
 
 void launch_spmv(bool fp64, bool dot, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st)
 {
-    if (dot) spmv_d<true>(fp64, P, S, L, st);
-    else spmv_d<false>(fp64, P, S, L, st);
+    if (dot) spmv_d<true>(fp64, P, S, L.lanes, L.grid_bonds, S.p, S.y, slot_of(S, 1), S.sc, nullptr, st);
+    else spmv_d<false>(fp64, P, S, L.lanes, L.grid_bonds, S.sol, S.y, slot_of(S, 1), nullptr, nullptr, st);
+}
+
+void launch_operator(bool fp64, const StepParams& P, const DeviceState& S, int lanes, int grid, const void* in,
+                     void* out, ReduceSlot slot, double* dot_out, cudaStream_t st)
+{
+    if (dot_out) spmv_d<true>(fp64, P, S, lanes, grid, in, out, slot, nullptr, dot_out, st);
+    else spmv_d<false>(fp64, P, S, lanes, grid, in, out, slot, nullptr, nullptr, st);
 }
 
 void launch_cg_init(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st)

@@ -121,3 +121,14 @@ def test_tiny_scenes(pdgb, scenes, n_side):
     sc.opt.precision = pdgb.PRECISION_FP64
     sim, ora = _run_pair(pdgb, scenes, sc, 5, check_every=5)
     assert rel_err(sim.get(pdgb.VAR_POSITION), ora.position) < FP64_TOL
+
+
+@pytest.mark.parametrize("precision,tol", [(1, FP64_TOL), (0, MIXED_TOL)])
+def test_newmark_dt_halving_and_doubling(pdgb, scenes, precision, tol):
+    """Breaking stops mid-run: pd_time_step goes 128 -> 64 -> 128 -> 64 -> 128;
+    the doubled step is used by the same step's assembly, solve and update."""
+    sc = scenes.reference_block(n_side=7, seed=5, integrator=pdgb.NEWMARK_BETA, adaptive=1, expansion=150.0,
+                                cg_tol=1e-10)
+    sc.opt.precision = precision
+    sim, ora = _run_pair(pdgb, scenes, sc, 90, check_every=5)
+    assert rel_err(sim.get(pdgb.VAR_POSITION), ora.position) < tol

@@ -1,0 +1,135 @@
+"""Host-side logic, no GPU: the C ABI library loads and exports every entry
+point declared in include/pd_gb300.h; parameter derivation follows
+SystemParameter; the s0 stream matches glibc's rand() after srand(1973);
+the adaptive time-step state machine; failure of device calls without a GPU."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = []
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if not h.endswith(".h"):
+            continue
+        text = open(os.path.join(ROOT, "include", h)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names += re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\*?\s*(pd_[a-z_0-9]+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol(pdgb):
+    lib = pdgb.library()
+    names = declared_functions()
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_abi_version(pdgb):
+    assert pdgb.library().pd_abi_version() == 1
+
+
+def test_params_file_and_derivation(pdgb, tmp_path):
+    """Keys of the reference's params.txt; derived values of
+    calculateDependentParameters (parameters.cu:351-453)."""
+    f = tmp_path / "params.txt"
+    f.write_text("\n".join([
+        "gpu_device 0", "adaptive_integration 1 ", "num_pd_particle 10000", "pd_stretch_limit_s0 1e-3",
+        "steps_per_frame 10", "final_step 100", "radius_pd_over_sph 1", "boundary_min_x 0", "boundary_min_y 0",
+        "boundary_min_z 0", "boundary_max_x 2", "boundary_max_y 2", "boundary_max_z 4", "sph_kernel_coeff 4.001",
+        "pd_kernel_coeff 5.001", "pd_particle_mass 1000", "// a comment line", "", "integrator newmark_beta",
+        "sph_sph_viscosity 1e-5",
+    ]))
+    sp = pdgb.SystemParameter(str(f))
+    s, r = sp.getSimulationParameters(), sp.getRunningParameters()
+    assert r.adaptive_integration == 1 and r.step_per_frame == 10 and r.final_step == 100
+    assert r.integrator == pdgb.NEWMARK_BETA
+    assert r.pd_stretch_limit_s0 == np.float32(1e-3)
+    cell = float(np.float32(max(np.float32(2 / 32), np.float32(2 / 32), np.float32(4 / 64))))
+    sph_r = cell / 4.001
+    rad = 1.0 * sph_r
+    scale = 2 * rad / 0.0005
+    assert s.cell_size == cell / scale
+    assert s.pd_particle_radius == rad / scale
+    assert s.pd_horizon == rad * 5.001 / scale
+    assert s.pd_C_times_V == 18.0 / 3.14159265358979323846264 / 2.0 / 1296.0 / rad
+    assert s.scaleFactor == scale
+    assert s.boundary_max_z == 4 / scale
+    assert s.pd_time_step == 128 and s.num_pd_particle == 10000
+
+
+def test_params_missing_file(pdgb):
+    with pytest.raises(pdgb.PdError) as e:
+        pdgb.SystemParameter("/nonexistent/params.txt")
+    assert e.value.status == 6
+
+
+def test_stretch_stream_matches_glibc_rand(pdgb, oracle_mod):
+    """pd_sample_stretch_limits restates glibc's rand(); the oracle calls the
+    C library's rand() after srand(1973) (simulator.cu:802-822, 852-857)."""
+    for s0 in (1e-3, 0.015, 0.02):
+        a = pdgb.sample_stretch_limits(s0, 5000)
+        b = oracle_mod.sample_stretch(5000, float(np.float32(s0)))
+        np.testing.assert_array_equal(a, b)
+    libc = ctypes.CDLL(None)
+    libc.srand(1973)
+    raw = [libc.rand() for _ in range(24)]
+    s = sum(x / 2147483647.0 for x in raw[:12]) - 6.0
+    assert pdgb.sample_stretch_limits(0.02, 2)[0] == (s * 0.01 + 1.0) * float(np.float32(0.02))
+
+
+def reference_decide(has_broken, ticks, substep, base=128, tmin=100, maxsub=10):
+    """simulator.cu:339-392 restated."""
+    if has_broken:
+        if ticks > tmin:
+            return ticks // 2, substep, True
+        substep = 1
+    else:
+        if substep > 0:
+            substep += 1
+        if substep >= maxsub:
+            ticks *= 2
+            substep = 0 if ticks >= base else 1
+    return ticks, substep, False
+
+
+def test_adaptive_state_machine(pdgb):
+    rng = np.random.default_rng(0)
+    t, s = 128, 0
+    tr, sr = 128, 0
+    for _ in range(2000):
+        hb = bool(rng.random() < 0.15)
+        t, s, rb = pdgb.adaptive_decide(hb, t, s)
+        tr, sr, rbr = reference_decide(hb, tr, sr)
+        assert (t, s, rb) == (tr, sr, rbr)
+    assert pdgb.adaptive_decide(True, 128, 0) == (64, 0, True)
+    assert pdgb.adaptive_decide(True, 64, 0) == (64, 1, False)
+    t, s = 64, 1
+    for _ in range(9):
+        t, s, _ = pdgb.adaptive_decide(False, t, s)
+    assert (t, s) == (128, 0)
+
+
+def test_no_gpu_fails_loudly(pdgb, scenes):
+    """Without a CUDA device the product path raises; there is no CPU fallback."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    sc = scenes.reference_block(n_side=3)
+    with pytest.raises(pdgb.PdError) as e:
+        scenes.make_simulator(sc)
+    assert e.value.status == 5
+
+
+def test_solver_option_defaults(pdgb):
+    o = pdgb.default_options()
+    assert o.cg_relative_tolerance == 1e-20 and o.cg_max_iterations == 100000
+    assert o.time_step_base == 1.0 / 8388608.0 and o.time_step_min == 100 and o.max_substep == 10
+    assert o.phase_in_steps == 30 and o.pd_k == 5.0 * 2.94315e9 and o.max_bonds_per_particle == 528
+    assert tuple(o.gravity) == (0.0, -9.8, 0.0) and o.restitution == 0.001
