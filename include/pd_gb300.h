@@ -269,6 +269,23 @@ pd_status pd_get_operator_view(pd_handle* h, pd_operator_view* view);
  * scratch; returns after enqueueing. */
 pd_status pd_apply_operator(pd_handle* h, const void* d_x, void* d_y, double* d_dot);
 
+/* No counterpart in the reference.  pd_apply_operator without any device
+ * allocation, for callers that cannot call cudaMalloc: a host application
+ * that owns every device allocation and hands this library only pointers
+ * into its own pool, or code that must not allocate inside a time-critical
+ * loop.  The caller passes the view (e.g. from pd_get_operator_view), the
+ * input and output vectors and the stream (NULL: the legacy default stream).
+ * The reduction scratch is a static device array of this library (one FP64
+ * partial per block for at most 4096 blocks plus a counter, ~33 KB on every
+ * GPU that loads the library, kept until exit); a view asking for more than
+ * 4096 blocks is rejected with PD_ERR_INVALID_ARGUMENT.  The first call on a
+ * device resolves the array's device address (one-time set-up), so make that
+ * first call before any stream capture.  Every call shares the array: calls
+ * whose launches overlap on the GPU race.  Calls no cudaMalloc or cudaFree.
+ * Returns after enqueueing; errors are read with pd_last_error_message(NULL). */
+pd_status pd_apply_operator_noalloc(const pd_operator_view* view, const void* d_x, void* d_y, double* d_dot,
+                                    void* stream);
+
 /* ---- profiling (Monitor, src/core/monitor.cu:53-95) ----------------------- */
 pd_status pd_set_profiling(pd_handle* h, int enabled);
 pd_status pd_get_kernel_times(pd_handle* h, pd_kernel_times* t);

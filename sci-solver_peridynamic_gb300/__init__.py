@@ -166,6 +166,7 @@ def library(build_if_missing: bool = True):
         "pd_get_stream": (st, [vp, P(vp)]),
         "pd_get_operator_view": (st, [vp, P(OperatorView)]),
         "pd_apply_operator": (st, [vp, vp, vp, vp]),
+        "pd_apply_operator_noalloc": (st, [P(OperatorView), vp, vp, vp, vp]),
         "pd_synchronize": (st, [vp]),
         "pd_status_string": (C.c_char_p, [C.c_int]),
         "pd_last_error_message": (C.c_char_p, [vp]),
@@ -205,6 +206,14 @@ def adaptive_decide(has_broken, ticks, substep, ticks_base=128, ticks_min=100, m
     _check(library().pd_adaptive_decide(int(has_broken), ticks_base, ticks_min, max_substep,
                                         C.byref(t), C.byref(s), C.byref(rb)))
     return t.value, s.value, bool(rb.value)
+
+
+def apply_operator_noalloc(view: OperatorView, d_x: int, d_y: int, d_dot: int | None = None, stream: int = 0):
+    """pd_apply_operator_noalloc: y = A x for callers that cannot allocate
+    device memory; every pointer is a raw device address they own."""
+    _check(library().pd_apply_operator_noalloc(C.byref(view), C.c_void_p(d_x), C.c_void_p(d_y),
+                                               C.c_void_p(d_dot) if d_dot else None,
+                                               C.c_void_p(stream) if stream else None))
 
 
 class SystemParameter:

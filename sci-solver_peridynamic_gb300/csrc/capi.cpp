@@ -14,6 +14,11 @@ namespace {
 thread_local std::string g_create_error;
 }
 
+namespace pdgb {
+// Error text of calls that have no handle (read with pd_last_error_message(NULL)).
+void set_handleless_error(const std::string& msg) { g_create_error = msg; }
+}  // namespace pdgb
+
 extern "C" {
 
 int pd_abi_version(void) { return PD_GB300_ABI_VERSION; }
