@@ -281,7 +281,8 @@ def run_gb300(args):
             "particles": n,
             "bonds_alive": int(bonds),
             "cg_iterations_per_step": round(iters / args.steps, 2),
-            "lanes_per_particle": sim.params()[2].lanes_per_particle or 8,
+            "spmv_variant": "%d lanes x %d unroll (autotuned)" % (sim.params()[2].lanes_per_particle,
+                                                                   sim.params()[2].spmv_unroll),
             "parallelism": "replicas x%d" % world,
             "l2": "inputs larger than L2 (bond list %.0f MB + particle state > 129 MB L2)" % (4 * bonds / 1e6),
         },

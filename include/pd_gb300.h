@@ -126,8 +126,9 @@ typedef struct pd_solver_options {
     double sphere_radius;
     double sphere_stiffness;
     /* performance knobs: 0 = automatic */
-    int lanes_per_particle;        /* 4, 8, 16 or 32 lanes cooperate on one bond row */
+    int lanes_per_particle;        /* 4, 8, 16 or 32 lanes cooperate on one bond row of the SpMV */
     int cg_check_interval;         /* CG iterations launched between convergence read-backs */
+    int spmv_unroll;               /* 1, 2 or 4 bonds loaded per lane before computing */
 } pd_solver_options;
 
 /* Export selectors for pd_get. */

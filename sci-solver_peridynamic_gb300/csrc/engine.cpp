@@ -262,14 +262,12 @@ pd_status Engine::make_ready()
     CK(cudaStreamSynchronize(stream_), "make_ready sync");
     for (int i = 0; i < n; ++i) inv_[perm_[i]] = i;
     // launch geometry
-    int lanes = opt_.lanes_per_particle;
-    if (lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32) lanes = 8;
-    L_.lanes = lanes;
-    const int bpsm = row_kernel_blocks_per_sm(fp64_, lanes);
-    const long long need_rows = ((long long)n + (kBlock / lanes) - 1) / (kBlock / lanes);
-    L_.grid_bonds = (int)std::max<long long>(1, std::min<long long>({need_rows, (long long)sm_count_ * bpsm, (long long)kMaxPartials}));
     const long long need_vec = ((long long)n + kBlock - 1) / kBlock;
     L_.grid_vec = (int)std::max<long long>(1, std::min<long long>({need_vec, (long long)sm_count_ * 8, (long long)kMaxPartials}));
+    L_.force_lanes = 8;
+    L_.grid_force = grid_for_rows(L_.force_lanes, force_kernel_blocks_per_sm(fp64_, L_.force_lanes));
+    s = tune_spmv();
+    if (s != PD_OK) return s;
     // step state
     step_ = 0;
     substep_ = 0;
@@ -282,6 +280,70 @@ pd_status Engine::make_ready()
     predicted_iters_ = 0;
     last_params_ = step_params();
     ready_ = true;
+    return PD_OK;
+}
+
+int Engine::grid_for_rows(int lanes, int blocks_per_sm) const
+{
+    const long long rows_per_block = kBlock / lanes;
+    const long long need = ((long long)n_ + rows_per_block - 1) / rows_per_block;
+    return (int)std::max<long long>(1, std::min<long long>({need, (long long)sm_count_ * blocks_per_sm,
+                                                             (long long)kMaxPartials}));
+}
+
+// Project autotuner: times each (lanes, unroll) variant of the SpMV on this
+// problem with CUDA events (one warm-up and three timed launches each) and
+// keeps the fastest.  Fixed choices in the options are respected.
+pd_status Engine::tune_spmv()
+{
+    std::vector<std::pair<int, int>> cand;
+    const int fixed_lanes = opt_.lanes_per_particle;
+    const int fixed_unroll = opt_.spmv_unroll;
+    for (int g : {4, 8, 16}) {
+        if (fixed_lanes && g != fixed_lanes) continue;
+        for (int u : {1, 2, 4}) {
+            if (fp64_ && u != 1) continue;
+            if (fixed_unroll && u != fixed_unroll) continue;
+            cand.push_back({g, u});
+        }
+    }
+    if (cand.empty()) cand.push_back({fixed_lanes ? fixed_lanes : 8, fixed_unroll ? fixed_unroll : 1});
+    auto apply = [&](int g, int u) {
+        L_.lanes = g;
+        L_.unroll = u;
+        L_.grid_bonds = grid_for_rows(g, row_kernel_blocks_per_sm(fp64_, g, u));
+    };
+    if (cand.size() == 1 || n_ < 20000) {
+        // small problems: launch overhead dominates, keep the default
+        const auto c = cand.size() == 1 ? cand[0] : std::make_pair(8, fp64_ ? 1 : 2);
+        apply(c.first, c.second);
+        return PD_OK;
+    }
+    const StepParams P = step_params();
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CK(cudaEventCreate(&e0), "event");
+    CK(cudaEventCreate(&e1), "event");
+    float best = 1e30f;
+    std::pair<int, int> best_c = cand[0];
+    for (const auto& c : cand) {
+        apply(c.first, c.second);
+        launch_spmv(fp64_, false, P, S_, L_, stream_);
+        CK(cudaEventRecord(e0, stream_), "event");
+        for (int k = 0; k < 3; ++k) launch_spmv(fp64_, false, P, S_, L_, stream_);
+        CK(cudaEventRecord(e1, stream_), "event");
+        CK(cudaEventSynchronize(e1), "tune sync");
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1), "event");
+        launches_ += 4;
+        if (ms < best) {
+            best = ms;
+            best_c = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    apply(best_c.first, best_c.second);
+    tuned_ms_ = best / 3.0f;
     return PD_OK;
 }
 
@@ -361,7 +423,7 @@ pd_status Engine::apply_operator(const void* d_x, void* d_y, double* d_dot)
     CK(cudaSetDevice(device_), "cudaSetDevice");
     // counter 4 of the handle's reduction scratch is reserved for this call
     ReduceSlot slot{S_.partials, S_.counters + 4};
-    launch_operator(fp64_, last_params_, S_, L_.lanes, L_.grid_bonds, d_x, d_y, slot, d_dot, stream_);
+    launch_operator_u(fp64_, last_params_, S_, L_.lanes, L_.unroll, L_.grid_bonds, d_x, d_y, slot, d_dot, stream_);
     ++launches_;
     CK(cudaGetLastError(), "apply_operator launch");
     return PD_OK;
@@ -711,7 +773,13 @@ void Engine::params(pd_sim_params* s, pd_run_params* r, pd_solver_options* o) co
 {
     if (s) *s = sim_;
     if (r) *r = run_;
-    if (o) *o = opt_;
+    if (o) {
+        *o = opt_;
+        if (ready_) {   // report the launch shape in use (autotuned when left at 0)
+            o->lanes_per_particle = L_.lanes;
+            o->spmv_unroll = L_.unroll;
+        }
+    }
 }
 
 }  // namespace pdgb

@@ -43,6 +43,8 @@ private:
     pd_status allocate();
     void free_all();
     StepParams step_params() const;
+    int grid_for_rows(int lanes, int blocks_per_sm) const;
+    pd_status tune_spmv();
     pd_status integrate(bool* advanced);
     pd_status solve(const StepParams& P);
     template <typename T>
@@ -84,6 +86,7 @@ private:
     int* h_flags_ = nullptr;      // pinned
     LaunchCfg L_{};
     StepParams last_params_{};   // constants of the latest step (the operator's time step)
+    float tuned_ms_ = 0.f;       // SpMV time of the autotuned variant
     // step state (Simulator members)
     int step_ = 0;
     int substep_ = 0;

@@ -106,8 +106,11 @@ struct DeviceState {
 
 // ---- step kernels (step.cu) --------------------------------------------------
 struct LaunchCfg {
-    int lanes;          // lanes per particle (4, 8, 16, 32)
-    int grid_bonds;     // blocks for row kernels (force, SpMV)
+    int lanes;          // SpMV lanes per particle row (4, 8, 16, 32)
+    int unroll;         // SpMV bonds loaded per lane before computing (1, 2, 4)
+    int grid_bonds;     // SpMV blocks
+    int force_lanes;    // force-pass lanes per particle row
+    int grid_force;     // force-pass blocks
     int grid_vec;       // blocks for per-particle vector kernels
 };
 
@@ -124,8 +127,11 @@ void launch_cg_axpy(bool fp64, const StepParams& P, const DeviceState& S, const 
 void launch_cg_xpby(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
 void launch_update(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
 void launch_refresh(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
-// Max resident blocks per SM of the row kernels for a lane count (for grid sizing).
-int row_kernel_blocks_per_sm(bool fp64, int lanes);
+// Max resident blocks per SM of the SpMV / force kernels (for grid sizing).
+int row_kernel_blocks_per_sm(bool fp64, int lanes, int unroll);
+int force_kernel_blocks_per_sm(bool fp64, int lanes);
+void launch_operator_u(bool fp64, const StepParams& P, const DeviceState& S, int lanes, int unroll, int grid,
+                       const void* in, void* out, ReduceSlot slot, double* dot_out, cudaStream_t st);
 
 // ---- bond construction kernels (bonds.cu) --------------------------------------
 struct BondBuildOut {

@@ -231,7 +231,8 @@ __global__ void __launch_bounds__(kBlock) k_force(StepParams P, DeviceState S)
 // DOT: reduce <in, A in>; with `cg` set (CG iteration) the result becomes
 // alpha = rz / <p, A p> and the launch is skipped once the CG has finished;
 // with `dot_out` set the result is also stored there.
-template <int G, bool FP64, bool DOT>
+// U: bonds each lane loads before it computes (memory-level parallelism).
+template <int G, bool FP64, bool DOT, int U>
 __global__ void __launch_bounds__(kBlock) k_spmv(StepParams P, DeviceState S, const void* __restrict__ in_,
                                                   void* __restrict__ out_, ReduceSlot slot, CgScalars* cg,
                                                   double* dot_out)
@@ -251,9 +252,13 @@ __global__ void __launch_bounds__(kBlock) k_spmv(StepParams P, DeviceState S, co
     const Real t2 = (Real)P.t2;
     const Real m = (Real)P.mass;
     // every group runs the same number of loop trips so that whole blocks reach the reduction
+    // Each block walks one contiguous run of rows: consecutive trips touch
+    // overlapping neighbourhoods (slots are in Morton cell order), so the
+    // gathered data stays in L1 between trips.
     const int trips = (P.n + stride - 1) / stride;
+    const int run_begin = blockIdx.x * trips * gpb;
     for (int t = 0; t < trips; ++t) {
-        const int p = t * stride + blockIdx.x * gpb + threadIdx.x / G;
+        const int p = run_begin + t * gpb + threadIdx.x / G;
         if (p >= P.n) continue;
         const uint8_t ab = S.act[p];
         if (is_dirichlet(ab & kActMask)) {
@@ -274,23 +279,41 @@ __global__ void __launch_bounds__(kBlock) k_spmv(StepParams P, DeviceState S, co
                 az += J[4] * wq.x + J[5] * wq.y + J[2] * wq.z;
             }
         } else {
-            const float4 Xp = S.X32[p];
-            const float4 Up = S.u32[p];
-            for (int j = lane; j < cn; j += G) {
-                const int q = S.col[rs + j];
-                const float4 Xq = S.X32[q];
-                const float4 Uq = S.u32[q];
-                const V4 wq = in[q];
-                const float x0 = Xq.x - Xp.x, y0 = Xq.y - Xp.y, z0 = Xq.z - Xp.z;
-                const float xs = x0 + (Uq.x - Up.x), ys = y0 + (Uq.y - Up.y), zs = z0 + (Uq.z - Up.z);
-                const float inv_d0 = rsqrtf(fmaf(x0, x0, fmaf(y0, y0, z0 * z0)));
-                const float inv_d = rsqrtf(fmaf(xs, xs, fmaf(ys, ys, zs * zs)));
-                const float wx = (float)w.x - (float)wq.x, wy = (float)w.y - (float)wq.y, wz = (float)w.z - (float)wq.z;
-                const float a1 = inv_d0 - inv_d;
-                const float g = fmaf(xs, wx, fmaf(ys, wy, zs * wz)) * (inv_d * inv_d * inv_d);
-                ax = fmaf(a1, wx, fmaf(g, xs, (float)ax));
-                ay = fmaf(a1, wy, fmaf(g, ys, (float)ay));
-                az = fmaf(a1, wz, fmaf(g, zs, (float)az));
+            const float4 Xp = __ldg(S.X32 + p);
+            const float4 Up = __ldg(S.u32 + p);
+            const float4* __restrict__ X32 = S.X32;
+            const float4* __restrict__ u32 = S.u32;
+            const float4* __restrict__ in32 = (const float4*)in;
+            for (int j0 = lane; j0 < cn; j0 += G * U) {
+                // issue every load of U bonds before any arithmetic
+                int qq[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int j = j0 + u * G;
+                    qq[u] = j < cn ? __ldcs(S.col + rs + j) : -1;
+                }
+                float4 Xq[U], Uq[U], Wq[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int q = qq[u] < 0 ? p : qq[u];
+                    Xq[u] = __ldg(X32 + q);
+                    Uq[u] = __ldg(u32 + q);
+                    Wq[u] = __ldg(in32 + q);
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    if (qq[u] < 0) continue;
+                    const float x0 = Xq[u].x - Xp.x, y0 = Xq[u].y - Xp.y, z0 = Xq[u].z - Xp.z;
+                    const float xs = x0 + (Uq[u].x - Up.x), ys = y0 + (Uq[u].y - Up.y), zs = z0 + (Uq[u].z - Up.z);
+                    const float inv_d0 = rsqrtf(fmaf(x0, x0, fmaf(y0, y0, z0 * z0)));
+                    const float inv_d = rsqrtf(fmaf(xs, xs, fmaf(ys, ys, zs * zs)));
+                    const float wx = (float)w.x - Wq[u].x, wy = (float)w.y - Wq[u].y, wz = (float)w.z - Wq[u].z;
+                    const float a1 = inv_d0 - inv_d;
+                    const float g = fmaf(xs, wx, fmaf(ys, wy, zs * wz)) * (inv_d * inv_d * inv_d);
+                    ax = fmaf(a1, wx, fmaf(g, xs, (float)ax));
+                    ay = fmaf(a1, wy, fmaf(g, ys, (float)ay));
+                    az = fmaf(a1, wz, fmaf(g, zs, (float)az));
+                }
             }
         }
         ax = group_sum<G>(ax, gmask);
@@ -591,45 +614,62 @@ static void force_g(bool fp64, const StepParams& P, const DeviceState& S, int gr
 
 void launch_force(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st)
 {
-    switch (L.lanes) {
-    case 4: force_g<4>(fp64, P, S, L.grid_bonds, st); break;
-    case 16: force_g<16>(fp64, P, S, L.grid_bonds, st); break;
-    case 32: force_g<32>(fp64, P, S, L.grid_bonds, st); break;
-    default: force_g<8>(fp64, P, S, L.grid_bonds, st); break;
+    switch (L.force_lanes) {
+    case 4: force_g<4>(fp64, P, S, L.grid_force, st); break;
+    case 16: force_g<16>(fp64, P, S, L.grid_force, st); break;
+    case 32: force_g<32>(fp64, P, S, L.grid_force, st); break;
+    default: force_g<8>(fp64, P, S, L.grid_force, st); break;
     }
 }
 
-template <int G, bool DOT>
+template <int G, bool DOT, int U>
 static void spmv_g(bool fp64, const StepParams& P, const DeviceState& S, int grid, const void* in, void* out,
                    ReduceSlot slot, CgScalars* cg, double* dot_out, cudaStream_t st)
 {
-    if (fp64) k_spmv<G, true, DOT><<<grid, kBlock, 0, st>>>(P, S, in, out, slot, cg, dot_out);
-    else k_spmv<G, false, DOT><<<grid, kBlock, 0, st>>>(P, S, in, out, slot, cg, dot_out);
+    if (fp64) k_spmv<G, true, DOT, 1><<<grid, kBlock, 0, st>>>(P, S, in, out, slot, cg, dot_out);
+    else k_spmv<G, false, DOT, U><<<grid, kBlock, 0, st>>>(P, S, in, out, slot, cg, dot_out);
+}
+
+template <bool DOT, int U>
+static void spmv_lanes(bool fp64, const StepParams& P, const DeviceState& S, int lanes, int grid, const void* in,
+                       void* out, ReduceSlot slot, CgScalars* cg, double* dot_out, cudaStream_t st)
+{
+    switch (lanes) {
+    case 4: spmv_g<4, DOT, U>(fp64, P, S, grid, in, out, slot, cg, dot_out, st); break;
+    case 16: spmv_g<16, DOT, U>(fp64, P, S, grid, in, out, slot, cg, dot_out, st); break;
+    case 32: spmv_g<32, DOT, U>(fp64, P, S, grid, in, out, slot, cg, dot_out, st); break;
+    default: spmv_g<8, DOT, U>(fp64, P, S, grid, in, out, slot, cg, dot_out, st); break;
+    }
 }
 
 template <bool DOT>
-static void spmv_d(bool fp64, const StepParams& P, const DeviceState& S, int lanes, int grid, const void* in,
-                   void* out, ReduceSlot slot, CgScalars* cg, double* dot_out, cudaStream_t st)
+static void spmv_d(bool fp64, const StepParams& P, const DeviceState& S, int lanes, int unroll, int grid,
+                   const void* in, void* out, ReduceSlot slot, CgScalars* cg, double* dot_out, cudaStream_t st)
 {
-    switch (lanes) {
-    case 4: spmv_g<4, DOT>(fp64, P, S, grid, in, out, slot, cg, dot_out, st); break;
-    case 16: spmv_g<16, DOT>(fp64, P, S, grid, in, out, slot, cg, dot_out, st); break;
-    case 32: spmv_g<32, DOT>(fp64, P, S, grid, in, out, slot, cg, dot_out, st); break;
-    default: spmv_g<8, DOT>(fp64, P, S, grid, in, out, slot, cg, dot_out, st); break;
+    switch (unroll) {
+    case 2: spmv_lanes<DOT, 2>(fp64, P, S, lanes, grid, in, out, slot, cg, dot_out, st); break;
+    case 4: spmv_lanes<DOT, 4>(fp64, P, S, lanes, grid, in, out, slot, cg, dot_out, st); break;
+    default: spmv_lanes<DOT, 1>(fp64, P, S, lanes, grid, in, out, slot, cg, dot_out, st); break;
     }
 }
 
 void launch_spmv(bool fp64, bool dot, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st)
 {
-    if (dot) spmv_d<true>(fp64, P, S, L.lanes, L.grid_bonds, S.p, S.y, slot_of(S, 1), S.sc, nullptr, st);
-    else spmv_d<false>(fp64, P, S, L.lanes, L.grid_bonds, S.sol, S.y, slot_of(S, 1), nullptr, nullptr, st);
+    if (dot) spmv_d<true>(fp64, P, S, L.lanes, L.unroll, L.grid_bonds, S.p, S.y, slot_of(S, 1), S.sc, nullptr, st);
+    else spmv_d<false>(fp64, P, S, L.lanes, L.unroll, L.grid_bonds, S.sol, S.y, slot_of(S, 1), nullptr, nullptr, st);
 }
 
 void launch_operator(bool fp64, const StepParams& P, const DeviceState& S, int lanes, int grid, const void* in,
                      void* out, ReduceSlot slot, double* dot_out, cudaStream_t st)
 {
-    if (dot_out) spmv_d<true>(fp64, P, S, lanes, grid, in, out, slot, nullptr, dot_out, st);
-    else spmv_d<false>(fp64, P, S, lanes, grid, in, out, slot, nullptr, nullptr, st);
+    launch_operator_u(fp64, P, S, lanes, 1, grid, in, out, slot, dot_out, st);
+}
+
+void launch_operator_u(bool fp64, const StepParams& P, const DeviceState& S, int lanes, int unroll, int grid,
+                       const void* in, void* out, ReduceSlot slot, double* dot_out, cudaStream_t st)
+{
+    if (dot_out) spmv_d<true>(fp64, P, S, lanes, unroll, grid, in, out, slot, nullptr, dot_out, st);
+    else spmv_d<false>(fp64, P, S, lanes, unroll, grid, in, out, slot, nullptr, nullptr, st);
 }
 
 void launch_cg_init(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st)
@@ -668,29 +708,56 @@ void launch_refresh(bool fp64, const StepParams& P, const DeviceState& S, const 
     k_refresh<<<L.grid_vec, kBlock, 0, st>>>(P, S);
 }
 
-template <int G>
-static int blocks_g(bool fp64)
+template <int G, int U>
+static int blocks_gu(bool fp64)
 {
-    int a = 0, b = 0;
+    int a = 0, b = 0, c = 0;
     if (fp64) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_spmv<G, true, true>, kBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_spmv<G, true, true, 1>, kBlock, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_force<G, true>, kBlock, 0);
+        c = a;
     } else {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_spmv<G, false, true>, kBlock, 0);
+        cudaFuncSetAttribute(k_spmv<G, false, true, U>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+        cudaFuncSetAttribute(k_spmv<G, false, false, U>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_spmv<G, false, true, U>, kBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_spmv<G, false, false, U>, kBlock, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_force<G, false>, kBlock, 0);
     }
-    const int m = a < b ? a : b;
+    int m = a < c ? a : c;
+    (void)b;
     return m > 0 ? m : 1;
 }
 
-int row_kernel_blocks_per_sm(bool fp64, int lanes)
+template <int G>
+static int blocks_g(bool fp64, int unroll)
+{
+    switch (unroll) {
+    case 2: return blocks_gu<G, 2>(fp64);
+    case 4: return blocks_gu<G, 4>(fp64);
+    default: return blocks_gu<G, 1>(fp64);
+    }
+}
+
+int row_kernel_blocks_per_sm(bool fp64, int lanes, int unroll)
 {
     switch (lanes) {
-    case 4: return blocks_g<4>(fp64);
-    case 16: return blocks_g<16>(fp64);
-    case 32: return blocks_g<32>(fp64);
-    default: return blocks_g<8>(fp64);
+    case 4: return blocks_g<4>(fp64, unroll);
+    case 16: return blocks_g<16>(fp64, unroll);
+    case 32: return blocks_g<32>(fp64, unroll);
+    default: return blocks_g<8>(fp64, unroll);
     }
+}
+
+int force_kernel_blocks_per_sm(bool fp64, int lanes)
+{
+    int b = 0;
+    switch (lanes) {
+    case 4: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fp64 ? (const void*)k_force<4, true> : (const void*)k_force<4, false>, kBlock, 0); break;
+    case 16: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fp64 ? (const void*)k_force<16, true> : (const void*)k_force<16, false>, kBlock, 0); break;
+    case 32: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fp64 ? (const void*)k_force<32, true> : (const void*)k_force<32, false>, kBlock, 0); break;
+    default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fp64 ? (const void*)k_force<8, true> : (const void*)k_force<8, false>, kBlock, 0); break;
+    }
+    return b > 0 ? b : 1;
 }
 
 }  // namespace pdgb
