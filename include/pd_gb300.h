@@ -129,6 +129,11 @@ typedef struct pd_solver_options {
     int lanes_per_particle;        /* 4, 8, 16 or 32 lanes cooperate on one bond row of the SpMV */
     int cg_check_interval;         /* CG iterations launched between convergence read-backs */
     int spmv_unroll;               /* 1, 2 or 4 bonds loaded per lane before computing */
+    /* CG initial guess (no reference counterpart for 1): 0 = the previous
+     * solution, as the reference (simulator.cu:745-770); 1 = previous solution
+     * plus the learned correction of pd_ws_set_params' network (mixed
+     * precision only; the CG still runs to the same tolerance) */
+    int warm_start;
 } pd_solver_options;
 
 /* Export selectors for pd_get. */
@@ -164,6 +169,8 @@ typedef struct pd_step_stats {
     int max_bonds_per_particle;    /* pd_max_num_bonds */
     double clock_scale;
     double sim_time;               /* simulated seconds */
+    long long ws_guesses_kept;     /* steps whose learned guess beat the previous solution */
+    double last_ws_residual_ratio; /* ||r(learned guess)|| / ||r(previous solution)|| of the last step */
 } pd_step_stats;
 
 /* Device time per kernel class, accumulated with CUDA events on the handle's
@@ -286,6 +293,33 @@ pd_status pd_apply_operator(pd_handle* h, const void* d_x, void* d_y, double* d_
  * Returns after enqueueing; errors are read with pd_last_error_message(NULL). */
 pd_status pd_apply_operator_noalloc(const pd_operator_view* view, const void* d_x, void* d_y, double* d_dot,
                                     void* stream);
+
+/* ---- learned CG warm start (no reference counterpart) ----------------------
+ * A per-particle MLP (64 features -> 128 -> 128 -> 3, GELU; BF16 tensor-core
+ * GEMMs with FP32 accumulation) predicts the change of the CG solution over
+ * the previous solution.  Parameters are one FP32 blob of
+ * pd_mlp_param_count() values: W1[64x128], b1[128], W2[128x128], b2[128],
+ * W3[128x3], b3[3] (row-major, input x output). */
+size_t pd_mlp_param_count(void);
+/* Glorot-uniform initial parameters (output layer scaled by 0.1). */
+pd_status pd_mlp_init(unsigned seed, float* params);
+/* Y[rows x 3] = MLP(X[rows x 64]) on `device` (inputs rounded to BF16). */
+pd_status pd_mlp_predict(int device, const float* X, long long rows, const float* params, float* Y);
+/* Mean squared error over rows (sum over the 3 outputs) and its gradient. */
+pd_status pd_mlp_loss_grad(int device, const float* X, const float* T, int rows, const float* params, float* grad,
+                           double* loss);
+/* Adam training on the GPU (batches drawn without replacement per epoch);
+ * params are read and overwritten; *final_loss = loss over all rows. */
+pd_status pd_mlp_train(int device, const float* X, const float* T, long long rows, int iterations, int batch,
+                       float lr, unsigned seed, float* params, double* final_loss);
+/* Network used by warm_start = 1 on this handle. */
+pd_status pd_ws_set_params(pd_handle* h, const float* params, size_t count);
+pd_status pd_ws_get_params(pd_handle* h, float* params, size_t count);
+/* Record up to samples_per_step (features, target) rows per step into a ring
+ * buffer of `capacity` rows (0 disables); targets are (x_new - x_prev) / sigma. */
+pd_status pd_ws_collect(pd_handle* h, int samples_per_step, long long capacity);
+/* Copies the recorded rows (at most max_rows) to X[rows x 64], T[rows x 3]. */
+pd_status pd_ws_dataset(pd_handle* h, float* X, float* T, long long max_rows, long long* rows);
 
 /* ---- profiling (Monitor, src/core/monitor.cu:53-95) ----------------------- */
 pd_status pd_set_profiling(pd_handle* h, int enabled);

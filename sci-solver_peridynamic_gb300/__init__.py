@@ -92,6 +92,7 @@ class SolverOptions(C.Structure):
         ("sphere_center", C.c_double * 3), ("sphere_velocity", C.c_double * 3),
         ("sphere_radius", C.c_double), ("sphere_stiffness", C.c_double),
         ("lanes_per_particle", C.c_int), ("cg_check_interval", C.c_int), ("spmv_unroll", C.c_int),
+        ("warm_start", C.c_int),
     ]
 
 
@@ -102,6 +103,7 @@ class StepStats(C.Structure):
         ("total_cg_iterations", C.c_longlong), ("time_step_ticks", C.c_int), ("substep", C.c_int),
         ("retries_last_step", C.c_int), ("bonds_initial", C.c_longlong), ("bonds_alive", C.c_longlong),
         ("max_bonds_per_particle", C.c_int), ("clock_scale", C.c_double), ("sim_time", C.c_double),
+        ("ws_guesses_kept", C.c_longlong), ("last_ws_residual_ratio", C.c_double),
     ]
 
     def as_dict(self):
@@ -167,6 +169,17 @@ def library(build_if_missing: bool = True):
         "pd_get_operator_view": (st, [vp, P(OperatorView)]),
         "pd_apply_operator": (st, [vp, vp, vp, vp]),
         "pd_apply_operator_noalloc": (st, [P(OperatorView), vp, vp, vp, vp]),
+        "pd_mlp_param_count": (C.c_size_t, []),
+        "pd_mlp_init": (st, [C.c_uint, P(C.c_float)]),
+        "pd_mlp_predict": (st, [C.c_int, P(C.c_float), C.c_longlong, P(C.c_float), P(C.c_float)]),
+        "pd_mlp_loss_grad": (st, [C.c_int, P(C.c_float), P(C.c_float), C.c_int, P(C.c_float), P(C.c_float),
+                                  P(C.c_double)]),
+        "pd_mlp_train": (st, [C.c_int, P(C.c_float), P(C.c_float), C.c_longlong, C.c_int, C.c_int, C.c_float, C.c_uint,
+                              P(C.c_float), P(C.c_double)]),
+        "pd_ws_set_params": (st, [vp, P(C.c_float), C.c_size_t]),
+        "pd_ws_get_params": (st, [vp, P(C.c_float), C.c_size_t]),
+        "pd_ws_collect": (st, [vp, C.c_int, C.c_longlong]),
+        "pd_ws_dataset": (st, [vp, P(C.c_float), P(C.c_float), C.c_longlong, P(C.c_longlong)]),
         "pd_synchronize": (st, [vp]),
         "pd_status_string": (C.c_char_p, [C.c_int]),
         "pd_last_error_message": (C.c_char_p, [vp]),
@@ -214,6 +227,49 @@ def apply_operator_noalloc(view: OperatorView, d_x: int, d_y: int, d_dot: int | 
     _check(library().pd_apply_operator_noalloc(C.byref(view), C.c_void_p(d_x), C.c_void_p(d_y),
                                                C.c_void_p(d_dot) if d_dot else None,
                                                C.c_void_p(stream) if stream else None))
+
+
+def _fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def mlp_param_count() -> int:
+    return int(library().pd_mlp_param_count())
+
+
+def mlp_init(seed: int = 1) -> np.ndarray:
+    p = np.zeros(mlp_param_count(), np.float32)
+    _check(library().pd_mlp_init(seed, _fp(p)))
+    return p
+
+
+def mlp_predict(X, params, device: int = 0) -> np.ndarray:
+    X = np.ascontiguousarray(X, np.float32)
+    params = np.ascontiguousarray(params, np.float32)
+    Y = np.zeros((X.shape[0], 3), np.float32)
+    _check(library().pd_mlp_predict(device, _fp(X), X.shape[0], _fp(params), _fp(Y)))
+    return Y
+
+
+def mlp_loss_grad(X, T, params, device: int = 0):
+    X = np.ascontiguousarray(X, np.float32)
+    T = np.ascontiguousarray(T, np.float32)
+    params = np.ascontiguousarray(params, np.float32)
+    g = np.zeros_like(params)
+    loss = C.c_double()
+    _check(library().pd_mlp_loss_grad(device, _fp(X), _fp(T), X.shape[0], _fp(params), _fp(g), C.byref(loss)))
+    return loss.value, g
+
+
+def mlp_train(X, T, params, iterations=2000, batch=1024, lr=1e-3, seed=1, device: int = 0):
+    """Adam on the GPU; returns (trained params, loss over all rows)."""
+    X = np.ascontiguousarray(X, np.float32)
+    T = np.ascontiguousarray(T, np.float32)
+    p = np.array(params, np.float32, copy=True)
+    loss = C.c_double()
+    _check(library().pd_mlp_train(device, _fp(X), _fp(T), X.shape[0], iterations, batch, lr, seed, _fp(p),
+                                  C.byref(loss)))
+    return p, loss.value
 
 
 class SystemParameter:
@@ -382,6 +438,27 @@ class Simulator:
         """y = A x on device vectors given as raw device pointers (slot order)."""
         _check(self.lib.pd_apply_operator(self.h, C.c_void_p(d_x), C.c_void_p(d_y),
                                           C.c_void_p(d_dot) if d_dot else None), self.h)
+
+    # learned warm start
+    def ws_set_params(self, params):
+        p = np.ascontiguousarray(params, np.float32)
+        _check(self.lib.pd_ws_set_params(self.h, _fp(p), p.size), self.h)
+
+    def ws_get_params(self) -> np.ndarray:
+        p = np.zeros(mlp_param_count(), np.float32)
+        _check(self.lib.pd_ws_get_params(self.h, _fp(p), p.size), self.h)
+        return p
+
+    def ws_collect(self, samples_per_step: int, capacity: int):
+        _check(self.lib.pd_ws_collect(self.h, samples_per_step, capacity), self.h)
+
+    def ws_dataset(self, max_rows: int = 1 << 22):
+        rows = C.c_longlong()
+        _check(self.lib.pd_ws_dataset(self.h, None, None, 0, C.byref(rows)), self.h)
+        X = np.zeros((max_rows if max_rows else 1, 64), np.float32)
+        T = np.zeros((max_rows if max_rows else 1, 3), np.float32)
+        _check(self.lib.pd_ws_dataset(self.h, _fp(X), _fp(T), max_rows, C.byref(rows)), self.h)
+        return X[:rows.value], T[:rows.value]
 
     def stream_handle(self) -> int:
         """cudaStream_t of this simulator, as an integer (for CUDA events)."""

@@ -217,6 +217,30 @@ pd_status pd_apply_operator(pd_handle* h, const void* d_x, void* d_y, double* d_
     return h->eng->apply_operator(d_x, d_y, d_dot);
 }
 
+pd_status pd_ws_set_params(pd_handle* h, const float* params, size_t count)
+{
+    ENG(h);
+    return h->eng->ws_set_params(params, count);
+}
+
+pd_status pd_ws_get_params(pd_handle* h, float* params, size_t count)
+{
+    ENG(h);
+    return h->eng->ws_get_params(params, count);
+}
+
+pd_status pd_ws_collect(pd_handle* h, int samples_per_step, long long capacity)
+{
+    ENG(h);
+    return h->eng->ws_collect(samples_per_step, capacity);
+}
+
+pd_status pd_ws_dataset(pd_handle* h, float* X, float* T, long long max_rows, long long* rows)
+{
+    ENG(h);
+    return h->eng->ws_dataset(X, T, max_rows, rows);
+}
+
 pd_status pd_get_stream(pd_handle* h, void** stream)
 {
     ENG(h);

@@ -11,6 +11,8 @@
 //  * errors are returned as pd_status instead of exit().
 #include "engine.h"
 
+#include <cuda_bf16.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -129,6 +131,7 @@ pd_status Engine::set_stretch(const double* s0, int n)
 
 void Engine::free_all()
 {
+    ws_free();
     void* ptrs[] = {S_.act, S_.x64, S_.v64, S_.X64, S_.x64_bk, S_.v64_bk, S_.st, S_.ost, S_.nst, S_.row_ptr,
                     S_.cnt, S_.cnt_bk, S_.col, S_.X32, S_.u32, S_.jac, S_.jdiag, S_.force, S_.rhs, S_.sol,
                     S_.r, S_.p, S_.y, S_.sc, S_.partials, S_.counters, S_.flags, d_perm_};
@@ -164,7 +167,7 @@ pd_status Engine::allocate()
     }
     if (fp64_) CK(dalloc(&S_.jdiag, 6 * n), "alloc jdiag");
     CK(dalloc(&S_.sc, 1), "alloc scalars");
-    CK(dalloc(&S_.partials, (size_t)kMaxPartials), "alloc partials");
+    CK(dalloc(&S_.partials, 4 * (size_t)kMaxPartials), "alloc partials");
     CK(dalloc(&S_.counters, 8), "alloc counters");
     CK(dalloc(&S_.flags, 4), "alloc flags");
     CK(cudaMemsetAsync(S_.counters, 0, sizeof(unsigned) * 8, stream_), "memset counters");
@@ -380,6 +383,195 @@ StepParams Engine::step_params() const
     return P;
 }
 
+// ---- learned warm start --------------------------------------------------------------
+bool Engine::ws_features_needed() const { return !fp64_ && ready_ && (opt_.warm_start == 1 || ws_samples_ > 0); }
+
+void Engine::ws_free()
+{
+    void* p[] = {W_.diag, W_.dj, W_.features, W_.hist2, W_.hist3, W_.xsave, W_.ds_x, W_.ds_t, W_.sc, W_.free_list,
+                 ws_rsave_};
+    for (void* q : p)
+        if (q) cudaFree(q);
+    W_ = WsState{};
+    ws_rsave_ = nullptr;
+    mlp_work_free(&mlp_work_);
+    mlp_free(&mlp_);
+    ws_ready_ = false;
+}
+
+pd_status Engine::ws_prepare()
+{
+    if (ws_ready_) return PD_OK;
+    const size_t N = (size_t)std::max(n_, 1);
+    CK(dalloc(&W_.diag, N), "alloc ws");
+    CK(dalloc(&W_.dj, N), "alloc ws");
+    CK(dalloc(&W_.features, N * kMlpIn), "alloc ws");
+    CK(dalloc(&W_.hist2, N), "alloc ws");
+    CK(dalloc(&W_.hist3, N), "alloc ws");
+    CK(dalloc(&W_.xsave, N), "alloc ws");
+    CK(dalloc(&ws_rsave_, N), "alloc ws");
+    CK(dalloc(&W_.sc, 1), "alloc ws");
+    CK(cudaMemsetAsync(W_.hist2, 0, sizeof(float4) * N, stream_), "memset ws");
+    CK(cudaMemsetAsync(W_.hist3, 0, sizeof(float4) * N, stream_), "memset ws");
+    CK(cudaMemsetAsync(W_.xsave, 0, sizeof(float4) * N, stream_), "memset ws");
+    // free slots (Dirichlet rows carry no prediction and no training sample)
+    std::vector<int> free_slots;
+    for (int i = 0; i < n_; ++i) {
+        const int a = h_act_[perm_[i]];
+        if (a != PD_INVISIBLE && a != PD_CLAMPED && a != PD_PRESCRIBED) free_slots.push_back(i);
+    }
+    W_.n_free_host = (int)free_slots.size();
+    CK(dalloc(&W_.free_list, std::max<size_t>(free_slots.size(), 1)), "alloc ws");
+    if (!free_slots.empty())
+        CK(cudaMemcpyAsync(W_.free_list, free_slots.data(), sizeof(int) * free_slots.size(), cudaMemcpyHostToDevice,
+                           stream_), "upload free list");
+    WsScalars sc{};
+    sc.n_free = W_.n_free_host;
+    CK(cudaMemcpyAsync(W_.sc, &sc, sizeof(sc), cudaMemcpyHostToDevice, stream_), "upload ws scalars");
+    W_.max_bonds = std::max(sim_.pd_max_num_bonds, 1);
+    CK(mlp_alloc(&mlp_, false), "alloc mlp");
+    CK(mlp_work_alloc(&mlp_work_, n_, false), "alloc mlp work");
+    if (ws_params_.size() != mlp_param_count()) {
+        ws_params_.assign(mlp_param_count(), 0.f);
+        mlp_init_params(ws_params_.data(), 1u);
+    }
+    CK(cudaMemcpyAsync(mlp_.params, ws_params_.data(), sizeof(float) * ws_params_.size(), cudaMemcpyHostToDevice,
+                       stream_), "upload mlp params");
+    mlp_refresh_bf16(mlp_, stream_);
+    if (ws_cap_ > 0) {
+        CK(dalloc(&W_.ds_x, (size_t)ws_cap_ * kMlpIn), "alloc dataset");
+        CK(dalloc(&W_.ds_t, (size_t)ws_cap_ * 3), "alloc dataset");
+    }
+    ws_pos_ = ws_count_ = 0;
+    CK(cudaStreamSynchronize(stream_), "ws prepare");
+    ws_ready_ = true;
+    return PD_OK;
+}
+
+// After the CG set-up (x1 = previous solution with Dirichlet values, r = b - A x1):
+// features, and with warm_start = 1 the learned guess x1 + sigma MLP(features),
+// its residual, and the guard that keeps the better of the two guesses.
+pd_status Engine::ws_before_cg(const StepParams& P)
+{
+    pd_status s = ws_prepare();
+    if (s != PD_OK) return s;
+    const size_t N = (size_t)n_;
+    if (N == 0) return PD_OK;
+    CK(cudaMemcpyAsync(W_.xsave, S_.sol, sizeof(float4) * N, cudaMemcpyDeviceToDevice, stream_), "save x1");
+    ReduceSlot s0{S_.partials + kMaxPartials, S_.counters + 5};
+    ReduceSlot s1{S_.partials + 2 * kMaxPartials, S_.counters + 6};
+    ReduceSlot s2{S_.partials + 3 * kMaxPartials, S_.counters + 7};
+    launch_ws_jacobi(P, S_, W_, 8, L_.grid_force, s0, s1, s2, stream_);
+    launch_ws_features(P, S_, W_, L_.grid_force, stream_);
+    launches_ += 2;
+    if (opt_.warm_start == 1) {
+        CK(cudaMemcpyAsync(ws_rsave_, S_.r, sizeof(float4) * N, cudaMemcpyDeviceToDevice, stream_), "save r");
+        launch_ws_save_plain(S_, stream_);
+        mlp_forward(mlp_, W_.features, n_, mlp_work_, mlp_work_.y, stream_);
+        launch_ws_apply(P, S_, W_, mlp_work_.y, L_.grid_vec, stream_);
+        launch_spmv(fp64_, false, P, S_, L_, stream_);
+        launch_cg_residual(fp64_, P, S_, L_, stream_);
+        launch_ws_guard(P, S_, W_.xsave, ws_rsave_, L_.grid_vec, stream_);
+        launches_ += 14;
+    }
+    CK(cudaGetLastError(), "warm start launch");
+    return PD_OK;
+}
+
+pd_status Engine::ws_after_cg(const StepParams& P)
+{
+    if (ws_samples_ > 0 && ws_cap_ > 0 && W_.n_free_host > 0) {
+        const int count = std::min(ws_samples_, W_.n_free_host);
+        const int stride = std::max(1, W_.n_free_host / count);
+        ws_rng_ ^= ws_rng_ << 13;
+        ws_rng_ ^= ws_rng_ >> 7;
+        ws_rng_ ^= ws_rng_ << 17;
+        const int offset = (int)(ws_rng_ % (unsigned long long)W_.n_free_host);
+        launch_ws_collect(P, S_, W_, count, stride, offset, ws_pos_, ws_cap_, stream_);
+        ++launches_;
+        ws_pos_ = (ws_pos_ + count) % ws_cap_;
+        ws_count_ = std::min(ws_count_ + count, ws_cap_);
+    }
+    float4* t = W_.hist3;   // x3 <- x2 <- x1
+    W_.hist3 = W_.hist2;
+    W_.hist2 = W_.xsave;
+    W_.xsave = t;
+    if (opt_.warm_start == 1) {
+        last_ws_ratio_ = h_sc_->rz_plain > 0 ? std::sqrt(h_sc_->rz_learned / h_sc_->rz_plain) : 0.0;
+        ws_kept_ = h_sc_->ws_kept;
+    }
+    CK(cudaGetLastError(), "warm start collect");
+    return PD_OK;
+}
+
+pd_status Engine::ws_set_params(const float* params, size_t count)
+{
+    if (!params || count != mlp_param_count()) {
+        err_ = "ws_set_params: expected pd_mlp_param_count() values";
+        return PD_ERR_INVALID_ARGUMENT;
+    }
+    ws_params_.assign(params, params + count);
+    if (ws_ready_) {
+        CK(cudaSetDevice(device_), "cudaSetDevice");
+        CK(cudaMemcpyAsync(mlp_.params, ws_params_.data(), sizeof(float) * count, cudaMemcpyHostToDevice, stream_),
+           "upload mlp params");
+        mlp_refresh_bf16(mlp_, stream_);
+        CK(cudaStreamSynchronize(stream_), "upload mlp params");
+    }
+    return PD_OK;
+}
+
+pd_status Engine::ws_get_params(float* params, size_t count)
+{
+    if (!params || count != mlp_param_count()) return PD_ERR_INVALID_ARGUMENT;
+    if (ws_params_.size() != count) {
+        ws_params_.assign(count, 0.f);
+        mlp_init_params(ws_params_.data(), 1u);
+    }
+    std::copy(ws_params_.begin(), ws_params_.end(), params);
+    return PD_OK;
+}
+
+pd_status Engine::ws_collect(int samples_per_step, long long capacity)
+{
+    if (samples_per_step < 0 || capacity < 0) return PD_ERR_INVALID_ARGUMENT;
+    if (fp64_ && samples_per_step > 0) {
+        err_ = "ws_collect: the learned warm start works in mixed precision";
+        return PD_ERR_INVALID_ARGUMENT;
+    }
+    const bool realloc = capacity != ws_cap_;
+    ws_samples_ = samples_per_step;
+    ws_cap_ = capacity;
+    if (ws_ready_ && realloc) {
+        if (W_.ds_x) cudaFree(W_.ds_x);
+        if (W_.ds_t) cudaFree(W_.ds_t);
+        W_.ds_x = nullptr;
+        W_.ds_t = nullptr;
+        if (ws_cap_ > 0) {
+            CK(dalloc(&W_.ds_x, (size_t)ws_cap_ * kMlpIn), "alloc dataset");
+            CK(dalloc(&W_.ds_t, (size_t)ws_cap_ * 3), "alloc dataset");
+        }
+        ws_pos_ = ws_count_ = 0;
+    }
+    return PD_OK;
+}
+
+pd_status Engine::ws_dataset(float* X, float* T, long long max_rows, long long* rows)
+{
+    if (!rows || max_rows < 0) return PD_ERR_INVALID_ARGUMENT;
+    const long long r = std::min(ws_count_, max_rows);
+    *rows = r;
+    if (r == 0) return PD_OK;
+    if (!X || !T) return PD_ERR_INVALID_ARGUMENT;
+    std::vector<__nv_bfloat16> xb((size_t)r * kMlpIn);
+    CK(cudaMemcpyAsync(xb.data(), W_.ds_x, sizeof(__nv_bfloat16) * xb.size(), cudaMemcpyDeviceToHost, stream_),
+       "download dataset");
+    CK(cudaMemcpyAsync(T, W_.ds_t, sizeof(float) * (size_t)r * 3, cudaMemcpyDeviceToHost, stream_), "download dataset");
+    CK(cudaStreamSynchronize(stream_), "download dataset");
+    for (size_t i = 0; i < xb.size(); ++i) X[i] = __bfloat162float(xb[i]);
+    return PD_OK;
+}
+
 pd_status Engine::synchronize()
 {
     CK(cudaSetDevice(device_), "cudaSetDevice");
@@ -510,6 +702,10 @@ pd_status Engine::solve(const StepParams& P)
     launch_spmv(fp64_, false, P, S_, L_, stream_);
     launch_cg_residual(fp64_, P, S_, L_, stream_);
     launches_ += 3;
+    if (ws_features_needed()) {
+        pd_status s = ws_before_cg(P);
+        if (s != PD_OK) return s;
+    }
     const int check = opt_.cg_check_interval > 0 ? opt_.cg_check_interval : 8;
     int batch = predicted_iters_ > 0 ? predicted_iters_ : check;
     int launched = 0;
@@ -542,6 +738,7 @@ pd_status Engine::solve(const StepParams& P)
     predicted_iters_ = std::max(1, last_iters_);
     flush_marks(last_iters_);
     if (!h_sc_->converged) cg_converged_ = false;
+    if (ws_features_needed()) return ws_after_cg(P);
     return PD_OK;
 }
 
@@ -756,6 +953,8 @@ pd_status Engine::stats(pd_step_stats* s) const
     s->clock_scale = clock_scale_;
     s->sim_time = sim_time_;
     s->bonds_alive = bonds_initial_;
+    s->ws_guesses_kept = ws_kept_;
+    s->last_ws_residual_ratio = last_ws_ratio_;
     if (ready_ && n_ > 0) {
         std::vector<int> c((size_t)n_);
         cudaSetDevice(device_);

@@ -36,6 +36,10 @@ public:
     pd_status synchronize();
     pd_status operator_view(pd_operator_view* v) const;
     pd_status apply_operator(const void* d_x, void* d_y, double* d_dot);
+    pd_status ws_set_params(const float* params, size_t count);
+    pd_status ws_get_params(float* params, size_t count);
+    pd_status ws_collect(int samples_per_step, long long capacity);
+    pd_status ws_dataset(float* X, float* T, long long max_rows, long long* rows);
     const std::string& error() const { return err_; }
 
 private:
@@ -45,6 +49,11 @@ private:
     StepParams step_params() const;
     int grid_for_rows(int lanes, int blocks_per_sm) const;
     pd_status tune_spmv();
+    pd_status ws_prepare();                 // allocates the warm-start state on first use
+    void ws_free();
+    bool ws_features_needed() const;
+    pd_status ws_before_cg(const StepParams& P);
+    pd_status ws_after_cg(const StepParams& P);
     pd_status integrate(bool* advanced);
     pd_status solve(const StepParams& P);
     template <typename T>
@@ -87,6 +96,19 @@ private:
     LaunchCfg L_{};
     StepParams last_params_{};   // constants of the latest step (the operator's time step)
     float tuned_ms_ = 0.f;       // SpMV time of the autotuned variant
+    // learned warm start
+    WsState W_{};
+    MlpDev mlp_{};
+    MlpWork mlp_work_{};
+    float4* ws_rsave_ = nullptr;
+    bool ws_ready_ = false;
+    bool ws_params_loaded_ = false;
+    std::vector<float> ws_params_;
+    int ws_samples_ = 0;
+    long long ws_cap_ = 0, ws_pos_ = 0, ws_count_ = 0;
+    unsigned long long ws_rng_ = 88172645463325252ull;
+    double last_ws_ratio_ = 0.0;
+    long long ws_kept_ = 0;
     // step state (Simulator members)
     int step_ = 0;
     int substep_ = 0;

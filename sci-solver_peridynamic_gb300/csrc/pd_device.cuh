@@ -152,6 +152,7 @@ __device__ __forceinline__ void block_reduce_finish(Acc acc, ReduceSlot slot, Fi
     __shared__ bool is_last;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
+    __syncthreads();   // a previous reduction of this block may still read warp_sums
     const double w = warp_total(acc);
     if (lane == 0) warp_sums[warp] = w;
     __syncthreads();

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 namespace pdgb {
@@ -39,6 +40,10 @@ struct CgScalars {
     int done;
     int converged;
     int max_iter;
+    double rz_plain;       // <r, r> of the previous-solution guess (learned warm start)
+    double rz_learned;     // <r, r> of the learned guess
+    int ws_revert;         // 1: the learned guess was worse and was replaced
+    int ws_kept;           // learned guesses kept so far
 };
 
 // Partial-sum scratch of a reducing launch: one double per block and an
@@ -162,5 +167,78 @@ void scatter_double4(const dbl4* in, const int* perm, dbl4* out, int n, cudaStre
 // FP32 copies relative to an origin
 void make_local32(const dbl4* X, double ox, double oy, double oz, float4* X32, float4* u32, int n,
                   cudaStream_t st);
+
+// ---- learned warm start (mlp.cu, warmstart.cu) -----------------------------------
+constexpr int kMlpIn = 64;
+constexpr int kMlpHidden = 128;
+constexpr int kMlpOut = 3;
+constexpr int kMlpOutPad = 8;
+
+struct MlpDev {
+    float* params;            // FP32 master parameters (mlp_param_count())
+    float* grad;
+    float* m1;                // Adam moments
+    float* m2;
+    __nv_bfloat16* w1b;       // [64 x 128]
+    __nv_bfloat16* w2b;       // [128 x 128]
+    __nv_bfloat16* w3b;       // [128 x 8] (3 used)
+};
+
+struct MlpWork {              // activations for up to `rows` rows
+    float* z1;
+    float* z2;
+    __nv_bfloat16* h1;
+    __nv_bfloat16* h2;
+    __nv_bfloat16* dy;        // [rows x 8]
+    float* dh;
+    __nv_bfloat16* dz;
+    float* y;                 // [rows x 8]
+    long long rows;
+};
+
+struct WsScalars {
+    double sum_x2, sum_r2, sum_v2;   // over free particles
+    int n_free;
+};
+
+struct WsState {
+    float* diag;                  // n
+    float4* dj;                   // n: Jacobi step r / D
+    __nv_bfloat16* features;      // n x 64
+    float4* hist2;                // solution two steps back
+    float4* hist3;                // three steps back
+    float4* xsave;                // previous solution (x1) saved before the CG
+    __nv_bfloat16* ds_x;          // dataset features (capacity x 64)
+    float* ds_t;                  // dataset targets (capacity x 3)
+    WsScalars* sc;
+    int* free_list;               // slots of the free (non-Dirichlet) particles
+    int n_free_host;
+    int max_bonds;
+};
+
+size_t mlp_param_count();
+void mlp_refresh_bf16(MlpDev& m, cudaStream_t st);
+void mlp_forward(const MlpDev& m, const __nv_bfloat16* X, int B, MlpWork& ws, float* Y, cudaStream_t st);
+void mlp_backward(const MlpDev& m, const __nv_bfloat16* X, const float* T, int B, MlpWork& ws, const float* Y,
+                  double* loss, cudaStream_t st);
+void mlp_adam(MlpDev& m, float lr, int t, cudaStream_t st);
+cudaError_t mlp_alloc(MlpDev* m, bool training);
+void mlp_free(MlpDev* m);
+cudaError_t mlp_work_alloc(MlpWork* w, long long rows, bool training);
+void mlp_work_free(MlpWork* w);
+void mlp_init_params(float* host_params, unsigned seed);
+
+void launch_ws_jacobi(const StepParams& P, const DeviceState& S, const WsState& W, int lanes, int grid,
+                      ReduceSlot s0, ReduceSlot s1, ReduceSlot s2, cudaStream_t st);
+void launch_ws_features(const StepParams& P, const DeviceState& S, const WsState& W, int grid, cudaStream_t st);
+void launch_ws_apply(const StepParams& P, const DeviceState& S, const WsState& W, const float* Y, int grid,
+                     cudaStream_t st);
+void launch_ws_collect(const StepParams& P, const DeviceState& S, const WsState& W, int count, int stride, int offset,
+                       long long pos, long long cap, cudaStream_t st);
+void launch_count_free(const uint8_t* act, int n, int* out, cudaStream_t st);
+// learned-guess guard: keep the guess with the smaller residual
+void launch_ws_save_plain(const DeviceState& S, cudaStream_t st);
+void launch_ws_guard(const StepParams& P, const DeviceState& S, const float4* xsave, const float4* rsave, int grid,
+                     cudaStream_t st);
 
 }  // namespace pdgb
