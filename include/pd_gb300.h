@@ -205,6 +205,9 @@ typedef struct pd_operator_view {
     const int32_t* perm;           /* n: slot -> caller index */
     const void* ref_pos;           /* mixed: float4 original positions minus origin */
     const void* disp;              /* mixed: float4 displacement x - X */
+    const void* pos_cell;          /* mixed: float4 position offset in its supercell, w = packed supercell coords */
+    const float* inv_d0;           /* mixed: 1 / d0 per bond slot */
+    double supercell_size;         /* mixed: supercell edge (a power of two) */
     const double* jac;             /* FP64: 6 entries per bond slot (xx yy zz xy xz yz) */
     const double* jac_diag;        /* FP64: 6 entries per particle */
     double mass;

@@ -636,3 +636,6 @@ void pdo_get_original_stretch(const pdo_state* s, double* o) { memcpy(o, s->ost,
 void pdo_get_bond_count(const pdo_state* s, int* o) { for (int i = 0; i < s->n; ++i) o[i] = s->top[i] + 1; }
 void pdo_get_row_ptr(const pdo_state* s, long* o) { memcpy(o, s->row_ptr, ((size_t)s->n + 1) * sizeof(long)); }
 void pdo_get_bond_list(const pdo_state* s, int* o) { if (s->total_bonds) memcpy(o, s->col, (size_t)s->total_bonds * sizeof(int)); }
+
+/* Diagonal 3x3 blocks of the assembled system matrix (row-major, 9 per particle). */
+void pdo_get_diag_blocks(const pdo_state* s, double* out) { memcpy(out, s->diag, 9 * (size_t)s->n * sizeof(double)); }

@@ -116,6 +116,7 @@ class OperatorView(C.Structure):
         ("n", C.c_int), ("precision", C.c_int), ("lanes_per_particle", C.c_int), ("blocks", C.c_int),
         ("activity", C.c_void_p), ("row_ptr", C.c_void_p), ("bond_count", C.c_void_p),
         ("bond_slot", C.c_void_p), ("perm", C.c_void_p), ("ref_pos", C.c_void_p), ("disp", C.c_void_p),
+        ("pos_cell", C.c_void_p), ("inv_d0", C.c_void_p), ("supercell_size", C.c_double),
         ("jac", C.c_void_p), ("jac_diag", C.c_void_p), ("mass", C.c_double), ("t2", C.c_double),
         ("bond_coeff", C.c_double), ("sphere_center_local", C.c_double * 3), ("sphere_stiffness", C.c_double),
     ]

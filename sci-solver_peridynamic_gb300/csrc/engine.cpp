@@ -133,7 +133,7 @@ void Engine::free_all()
 {
     ws_free();
     void* ptrs[] = {S_.act, S_.x64, S_.v64, S_.X64, S_.x64_bk, S_.v64_bk, S_.st, S_.ost, S_.nst, S_.row_ptr,
-                    S_.cnt, S_.cnt_bk, S_.col, S_.X32, S_.u32, S_.jac, S_.jdiag, S_.force, S_.rhs, S_.sol,
+                    S_.cnt, S_.cnt_bk, S_.col, S_.X32, S_.u32, S_.xs4, S_.inv_d0, S_.jac, S_.jdiag, S_.force, S_.rhs, S_.sol,
                     S_.r, S_.p, S_.y, S_.sc, S_.partials, S_.counters, S_.flags, d_perm_};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -160,6 +160,7 @@ pd_status Engine::allocate()
     CK(dalloc(&S_.cnt_bk, n), "alloc cnt backup");
     CK(dalloc(&S_.X32, n), "alloc X32");
     CK(dalloc(&S_.u32, n), "alloc u32");
+    if (!fp64_) CK(dalloc(&S_.xs4, n), "alloc xs4");
     void** vecs[] = {&S_.force, &S_.rhs, &S_.sol, &S_.r, &S_.p, &S_.y};
     for (void** v : vecs) {
         CK(cudaMalloc(v, r4 * (n ? n : 1)), "alloc vector");
@@ -248,6 +249,20 @@ pd_status Engine::make_ready()
     }
     if (fp64_) {
         CK(dalloc(&S_.jac, 6 * (size_t)std::max<long long>(total_slots_, 1)), "alloc jac");
+    } else {
+        // 1/d0 per bond slot, and the supercell frame of the FP32 positions:
+        // edge = the smallest power of two >= horizon, +-512 cells around the box centre
+        const size_t slots = (size_t)std::max<long long>(total_slots_, 1);
+        CK(dalloc(&S_.inv_d0, slots), "alloc inv_d0");
+        CK(cudaMemsetAsync(S_.inv_d0, 0, sizeof(float) * slots, stream_), "memset inv_d0");
+        if (n > 0) {
+            const int g = (int)std::min<long long>(std::max<long long>(((long long)n + kBlock - 1) / kBlock, 1), kMaxPartials);
+            launch_bond_geometry(S_, g, stream_);
+            ++launches_;
+        }
+        const double h = sim_.pd_horizon > 0 ? sim_.pd_horizon : 1.0;
+        sup_ = std::ldexp(1.0, (int)std::ceil(std::log2(h)));
+        for (int k = 0; k < 3; ++k) sup_lo_[k] = origin_[k] - 512.0 * sup_;
     }
     // CG scalars (initPDSolutions zeroed the solution, cg_solver.cuh:184-194)
     std::memset(h_sc_, 0, sizeof(CgScalars));
@@ -269,6 +284,10 @@ pd_status Engine::make_ready()
     L_.grid_vec = (int)std::max<long long>(1, std::min<long long>({need_vec, (long long)sm_count_ * 8, (long long)kMaxPartials}));
     L_.force_lanes = 8;
     L_.grid_force = grid_for_rows(L_.force_lanes, force_kernel_blocks_per_sm(fp64_, L_.force_lanes));
+    if (!fp64_ && n > 0) {   // supercell positions of the initial state (read by the SpMV)
+        launch_refresh(fp64_, step_params(), S_, L_, stream_);
+        ++launches_;
+    }
     s = tune_spmv();
     if (s != PD_OK) return s;
     // step state
@@ -380,6 +399,9 @@ StepParams Engine::step_params() const
     }
     P.sphere_r = opt_.sphere_radius;
     P.sphere_k = opt_.sphere_stiffness;
+    for (int k = 0; k < 3; ++k) P.sup_lo[k] = sup_lo_[k];
+    P.sup = sup_;
+    P.inv_sup = sup_ > 0 ? 1.0 / sup_ : 0.0;
     return P;
 }
 
@@ -595,6 +617,9 @@ pd_status Engine::operator_view(pd_operator_view* v) const
     v->perm = d_perm_;
     v->ref_pos = S_.X32;
     v->disp = S_.u32;
+    v->pos_cell = S_.xs4;
+    v->inv_d0 = S_.inv_d0;
+    v->supercell_size = sup_;
     v->jac = S_.jac;
     v->jac_diag = S_.jdiag;
     v->mass = P.mass;

@@ -86,6 +86,8 @@ private:
     std::vector<int32_t> h_act_;
     std::vector<int> perm_, inv_, cnt_init_;
     double origin_[3] = {0, 0, 0};
+    double sup_ = 0;              // supercell edge of the FP32 positions
+    double sup_lo_[3] = {0, 0, 0};
     double bond_coeff_ = 0;
     long long total_slots_ = 0;
     long long bonds_initial_ = 0;

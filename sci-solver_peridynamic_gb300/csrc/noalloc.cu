@@ -89,7 +89,7 @@ extern "C" pd_status pd_apply_operator_noalloc(const pd_operator_view* v, const 
     if (v->n > 0) {
         if (!d_x || !d_y || !v->activity || !v->row_ptr || !v->bond_count || !v->bond_slot)
             return reject("a required device pointer is NULL");
-        if (fp64 ? (!v->jac || !v->jac_diag) : (!v->ref_pos || !v->disp))
+        if (fp64 ? (!v->jac || !v->jac_diag) : (!v->ref_pos || !v->disp || !v->pos_cell || !v->inv_d0))
             return reject("the view lacks the arrays of its precision mode");
     }
     DeviceScratch scratch;
@@ -114,6 +114,10 @@ extern "C" pd_status pd_apply_operator_noalloc(const pd_operator_view* v, const 
     S.col = const_cast<int*>(v->bond_slot);
     S.X32 = (float4*)const_cast<void*>(v->ref_pos);
     S.u32 = (float4*)const_cast<void*>(v->disp);
+    S.xs4 = (float4*)const_cast<void*>(v->pos_cell);
+    S.inv_d0 = const_cast<float*>(v->inv_d0);
+    P.sup = v->supercell_size;
+    P.inv_sup = v->supercell_size > 0 ? 1.0 / v->supercell_size : 0.0;
     S.jac = const_cast<double*>(v->jac);
     S.jdiag = const_cast<double*>(v->jac_diag);
     int grid = v->blocks;

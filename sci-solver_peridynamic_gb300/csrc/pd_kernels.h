@@ -75,6 +75,10 @@ struct StepParams {
     double sphere_c[3];        // centre at the start of this step (absolute coordinates)
     double sphere_c_local[3];  // same, relative to the FP32 coordinate origin
     double sphere_r, sphere_k;
+    // supercells of edge sup (a power of two >= horizon) anchored at sup_lo:
+    // x = sup_lo + sup * ijk + offset, ijk in [0, 1023]^3
+    double sup_lo[3];
+    double sup, inv_sup;
 };
 
 // Device pointers of one handle (particles in cell-sorted order).
@@ -95,6 +99,8 @@ struct DeviceState {
     int* col;          // neighbour slots
     float4* X32;       // original positions relative to origin (mixed)
     float4* u32;       // displacement x - X (mixed)
+    float4* xs4;       // mixed: position as FP32 offset in its supercell, w = packed supercell coords
+    float* inv_d0;     // mixed: 1 / |X_q - X_p| per bond slot (from FP64)
     double* jac;       // FP64 mode: symmetric bond Jacobians, 6 per bond slot
     double* jdiag;     // FP64 mode: 6 per particle (sum of bond Jacobians + contact)
     void* force;       // Real4 per particle: pd_force
@@ -132,6 +138,7 @@ void launch_cg_axpy(bool fp64, const StepParams& P, const DeviceState& S, const 
 void launch_cg_xpby(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
 void launch_update(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
 void launch_refresh(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
+void launch_bond_geometry(const DeviceState& S, int grid, cudaStream_t st);
 // Max resident blocks per SM of the SpMV / force kernels (for grid sizing).
 int row_kernel_blocks_per_sm(bool fp64, int lanes, int unroll);
 int force_kernel_blocks_per_sm(bool fp64, int lanes);

@@ -52,6 +52,32 @@ __device__ __forceinline__ BondEval eval_bond(const dbl4& xp, const dbl4& Xp, co
     return b;
 }
 
+// Position as an FP32 offset inside its supercell plus the supercell's integer
+// coordinates (10 bits each) in the w lane.  A bond vector is then
+// (off_q - off_p) + sup * (ijk_q - ijk_p): the offsets are small, so the FP32
+// bond vector keeps ~2^-23 * sup / |xi| relative accuracy wherever the body is.
+__device__ __forceinline__ float4 encode_supercell(const StepParams& P, const dbl4& x)
+{
+    const double v[3] = {x.x - P.sup_lo[0], x.y - P.sup_lo[1], x.z - P.sup_lo[2]};
+    int c[3];
+    float o[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        int ck = (int)floor(v[k] * P.inv_sup);
+        ck = ck < 0 ? 0 : (ck > 1023 ? 1023 : ck);
+        c[k] = ck;
+        o[k] = (float)(v[k] - P.sup * (double)ck);
+    }
+    return make_float4(o[0], o[1], o[2], __int_as_float(c[0] | (c[1] << 10) | (c[2] << 20)));
+}
+
+__device__ __forceinline__ void supercell_delta(int wq, int wp, float sup, float& dx, float& dy, float& dz)
+{
+    dx = sup * (float)((wq & 1023) - (wp & 1023));
+    dy = sup * (float)(((wq >> 10) & 1023) - ((wp >> 10) & 1023));
+    dz = sup * (float)(((wq >> 20) & 1023) - ((wp >> 20) & 1023));
+}
+
 // fmaxf(stretch_p, stretch_q) of cg_solver.cuh:264: both limits rounded to float.
 __device__ __forceinline__ double break_threshold(float thp, double stq)
 {
@@ -75,8 +101,10 @@ __global__ void __launch_bounds__(kBlock) k_force(StepParams P, DeviceState S)
         const dbl4 xp = S.x64[p];
         const dbl4 Xp = S.X64[p];
         // FP32 displacement of this step's linear system (read by k_spmv)
-        if (!FP64 && lane == 0)
+        if (!FP64 && lane == 0) {
             S.u32[p] = make_float4((float)(xp.x - Xp.x), (float)(xp.y - Xp.y), (float)(xp.z - Xp.z), 0.f);
+            S.xs4[p] = encode_supercell(P, xp);
+        }
         if (a == ACT_INVISIBLE) continue;
         const float thp = (float)S.st[p];
         const int rs = S.row_ptr[p];
@@ -151,6 +179,11 @@ __global__ void __launch_bounds__(kBlock) k_force(StepParams P, DeviceState S)
                     if (b.s > break_threshold(thp, S.st[q])) {
                         S.col[rs + bond] = S.col[rs + top];
                         S.col[rs + top] = q;
+                        if (!FP64) {
+                            const float t = S.inv_d0[rs + bond];
+                            S.inv_d0[rs + bond] = S.inv_d0[rs + top];
+                            S.inv_d0[rs + top] = t;
+                        }
                         --top;
                         continue;
                     }
@@ -279,33 +312,37 @@ __global__ void __launch_bounds__(kBlock) k_spmv(StepParams P, DeviceState S, co
                 az += J[4] * wq.x + J[5] * wq.y + J[2] * wq.z;
             }
         } else {
-            const float4 Xp = __ldg(S.X32 + p);
-            const float4 Up = __ldg(S.u32 + p);
-            const float4* __restrict__ X32 = S.X32;
-            const float4* __restrict__ u32 = S.u32;
+            // per bond: the column index and 1/d0 stream in coalesced; the
+            // neighbour's supercell position and its CG entry are gathered
+            const float4 xp4 = __ldg(S.xs4 + p);
+            const int wp = __float_as_int(xp4.w);
+            const float sup = (float)P.sup;
+            const float4* __restrict__ xs4 = S.xs4;
             const float4* __restrict__ in32 = (const float4*)in;
             for (int j0 = lane; j0 < cn; j0 += G * U) {
                 // issue every load of U bonds before any arithmetic
                 int qq[U];
+                float id0[U];
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
                     const int j = j0 + u * G;
                     qq[u] = j < cn ? __ldcs(S.col + rs + j) : -1;
+                    id0[u] = j < cn ? __ldcs(S.inv_d0 + rs + j) : 0.f;
                 }
-                float4 Xq[U], Uq[U], Wq[U];
+                float4 Xq[U], Wq[U];
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
                     const int q = qq[u] < 0 ? p : qq[u];
-                    Xq[u] = __ldg(X32 + q);
-                    Uq[u] = __ldg(u32 + q);
+                    Xq[u] = __ldg(xs4 + q);
                     Wq[u] = __ldg(in32 + q);
                 }
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
                     if (qq[u] < 0) continue;
-                    const float x0 = Xq[u].x - Xp.x, y0 = Xq[u].y - Xp.y, z0 = Xq[u].z - Xp.z;
-                    const float xs = x0 + (Uq[u].x - Up.x), ys = y0 + (Uq[u].y - Up.y), zs = z0 + (Uq[u].z - Up.z);
-                    const float inv_d0 = rsqrtf(fmaf(x0, x0, fmaf(y0, y0, z0 * z0)));
+                    float cx, cy, cz;
+                    supercell_delta(__float_as_int(Xq[u].w), wp, sup, cx, cy, cz);
+                    const float xs = (Xq[u].x - xp4.x) + cx, ys = (Xq[u].y - xp4.y) + cy, zs = (Xq[u].z - xp4.z) + cz;
+                    const float inv_d0 = id0[u];
                     const float inv_d = rsqrtf(fmaf(xs, xs, fmaf(ys, ys, zs * zs)));
                     const float wx = (float)w.x - Wq[u].x, wy = (float)w.y - Wq[u].y, wz = (float)w.z - Wq[u].z;
                     const float a1 = inv_d0 - inv_d;
@@ -598,8 +635,28 @@ __global__ void __launch_bounds__(kBlock) k_refresh(StepParams P, DeviceState S)
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
         const dbl4 x = S.x64[i], X = S.X64[i];
         S.u32[i] = make_float4((float)(x.x - X.x), (float)(x.y - X.y), (float)(x.z - X.z), 0.f);
+        if (S.xs4) S.xs4[i] = encode_supercell(P, x);
         S.act[i] &= kActMask;
     }
+}
+
+// 1 / d0 per bond slot from the FP64 original positions (once, after the bond build)
+__global__ void __launch_bounds__(kBlock) k_bond_geometry(int n, DeviceState S)
+{
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const dbl4 Xp = S.X64[p];
+        const int rs = S.row_ptr[p], cn = S.cnt[p];
+        for (int j = 0; j < cn; ++j) {
+            const dbl4 Xq = S.X64[S.col[rs + j]];
+            const double dx = Xp.x - Xq.x, dy = Xp.y - Xq.y, dz = Xp.z - Xq.z;
+            S.inv_d0[rs + j] = (float)(1.0 / sqrt(dx * dx + dy * dy + dz * dz));
+        }
+    }
+}
+
+void launch_bond_geometry(const DeviceState& S, int grid, cudaStream_t st)
+{
+    k_bond_geometry<<<grid, kBlock, 0, st>>>(S.n, S);
 }
 
 // ---- launchers ------------------------------------------------------------------
