@@ -48,11 +48,16 @@ TARGET_N = 1_000_000
 def parse_args(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     ap.add_argument("--n", type=int, default=TARGET_N, help="target particle count")
     ap.add_argument("--lanes", type=int, default=0, help="lanes per particle row (0 = automatic)")
+    ap.add_argument("--unroll", type=int, default=0, help="SpMV gather unroll 1/2/4 (0 = automatic)")
+    ap.add_argument("--workload", choices=("ellipsoid", "batched", "learned", "beam"), default="ellipsoid",
+                    help="ellipsoid: the 1M-particle headline; batched: 64 scenes in one batch; learned: "
+                         "learned vs plain CG warm start on the 16^3 cube; beam: FP32 vs FP64 notched beam")
+    ap.add_argument("--check-every", type=int, default=10, help="beam: steps between FP32/FP64 comparisons")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args(argv)
@@ -216,6 +221,8 @@ def run_gb300(args):
     sc = scenes.ellipsoid_impact(target_n=args.n, gap=0.0)
     if args.lanes:
         sc.opt.lanes_per_particle = args.lanes
+    if args.unroll:
+        sc.opt.spmv_unroll = args.unroll
     sim = scenes.make_simulator(sc, device=local)
     sim.makeReady()
     sim.advance(args.warmup)
@@ -281,10 +288,11 @@ def run_gb300(args):
             "particles": n,
             "bonds_alive": int(bonds),
             "cg_iterations_per_step": round(iters / args.steps, 2),
-            "spmv_variant": "%d lanes x %d unroll (autotuned)" % (sim.params()[2].lanes_per_particle,
-                                                                   sim.params()[2].spmv_unroll),
+            "spmv_variant": "%d lanes x %d unroll (%s)" % (sim.params()[2].lanes_per_particle,
+                                                            sim.params()[2].spmv_unroll,
+                                                            "fixed" if args.lanes and args.unroll else "autotuned"),
             "parallelism": "replicas x%d" % world,
-            "l2": "inputs larger than L2 (bond list %.0f MB + particle state > 129 MB L2)" % (4 * bonds / 1e6),
+            "l2": "inputs larger than L2 (bond columns + 1/d0 %.0f MB + particle state > 129 MB L2)" % (8 * bonds / 1e6),
         },
         "gpu_launches": int(launches),
         "kernel_time_share": shares,
@@ -367,10 +375,251 @@ def run_reference(args):
     print(json.dumps(result), flush=True)
 
 
+# ---- other workloads (one JSON line each; not the headline metric) ----------------------
+def _timed(stream_handle, fn, local):
+    import torch
+    stream = torch.cuda.ExternalStream(stream_handle, device=torch.device("cuda", local))
+    torch.cuda.synchronize(local)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    fn()
+    ev1.record(stream)
+    torch.cuda.synchronize(local)
+    return ev0.elapsed_time(ev1)
+
+
+def run_batched(args):
+    """64 independent scenes (log-uniform 4096..65536 particles, horizons
+    4/5/6, impacts 1-10 m/s) stepped together by the batch API; compared with
+    the same scenes stepped one pd_handle at a time."""
+    import torch
+    pkg = importlib.import_module(PKG_NAME)
+    scenes = importlib.import_module(PKG_NAME + ".scenes")
+    local = 0
+    torch.cuda.set_device(local)
+    lst = scenes.batched_scenes(count=64, seed=0)
+    n_total = sum(sc.n for sc in lst)
+    b = pkg.Batch(local)
+    for sc in lst:
+        scenes.add_to_batch(b, sc)
+    b.makeReady()
+    cfg = b.config()
+    b.advance(args.warmup)
+    it0 = sum(b.stats(k).total_cg_iterations for k in range(len(lst)))
+    l0 = b.launch_count()
+    sampler = ClockSampler(local)
+    sampler.start()
+    ms = _timed(b.stream_handle(), lambda: b.advance(args.steps), local)
+    clocks = sampler.stop()
+    launches = b.launch_count() - l0
+    iters = sum(b.stats(k).total_cg_iterations for k in range(len(lst))) - it0
+    bonds = sum(b.stats(k).bonds_alive for k in range(len(lst)))
+    max_iters = max(b.stats(k).last_cg_iterations for k in range(len(lst)))
+    b.close()
+    # the same scenes, one handle each, stepped in turn
+    sims = []
+    for sc in lst:
+        s = scenes.make_simulator(sc, local)
+        s.makeReady()
+        s.advance(args.warmup)
+        s.synchronize()
+        sims.append(s)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for s in sims:
+            s.advance(1)
+    for s in sims:
+        s.synchronize()
+    t_seq = time.perf_counter() - t0
+    for s in sims:
+        s.close()
+    spmv_bytes = 4.0 * bonds + 64.0 * n_total
+    achieved = spmv_bytes / (cfg.tuned_spmv_ms / 1e3) / 1e9 if cfg.tuned_spmv_ms > 0 else None
+    peak, peak_kind = measured_peak_hbm()
+    value = args.steps / (ms / 1e3)
+    result = {
+        "metric": "batched implicit steps/s (64 scenes, every scene advances one step)",
+        "value": round(value, 4), "unit": "steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 force/SpMV, f64 stretch test + master state, double-float->f64 dots",
+        "data": "synthetic (seeded jittered blocks and balls)",
+        "config": {"workload": "64 impact bodies, %d particles in total (log-uniform 4096..65536 each), horizons "
+                               "4/5/6 r, impacts 1-10 m/s, blocks implicit Euler dt=1e-4, balls Newmark dt=5e-5, "
+                               "CG rel 1e-6" % n_total,
+                   "particles": n_total, "bonds_alive": int(bonds), "scenes": len(lst),
+                   "cg_iterations_per_step_all_scenes": round(iters / args.steps, 1),
+                   "cg_iterations_last_step_max": int(max_iters),
+                   "launch_shape": {"lanes": cfg.lanes_per_particle, "unroll": cfg.spmv_unroll,
+                                    "item_rows": cfg.item_rows, "work_items": cfg.work_items,
+                                    "grid_pre": cfg.grid_pre, "grid_cg": cfg.grid_cg,
+                                    "autotuned": bool(cfg.autotuned)},
+                   "l2": "inputs larger than L2 (bond columns + 1/d0 %.0f MB)" % (8 * bonds / 1e6)},
+        "gpu_launches": int(launches),
+        "scene_steps_per_s": round(value * len(lst), 2),
+        "particle_steps_per_s": round(value * n_total, 1),
+        "unbatched": {"value": round(args.steps / t_seq, 4), "unit": "steps/s",
+                      "what": "the same 64 scenes as 64 pd_handles, pd_advance(1) each in turn, wall clock"},
+        "roofline": {"kernel": "SpMV phase of k_batch_cg over all scenes (autotuner timing)", "bound": "hbm",
+                     "achieved": round(achieved, 1) if achieved else None, "peak": peak, "peak_kind": peak_kind,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None, "traffic": None,
+                     "algorithmic_bytes_per_launch": int(spmv_bytes)},
+        "clocks": clocks,
+    }
+    print(json.dumps(result), flush=True)
+
+
+def run_learned(args):
+    """Learned vs plain CG warm start on the 16^3 cube: 5 training seeds x
+    100 steps x 100 sampled particles = 50k pairs, BF16 MLP trained on the
+    GPU, then 100 steps of the seed-0 scene with each warm start."""
+    import numpy as np
+    import torch
+    pkg = importlib.import_module(PKG_NAME)
+    scenes = importlib.import_module(PKG_NAME + ".scenes")
+    ws = importlib.import_module(PKG_NAME + ".warmstart")
+    local = 0
+    torch.cuda.set_device(local)
+    t0 = time.perf_counter()
+    X, T = ws.collect(lambda s: scenes.cube_lattice(seed=s), seeds=[1, 2, 3, 4, 5], steps=100, samples_per_step=100)
+    t_collect = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    params, loss = ws.train(X, T, iterations=3000)
+    t_train = time.perf_counter() - t0
+    out = {}
+    for mode in (0, 1):
+        sc = scenes.cube_lattice(seed=0)
+        sc.opt.warm_start = mode
+        sim = scenes.make_simulator(sc, local)
+        sim.makeReady()
+        if mode:
+            sim.ws_set_params(params)
+        sim.advance(args.warmup)
+        st0 = sim.stats()
+        steps = 100 - args.warmup
+        ms = _timed(sim.stream_handle(), lambda: sim.advance(steps), local)
+        st1 = sim.stats()
+        out["learned" if mode else "plain"] = {
+            "steps_per_s": round(steps / (ms / 1e3), 3),
+            "cg_iterations_per_step": round((st1.total_cg_iterations - st0.total_cg_iterations) / steps, 2),
+            "position": sim.get(pkg.VAR_POSITION), "kept": int(st1.ws_guesses_kept),
+            "alive": sim.alive_sets(),
+        }
+        sim.close()
+    pl, le = out["plain"], out["learned"]
+    same = all(np.array_equal(a, c) for a, c in zip(pl["alive"], le["alive"]))
+    dpos = float(np.abs(pl["position"] - le["position"])[:, :3].max() / np.abs(pl["position"][:, :3]).max())
+    result = {
+        "metric": "CG iterations per step, learned vs plain warm start (rel. residual 1e-6)",
+        "value": round(pl["cg_iterations_per_step"] / max(le["cg_iterations_per_step"], 1e-9), 4),
+        "unit": "plain/learned iterations ratio", "higher_is_better": True, "n_gpus": 1,
+        "steps": 100 - args.warmup, "warmup": args.warmup, "dtype": "bf16 MLP (f32 accumulate), f32/f64 CG",
+        "data": "synthetic (16^3 jittered cube, training seeds 1-5, evaluation seed 0)",
+        "config": {"workload": "cube_lattice 16^3 = 4096 particles, implicit Euler dt=1e-4, CG rel 1e-6, 100 steps",
+                   "training_pairs": int(X.shape[0]), "train_iterations": 3000, "final_loss": float(loss),
+                   "collect_s": round(t_collect, 2), "train_s": round(t_train, 2)},
+        "plain": {k: pl[k] for k in ("steps_per_s", "cg_iterations_per_step")},
+        "learned": {k: le[k] for k in ("steps_per_s", "cg_iterations_per_step", "kept")},
+        "steps_per_s_ratio": round(le["steps_per_s"] / pl["steps_per_s"], 4),
+        "same_broken_bond_set": bool(same),
+        "max_position_difference_rel": dpos,
+    }
+    print(json.dumps(result), flush=True)
+
+
+def _bond_set_difference(sim_a, sim_b):
+    """Bonds alive in exactly one of two runs of the same scene (each bond
+    counted once).  Rows are compared by count and an order-free hash of
+    their live neighbours; only rows that differ are compared exactly."""
+    import numpy as np
+    ra, la, ca = sim_a.bond_rows()
+    rb, lb, cb = sim_b.bond_rows()
+
+    def row_hash(rp, bl, cnt):
+        v = bl.astype(np.uint64) * np.uint64(0x9E3779B97F4A7C15)
+        v ^= v >> np.uint64(29)
+        cs = np.zeros(v.size + 1, np.uint64)
+        np.cumsum(v, dtype=np.uint64, out=cs[1:])
+        start = rp[:-1].astype(np.int64)
+        return cs[start + cnt] - cs[start]
+
+    ha, hb = row_hash(ra, la, ca), row_hash(rb, lb, cb)
+    rows = np.nonzero((ca != cb) | (ha != hb))[0]
+    diff = 0
+    for i in rows:
+        a = la[ra[i]:ra[i] + ca[i]]
+        b = lb[rb[i]:rb[i] + cb[i]]
+        diff += len(np.setxor1d(a, b))
+    return diff // 2
+
+
+def run_beam(args):
+    """Precision study: the notched beam (2M particles, horizon 6r, three-point
+    bending) stepped in mixed precision and in FP64 side by side; every
+    --check-every steps the positions and the broken-bond sets are compared."""
+    import numpy as np
+    import torch
+    pkg = importlib.import_module(PKG_NAME)
+    scenes = importlib.import_module(PKG_NAME + ".scenes")
+    local = 0
+    torch.cuda.set_device(local)
+    sims = {}
+    for prec in (pkg.PRECISION_MIXED, pkg.PRECISION_FP64):
+        sc = scenes.notched_beam(target_n=args.n if args.n != TARGET_N else 2_000_000, precision=prec)
+        s = scenes.make_simulator(sc, local)
+        s.makeReady()
+        sims[prec] = s
+    n = sc.n
+    mixed, fp64 = sims[pkg.PRECISION_MIXED], sims[pkg.PRECISION_FP64]
+    b0 = fp64.stats().bonds_initial
+    rows = []
+    t_mixed = t_fp64 = 0.0
+    done = 0
+    while done < args.steps:
+        k = min(args.check_every, args.steps - done)
+        t_mixed += _timed(mixed.stream_handle(), lambda: mixed.advance(k), local)
+        t_fp64 += _timed(fp64.stream_handle(), lambda: fp64.advance(k), local)
+        done += k
+        xm, xd = mixed.get(pkg.VAR_POSITION), fp64.get(pkg.VAR_POSITION)
+        um = xm - sc.pos
+        ud = xd - sc.pos
+        err_x = float(np.abs(xm - xd)[:, :3].max() / np.abs(xd[:, :3]).max())
+        err_u = float(np.abs(um - ud)[:, :3].max() / max(np.abs(ud[:, :3]).max(), 1e-300))
+        diff = _bond_set_difference(mixed, fp64)
+        rows.append({"step": done, "pos_rel_err": err_x, "disp_rel_err": err_u, "bond_set_diff": int(diff),
+                     "bonds_broken_fp64": int(b0 - fp64.stats().bonds_alive),
+                     "cg_iters_mixed": int(mixed.stats().last_cg_iterations),
+                     "cg_iters_fp64": int(fp64.stats().last_cg_iterations),
+                     "ticks_mixed": int(mixed.stats().time_step_ticks),
+                     "ticks_fp64": int(fp64.stats().time_step_ticks)})
+    result = {
+        "metric": "FP32 vs FP64 step on the notched beam: max position error per check, bond-set differences",
+        "value": max(r["pos_rel_err"] for r in rows), "unit": "max relative position difference",
+        "higher_is_better": False, "n_gpus": 1, "steps": args.steps, "warmup": 0, "dtype": "f32 vs f64",
+        "data": "synthetic (seeded jittered notched beam)",
+        "config": {"workload": "notched_beam %d particles, 1.0x0.2x0.2 m, notch 0.05 m, horizon 6r, s0 0.01, "
+                               "load strip at 1 m/s, Newmark dt=5e-5, CG rel 1e-6" % n,
+                   "check_every": args.check_every, "bonds_initial": int(b0)},
+        "mixed_steps_per_s": round(args.steps / (t_mixed / 1e3), 4),
+        "fp64_steps_per_s": round(args.steps / (t_fp64 / 1e3), 4),
+        "checks": rows,
+    }
+    for s in sims.values():
+        s.close()
+    print(json.dumps(result), flush=True)
+
+
 def main(argv=None):
     args = parse_args(argv)
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batched":
+        run_batched(args)
+    elif args.workload == "learned":
+        run_learned(args)
+    elif args.workload == "beam":
+        run_beam(args)
     else:
         run_gb300(args)
 

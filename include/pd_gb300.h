@@ -336,6 +336,68 @@ pd_status pd_get_stream(pd_handle* h, void** stream);
 /* Waits until all work of the handle has finished on the device. */
 pd_status pd_synchronize(pd_handle* h);
 
+/* ---- batched scenes (no reference counterpart) -----------------------------
+ * Many independent scenes (each with the parameter surface of one Simulator)
+ * stepped together: per step, two cooperative persistent launches cover every
+ * scene -- force passes and adaptive decisions, then the CG iterations of all
+ * scenes until each has converged, then the update -- replayed from one CUDA
+ * graph.  Each scene keeps its own step state, time step, CG scalars and
+ * statistics, and gives the same results as a pd_handle of its own (within the
+ * CG tolerance: per-scene sums are reduced in a different, fixed order).  All
+ * scenes of a batch use the same precision.  Scenes are numbered in the order
+ * of pd_batch_add_scene; "offsets" are the scenes' first particles in the
+ * concatenation of all scenes in that order. */
+typedef struct pd_batch pd_batch;
+
+typedef struct pd_batch_options {
+    int lanes_per_particle;   /* SpMV lanes per particle row: 4 or 8, 0 = autotune */
+    int spmv_unroll;          /* 2 or 4, 0 = autotune */
+    int item_rows;            /* rows per work item: 64..4096, 0 = autotune */
+    int use_graph;            /* 1 (default): replay each step from a CUDA graph */
+} pd_batch_options;
+
+/* The launch shape in use after pd_batch_make_ready. */
+typedef struct pd_batch_config {
+    int lanes_per_particle;
+    int spmv_unroll;
+    int item_rows;
+    int work_items;
+    int grid_pre;             /* blocks of the force/decision launch */
+    int grid_cg;              /* blocks of the CG launch */
+    int autotuned;            /* 1 when the shape was measured, 0 when fixed/default */
+    double tuned_spmv_ms;     /* SpMV phase time of the chosen shape (autotuned only) */
+} pd_batch_config;
+
+pd_status pd_batch_options_default(pd_batch_options* opt);
+/* device: CUDA device ordinal; opt may be NULL. */
+pd_status pd_batch_create(int device, const pd_batch_options* opt, pd_batch** out);
+pd_status pd_batch_destroy(pd_batch* b);
+/* Adds a scene (as pd_create; opt may be NULL); its index is returned in *scene. */
+pd_status pd_batch_add_scene(pd_batch* b, const pd_sim_params* sim, const pd_run_params* run,
+                             const pd_solver_options* opt, int* scene);
+/* As pd_set_particles / pd_set_stretch_limits for one scene. */
+pd_status pd_batch_set_particles(pd_batch* b, int scene, const double* pos4, const double* vel4,
+                                 const int32_t* activity, int n);
+pd_status pd_batch_set_stretch_limits(pd_batch* b, int scene, const double* s0, int n);
+/* pd_make_ready of every scene, then work items, launch shape and graph. */
+pd_status pd_batch_make_ready(pd_batch* b);
+/* nsteps steps of every scene (a scene whose CG failed stops, as pd_advance). */
+pd_status pd_batch_advance(pd_batch* b, int nsteps);
+pd_status pd_batch_scene_count(pd_batch* b, int* count);
+/* offsets[0..count]: first particle of each scene in the concatenation; offsets[count] = total. */
+pd_status pd_batch_scene_offsets(pd_batch* b, int64_t* offsets, int count_plus_one);
+/* Per-scene queries (as the pd_handle calls). */
+pd_status pd_batch_get(pd_batch* b, int scene, pd_variable var, void* dst, size_t bytes);
+pd_status pd_batch_get_size(pd_batch* b, int scene, pd_variable var, size_t* bytes);
+pd_status pd_batch_get_stats(pd_batch* b, int scene, pd_step_stats* stats);
+pd_status pd_batch_finished(pd_batch* b, int scene, int* finished);
+pd_status pd_batch_get_config(pd_batch* b, pd_batch_config* config);
+pd_status pd_batch_get_launch_count(pd_batch* b, long long* launches);
+pd_status pd_batch_get_stream(pd_batch* b, void** stream);
+pd_status pd_batch_synchronize(pd_batch* b);
+/* Last error text of a batch. */
+const char* pd_batch_last_error_message(pd_batch* b);
+
 /* ---- errors --------------------------------------------------------------- */
 const char* pd_status_string(pd_status s);
 /* Last error text of a handle (or of the last failed pd_create when h is NULL). */

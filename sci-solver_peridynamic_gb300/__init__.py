@@ -129,6 +129,19 @@ class KernelTimes(C.Structure):
 _lib = None
 
 
+class BatchOptions(C.Structure):
+    """pd_batch_options: SpMV launch shape and item size (0 = autotune), graph replay."""
+    _fields_ = [("lanes_per_particle", C.c_int), ("spmv_unroll", C.c_int), ("item_rows", C.c_int),
+                ("use_graph", C.c_int)]
+
+
+class BatchConfig(C.Structure):
+    """pd_batch_config: the launch shape in use."""
+    _fields_ = [("lanes_per_particle", C.c_int), ("spmv_unroll", C.c_int), ("item_rows", C.c_int),
+                ("work_items", C.c_int), ("grid_pre", C.c_int), ("grid_cg", C.c_int), ("autotuned", C.c_int),
+                ("tuned_spmv_ms", C.c_double)]
+
+
 def library(build_if_missing: bool = True):
     """Load libpd_gb300.so (building it first if needed)."""
     global _lib
@@ -187,6 +200,26 @@ def library(build_if_missing: bool = True):
         "pd_abi_version": (C.c_int, []),
         "pd_sample_stretch_limits": (st, [C.c_float, C.c_int, P(C.c_double)]),
         "pd_adaptive_decide": (st, [C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_int), P(C.c_int), P(C.c_int)]),
+        "pd_batch_options_default": (st, [P(BatchOptions)]),
+        "pd_batch_create": (st, [C.c_int, P(BatchOptions), P(vp)]),
+        "pd_batch_destroy": (st, [vp]),
+        "pd_batch_add_scene": (st, [vp, P(SimulationParameters), P(RunningParameters), P(SolverOptions),
+                                    P(C.c_int)]),
+        "pd_batch_set_particles": (st, [vp, C.c_int, P(C.c_double), P(C.c_double), P(C.c_int32), C.c_int]),
+        "pd_batch_set_stretch_limits": (st, [vp, C.c_int, P(C.c_double), C.c_int]),
+        "pd_batch_make_ready": (st, [vp]),
+        "pd_batch_advance": (st, [vp, C.c_int]),
+        "pd_batch_scene_count": (st, [vp, P(C.c_int)]),
+        "pd_batch_scene_offsets": (st, [vp, P(C.c_int64), C.c_int]),
+        "pd_batch_get": (st, [vp, C.c_int, C.c_int, vp, C.c_size_t]),
+        "pd_batch_get_size": (st, [vp, C.c_int, C.c_int, P(C.c_size_t)]),
+        "pd_batch_get_stats": (st, [vp, C.c_int, P(StepStats)]),
+        "pd_batch_finished": (st, [vp, C.c_int, P(C.c_int)]),
+        "pd_batch_get_config": (st, [vp, P(BatchConfig)]),
+        "pd_batch_get_launch_count": (st, [vp, P(C.c_longlong)]),
+        "pd_batch_get_stream": (st, [vp, P(vp)]),
+        "pd_batch_synchronize": (st, [vp]),
+        "pd_batch_last_error_message": (C.c_char_p, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -474,3 +507,126 @@ class Simulator:
         v = C.c_longlong()
         _check(self.lib.pd_get_launch_count(self.h, C.byref(v)), self.h)
         return v.value
+
+
+def _bcheck(status, batch=None):
+    if status != PD_OK:
+        lib = library(False)
+        msg = lib.pd_batch_last_error_message(batch)
+        raise PdError(status, msg.decode() if msg else "")
+
+
+class Batch:
+    """Many independent scenes stepped together (pd_batch_*, no reference
+    counterpart).  Each scene has the parameter surface of one Simulator;
+    per-scene exports and statistics answer as that Simulator would.
+
+        b = Batch(device=0)
+        k = b.add_scene(sim, run, options, pos4, vel4, activity, s0=None)
+        b.makeReady(); b.advance(100); b.get(k, VAR_POSITION)
+    """
+
+    def __init__(self, device: int = 0, options: BatchOptions | None = None):
+        self.lib = library()
+        if options is None:
+            options = BatchOptions()
+            self.lib.pd_batch_options_default(C.byref(options))
+        self.options = options
+        h = C.c_void_p()
+        _bcheck(self.lib.pd_batch_create(int(device), C.byref(options), C.byref(h)))
+        self.h = h
+        self.sizes = []
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pd_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_scene(self, sim: SimulationParameters, run: RunningParameters, options: SolverOptions | None,
+                  pos4, vel4=None, activity=None, s0=None) -> int:
+        dp = C.POINTER(C.c_double)
+        opts = options if options is not None else default_options()
+        k = C.c_int()
+        _bcheck(self.lib.pd_batch_add_scene(self.h, C.byref(sim), C.byref(run), C.byref(opts), C.byref(k)), self.h)
+        n = int(sim.num_pd_particle)
+        pos = np.ascontiguousarray(pos4, np.float64).reshape(n, 4)
+        vel = np.ascontiguousarray(vel4 if vel4 is not None else np.zeros((n, 4)), np.float64).reshape(n, 4)
+        act = np.ascontiguousarray(activity if activity is not None else np.zeros(n), np.int32)
+        _bcheck(self.lib.pd_batch_set_particles(self.h, k.value, pos.ctypes.data_as(dp), vel.ctypes.data_as(dp),
+                                                act.ctypes.data_as(C.POINTER(C.c_int32)), n), self.h)
+        if s0 is not None:
+            s = np.ascontiguousarray(s0, np.float64)
+            _bcheck(self.lib.pd_batch_set_stretch_limits(self.h, k.value, s.ctypes.data_as(dp), n), self.h)
+        self.sizes.append(n)
+        return k.value
+
+    def makeReady(self):
+        _bcheck(self.lib.pd_batch_make_ready(self.h), self.h)
+
+    def advance(self, nsteps: int = 1):
+        _bcheck(self.lib.pd_batch_advance(self.h, int(nsteps)), self.h)
+
+    def scene_count(self) -> int:
+        v = C.c_int()
+        _bcheck(self.lib.pd_batch_scene_count(self.h, C.byref(v)), self.h)
+        return v.value
+
+    def offsets(self) -> np.ndarray:
+        n = self.scene_count()
+        out = np.zeros(n + 1, np.int64)
+        _bcheck(self.lib.pd_batch_scene_offsets(self.h, out.ctypes.data_as(C.POINTER(C.c_int64)), n + 1), self.h)
+        return out
+
+    def get(self, scene: int, var: int) -> np.ndarray:
+        size = C.c_size_t()
+        _bcheck(self.lib.pd_batch_get_size(self.h, scene, var, C.byref(size)), self.h)
+        if var in (VAR_ACTIVITY, VAR_BOND_COUNT, VAR_BOND_LIST, VAR_SLOT_PERMUTATION):
+            out = np.zeros(size.value // 4, np.int32)
+        elif var == VAR_BOND_ROW_PTR:
+            out = np.zeros(size.value // 8, np.int64)
+        else:
+            out = np.zeros(size.value // 8, np.float64)
+        _bcheck(self.lib.pd_batch_get(self.h, scene, var, out.ctypes.data_as(C.c_void_p), size.value), self.h)
+        if var in (VAR_POSITION, VAR_VELOCITY, VAR_FORCE, VAR_SOLUTION, VAR_POSITION_SCALED, VAR_ORIGINAL_POSITION):
+            out = out.reshape(self.sizes[scene], 4)
+        return out
+
+    def alive_sets(self, scene: int):
+        rp = self.get(scene, VAR_BOND_ROW_PTR)
+        bl = self.get(scene, VAR_BOND_LIST)
+        cnt = self.get(scene, VAR_BOND_COUNT)
+        return [bl[rp[i]:rp[i] + cnt[i]] for i in range(self.sizes[scene])]
+
+    def stats(self, scene: int) -> StepStats:
+        s = StepStats()
+        _bcheck(self.lib.pd_batch_get_stats(self.h, scene, C.byref(s)), self.h)
+        return s
+
+    def finished(self, scene: int) -> bool:
+        v = C.c_int()
+        _bcheck(self.lib.pd_batch_finished(self.h, scene, C.byref(v)), self.h)
+        return bool(v.value)
+
+    def config(self) -> BatchConfig:
+        c = BatchConfig()
+        _bcheck(self.lib.pd_batch_get_config(self.h, C.byref(c)), self.h)
+        return c
+
+    def launch_count(self) -> int:
+        v = C.c_longlong()
+        _bcheck(self.lib.pd_batch_get_launch_count(self.h, C.byref(v)), self.h)
+        return v.value
+
+    def stream_handle(self) -> int:
+        v = C.c_void_p()
+        _bcheck(self.lib.pd_batch_get_stream(self.h, C.byref(v)), self.h)
+        return v.value or 0
+
+    def synchronize(self):
+        _bcheck(self.lib.pd_batch_synchronize(self.h), self.h)

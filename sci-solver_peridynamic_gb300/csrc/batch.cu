@@ -1,0 +1,508 @@
+// batch.cu -- persistent multi-scene step kernels (cooperative launches).
+//
+// Each phase of the reference step (Simulator::integratePeridynamics*,
+// simulator.cu:297-652, and CUSP krylov::cg) runs over the work items of the
+// scenes taking part, strided over all blocks so that a lone large scene still
+// spreads over the whole GPU; phases are separated by a grid barrier.  Scalar
+// work of a scene (adaptive time-step decision, CG alpha / beta / test) is done
+// by the block that reduces the scene's last item (reductions) or by the
+// scene's owner block (step-loop bookkeeping).
+//
+// Memory visibility: every barrier is a gpu-scope release/acquire; data that
+// a phase writes and a later phase of the same launch gathers from other rows
+// is read through the coherent load path, never the read-only one.
+#include "batch.h"
+#include "step_rows.cuh"
+
+namespace pdgb {
+
+namespace {
+
+constexpr unsigned long long kBarrierTimeoutNs = 5000000000ull;   // 5 s
+constexpr int kForceLanes = 8;
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Sense-counting grid barrier.  A wait is bounded: after kBarrierTimeoutNs
+// the block records the error and every later barrier returns false at once,
+// so the launch ends instead of hanging.  Returns false on error.
+__device__ bool grid_barrier(BatchSync* sync)
+{
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned g = ld_acquire(&sync->gen);
+        __threadfence();
+        const unsigned prev = atomicAdd(&sync->count, 1u);
+        if (prev == gridDim.x - 1) {
+            atomicExch(&sync->count, 0u);
+            __threadfence();
+            atomicAdd(&sync->gen, 1u);
+        } else {
+            const unsigned long long t0 = global_ns();
+            unsigned spins = 0;
+            while (ld_acquire(&sync->gen) == g) {
+                if (*(volatile int*)&sync->error) break;
+                __nanosleep(32);
+                if ((++spins & 63u) == 0 && global_ns() - t0 > kBarrierTimeoutNs) {
+                    atomicExch(&sync->error, 1);
+                    break;
+                }
+            }
+        }
+        __threadfence();
+        s_ok = *(volatile int*)&sync->error == 0;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+__device__ __forceinline__ int ld_volatile(const int* p) { return *(const volatile int*)p; }
+
+// Block reduction of one item's partial; the block that completes a scene sums
+// the scene's item partials in item order and runs fin(total) on thread 0.
+template <typename Acc, typename Fin>
+__device__ __forceinline__ void item_reduce(Acc acc, const BatchArgs& A, int item, const SceneConst& C, int s, Fin fin)
+{
+    __shared__ double warp_sums[kBlock / 32];
+    __shared__ bool is_last;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    __syncthreads();
+    const double w = warp_total(acc);
+    if (lane == 0) warp_sums[warp] = w;
+    __syncthreads();
+    const int count = C.item_end - C.item_begin;
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += warp_sums[i];
+        A.partials[item] = t;
+        __threadfence();
+        const unsigned prev = atomicAdd(A.counters + s, 1u);
+        is_last = (prev == (unsigned)count - 1u);
+    }
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    double t = 0.0;
+    for (int i = threadIdx.x; i < count; i += blockDim.x) t += __ldcg(A.partials + C.item_begin + i);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+    __syncthreads();
+    if (lane == 0) warp_sums[warp] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double total = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) total += warp_sums[i];
+        A.counters[s] = 0u;
+        fin(total);
+        __threadfence();
+    }
+}
+
+// Time-dependent step constants of a scene (Engine::step_params).
+__device__ __forceinline__ void set_time_fields(StepParams& P, const SceneConst& C, const SceneRun& R)
+{
+    P.ticks = R.ticks;
+    P.cs = R.cs;
+    P.h = R.ticks * C.dt_base;
+    P.t2 = C.integrator == 0 ? P.h * P.h : (P.h * P.h) / 4.0;
+    for (int k = 0; k < 3; ++k) {
+        P.sphere_c[k] = C.sphere_center0[k] + C.sphere_velocity[k] * R.sim_time;
+        P.sphere_c_local[k] = P.sphere_c[k] - C.origin[k];
+    }
+}
+
+// The adaptive time-step decision of integratePeridynamics* (simulator.cu:540-572).
+__device__ __forceinline__ int adaptive_decide(int has_broken, const SceneConst& C, SceneRun& R)
+{
+    if (has_broken) {
+        if (R.ticks > C.ticks_min) {
+            R.ticks /= 2;
+            return 1;
+        }
+        R.substep = 1;
+    } else {
+        if (R.substep > 0) ++R.substep;
+        if (R.substep >= C.max_substep) {
+            R.ticks *= 2;
+            R.substep = (R.ticks >= C.ticks_base) ? 0 : 1;
+        }
+    }
+    return 0;
+}
+
+// ---- per-phase item lists ----------------------------------------------------------
+// Block b owns items b, b + grid, b + 2 grid, ...: a scene's items spread over
+// consecutive blocks, so a lone large scene still uses the whole GPU.  At the
+// start of a phase each block tests up to kBlock of its items at once (one
+// parallel round of flag loads) and compacts the ones taking part, in item
+// order, into shared memory.
+enum : int { kSelForce = 0, kSelRestore = 1, kSelSolving = 2, kSelRunning = 3, kSelAll = 4 };
+
+struct ItemList {
+    int idx[kBlock];
+    int count;
+};
+
+__device__ __forceinline__ bool selected(const BatchArgs& A, int s, int sel)
+{
+    const SceneRun* R = A.run + s;
+    switch (sel) {
+    case kSelForce: return ld_volatile(&R->active) != 0;
+    case kSelRestore: return ld_volatile(&R->restore) != 0;
+    case kSelSolving: return ld_volatile(&R->solving) != 0;
+    case kSelRunning: return ld_volatile(&R->solving) != 0 && ld_volatile(&A.scenes[s].S.sc->done) == 0;
+    default: return true;
+    }
+}
+
+__device__ __forceinline__ void build_chunk(const BatchArgs& A, int sel, int c0, ItemList& L)
+{
+    __shared__ int warp_cnt[kBlock / 32];
+    __syncthreads();   // the previous chunk's items are done
+    const int i = (int)blockIdx.x + (c0 + (int)threadIdx.x) * (int)gridDim.x;
+    const bool f = i < A.n_items && selected(A, A.items[i].scene, sel);
+    const unsigned b = __ballot_sync(0xffffffffu, f);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) warp_cnt[warp] = __popc(b);
+    __syncthreads();
+    int off = 0;
+    for (int w = 0; w < warp; ++w) off += warp_cnt[w];
+    if (f) L.idx[off + __popc(b & ((1u << lane) - 1u))] = i;
+    if (threadIdx.x == kBlock - 1) L.count = off + __popc(b);
+    __syncthreads();
+}
+
+// fn(item index, item) for this block's items selected by `sel`; every
+// thread of the block runs every call (fn may contain block barriers).
+template <typename Fn>
+__device__ __forceinline__ void for_each_item(const BatchArgs& A, int sel, ItemList& L, Fn fn)
+{
+    const int b = (int)blockIdx.x, g = (int)gridDim.x;
+    const int mine = A.n_items > b ? (A.n_items - b + g - 1) / g : 0;
+    for (int c0 = 0; c0 < mine; c0 += kBlock) {
+        build_chunk(A, sel, c0, L);
+        const int count = L.count;
+        for (int k = 0; k < count; ++k) {
+            const int i = L.idx[k];
+            fn(i, A.items[i]);
+        }
+    }
+}
+
+// ---- phases ------------------------------------------------------------------------
+template <int G, bool FP64>
+__device__ void force_item(const SceneDesc& d, const WorkItem& it)
+{
+    const unsigned gmask = group_mask<G>();
+    const int lane = threadIdx.x & (G - 1);
+    constexpr int gpb = kBlock / G;
+    for (int p = it.lo + threadIdx.x / G; p < it.hi; p += gpb) force_row<G, FP64>(d.P, d.S, p, lane, gmask);
+}
+
+template <int G, bool FP64, bool DOT, int U, int LD, typename Acc>
+__device__ void spmv_item(const SceneDesc& d, const WorkItem& it, const void* in_, void* out_, Acc& acc)
+{
+    using Real = typename std::conditional<FP64, double, float>::type;
+    using V4 = typename Vec4<Real>::type;
+    const unsigned gmask = group_mask<G>();
+    const int lane = threadIdx.x & (G - 1);
+    constexpr int gpb = kBlock / G;
+    // every group runs the same number of trips (the shuffles need whole groups)
+    for (int p0 = it.lo; p0 < it.hi; p0 += gpb) {
+        const int p = p0 + threadIdx.x / G;
+        if (p < it.hi) spmv_row<G, FP64, DOT, U, LD>(d.P, d.S, (const V4*)in_, (V4*)out_, p, lane, gmask, acc);
+    }
+}
+
+// ---- k_batch_pre ---------------------------------------------------------------------
+// The scenes' descriptors are read in place: their time-dependent fields are
+// rewritten by owner blocks only in phases separated from the readers by a
+// grid barrier.
+template <bool FP64>
+__global__ void __launch_bounds__(kBlock) k_batch_pre(BatchArgs A)
+{
+    using Real = typename std::conditional<FP64, double, float>::type;
+    using Acc = typename DotAccFor<Real>::type;
+    __shared__ ItemList L;
+
+    // step start (Simulator::advance: ++step, phase-in clockScale, retries = 0)
+    if (threadIdx.x == 0) {
+        for (int s = blockIdx.x; s < A.n_scenes; s += gridDim.x) {
+            SceneRun& R = A.run[s];
+            SceneDesc& D = A.scenes[s];
+            R.solving = 0;
+            R.restore = 0;
+            R.active = 0;
+            if (!R.cg_converged || R.error || D.C.n == 0) continue;
+            R.step += 1;
+            if (R.step <= D.C.phase_in_steps) R.cs = (double)R.step / (double)D.C.phase_in_steps;
+            R.retries = 0;
+            R.active = 1;
+            set_time_fields(D.P, D.C, R);
+            D.S.flags[0] = 0;
+            D.S.flags[1] = 0;
+        }
+        if (blockIdx.x == 0) {
+            A.sync->pending[0] = 0;
+            A.sync->pending[1] = 0;
+            A.sync->running = 0;
+        }
+    }
+    if (!grid_barrier(A.sync)) return;
+
+    for (int round = 0; round < A.max_rounds; ++round) {
+        // force pass of the scenes still pending
+        for_each_item(A, kSelForce, L, [&](int, const WorkItem& it) {
+            force_item<kForceLanes, FP64>(A.scenes[it.scene], it);
+        });
+        if (!grid_barrier(A.sync)) return;
+        // decision (owner block of each scene).  Every block has read the
+        // previous round's pending count by now, so its counter can be reset
+        // for the next round.
+        if (threadIdx.x == 0) {
+            if (blockIdx.x == 0) A.sync->pending[(round + 1) & 1] = 0;
+            for (int s = blockIdx.x; s < A.n_scenes; s += gridDim.x) {
+                SceneRun& R = A.run[s];
+                if (!R.active) {
+                    R.restore = 0;
+                    continue;
+                }
+                SceneDesc& D = A.scenes[s];
+                volatile int* flags = D.S.flags;
+                const int has_broken = flags[0];
+                const int nbroken = flags[1];
+                flags[0] = 0;
+                flags[1] = 0;
+                int rollback = 0;
+                if (D.C.adaptive) rollback = adaptive_decide(has_broken, D.C, R);
+                if (rollback) {
+                    R.restore = 1;
+                    R.rollbacks += 1;
+                    if (++R.retries > 64) {
+                        R.error = 1;
+                        R.active = 0;
+                        R.restore = 0;
+                        continue;
+                    }
+                    atomicAdd(&A.sync->pending[round & 1], 1);
+                } else {
+                    R.restore = D.C.adaptive ? 2 : 0;
+                    R.active = 0;
+                    R.solving = 1;
+                    R.broken += nbroken;
+                }
+                set_time_fields(D.P, D.C, R);
+            }
+        }
+        if (!grid_barrier(A.sync)) return;
+        // rollback restore (restoreBondListTopIndex / restorePDPosition /
+        // restorePDVelocity, memory_manager.cu:500-550) or the step's backup
+        for_each_item(A, kSelRestore, L, [&](int, const WorkItem& it) {
+            const int mode = ld_volatile(&A.run[it.scene].restore);
+            const DeviceState& S = A.scenes[it.scene].S;
+            for (int r = it.lo + threadIdx.x; r < it.hi; r += blockDim.x) {
+                if (mode == 1) {
+                    S.cnt[r] = S.cnt_bk[r];
+                    S.x64[r] = S.x64_bk[r];
+                    S.v64[r] = S.v64_bk[r];
+                } else {
+                    S.cnt_bk[r] = S.cnt[r];
+                    S.x64_bk[r] = S.x64[r];
+                    S.v64_bk[r] = S.v64[r];
+                }
+            }
+        });
+        if (!grid_barrier(A.sync)) return;
+        if (ld_volatile(&A.sync->pending[round & 1]) == 0) break;
+    }
+
+    // CG set-up of the solving scenes: b, Dirichlet values, ||b||
+    for_each_item(A, kSelSolving, L, [&](int i, const WorkItem& it) {
+        const SceneDesc& d = A.scenes[it.scene];
+        Acc acc;
+        for (int r = it.lo + threadIdx.x; r < it.hi; r += blockDim.x) cg_init_elem<FP64>(d.P, d.S, r, acc);
+        CgScalars* sc = d.S.sc;
+        item_reduce(acc, A, i, d.C, it.scene, [sc](double bb) { cg_fin_init(sc, bb); });
+    });
+    if (!grid_barrier(A.sync)) return;
+    // y = A x0 (warm start: the previous solution)
+    for_each_item(A, kSelSolving, L, [&](int, const WorkItem& it) {
+        const SceneDesc& d = A.scenes[it.scene];
+        Acc acc;
+        spmv_item<8, FP64, false, 2, kLdCoherent>(d, it, d.S.sol, d.S.y, acc);
+    });
+    if (!grid_barrier(A.sync)) return;
+    // r = b - A x0, p = r, convergence test
+    for_each_item(A, kSelSolving, L, [&](int i, const WorkItem& it) {
+        const SceneDesc& d = A.scenes[it.scene];
+        Acc acc;
+        for (int r = it.lo + threadIdx.x; r < it.hi; r += blockDim.x) residual_elem<FP64>(d.S, r, acc);
+        CgScalars* sc = d.S.sc;
+        BatchSync* sync = A.sync;
+        item_reduce(acc, A, i, d.C, it.scene, [sc, sync](double rr) {
+            cg_fin_residual(sc, rr);
+            if (!sc->done) atomicAdd(&sync->running, 1);
+        });
+    });
+}
+
+// ---- k_batch_cg ----------------------------------------------------------------------
+template <int G, bool FP64, int U>
+__global__ void __launch_bounds__(kBlock) k_batch_cg(BatchArgs A)
+{
+    using Real = typename std::conditional<FP64, double, float>::type;
+    using Acc = typename DotAccFor<Real>::type;
+    __shared__ ItemList L;
+
+    if (A.tune_reps > 0) {
+        // autotuning: the SpMV phase alone (y = A x), no state changes
+        for (int rep = 0; rep < A.tune_reps; ++rep) {
+            for_each_item(A, kSelAll, L, [&](int, const WorkItem& it) {
+                const SceneDesc& d = A.scenes[it.scene];
+                Acc acc;
+                spmv_item<G, FP64, false, U, kLdCoherentIn>(d, it, d.S.sol, d.S.y, acc);
+            });
+            if (!grid_barrier(A.sync)) return;
+        }
+        return;
+    }
+
+    for (int iter = 0; iter < A.max_cg_iters; ++iter) {
+        if (ld_volatile(&A.sync->running) == 0) break;
+        // y = A p, alpha = rz / <p, y>
+        for_each_item(A, kSelRunning, L, [&](int i, const WorkItem& it) {
+            const SceneDesc& d = A.scenes[it.scene];
+            CgScalars* sc = d.S.sc;
+            Acc acc;
+            spmv_item<G, FP64, true, U, kLdCoherentIn>(d, it, d.S.p, d.S.y, acc);
+            item_reduce(acc, A, i, d.C, it.scene, [sc](double pAp) { cg_fin_alpha(sc, pAp); });
+        });
+        if (!grid_barrier(A.sync)) return;
+        // x += alpha p, r -= alpha y, beta, test (a scene is marked done only
+        // after all its items have reported, so the selection stays valid)
+        for_each_item(A, kSelRunning, L, [&](int i, const WorkItem& it) {
+            const SceneDesc& d = A.scenes[it.scene];
+            CgScalars* sc = d.S.sc;
+            const Real alpha = (Real)__ldcg(&sc->alpha);
+            Acc acc;
+            for (int r = it.lo + threadIdx.x; r < it.hi; r += blockDim.x) axpy_elem<FP64>(d.S, r, alpha, acc);
+            BatchSync* sync = A.sync;
+            item_reduce(acc, A, i, d.C, it.scene, [sc, sync](double rr) {
+                cg_fin_axpy(sc, rr);
+                if (sc->done) atomicSub(&sync->running, 1);
+            });
+        });
+        if (!grid_barrier(A.sync)) return;
+        if (ld_volatile(&A.sync->running) == 0) break;
+        // p = r + beta p
+        for_each_item(A, kSelRunning, L, [&](int, const WorkItem& it) {
+            const SceneDesc& d = A.scenes[it.scene];
+            const Real beta = (Real)__ldcg(&d.S.sc->beta);
+            for (int r = it.lo + threadIdx.x; r < it.hi; r += blockDim.x) xpby_elem<FP64>(d.S, r, beta);
+        });
+        if (!grid_barrier(A.sync)) return;
+    }
+    // update of the solved scenes
+    for_each_item(A, kSelSolving, L, [&](int, const WorkItem& it) {
+        const SceneDesc& d = A.scenes[it.scene];
+        for (int r = it.lo + threadIdx.x; r < it.hi; r += blockDim.x) update_elem<FP64>(d.P, d.S, r);
+    });
+    // per-scene bookkeeping (owner block): solve statistics, simulated time.
+    // `solving` stays set until the next step starts: other blocks may still
+    // be reading it in the update phase above.
+    if (threadIdx.x == 0) {
+        for (int s = blockIdx.x; s < A.n_scenes; s += gridDim.x) {
+            SceneRun& R = A.run[s];
+            if (!R.solving) continue;
+            const SceneDesc& D = A.scenes[s];
+            const volatile CgScalars* sc = D.S.sc;
+            R.last_iters = sc->iter;
+            R.total_iters += sc->iter;
+            R.last_res = sc->rnorm;
+            R.last_tol = sc->tol;
+            if (!sc->converged) R.cg_converged = 0;
+            R.sim_time += D.P.h;
+        }
+    }
+}
+
+template <int G, int U>
+cudaError_t cg_launch(bool fp64, const BatchArgs& A, int grid, cudaStream_t st)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kBlock);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (fp64) return cudaLaunchKernelEx(&cfg, k_batch_cg<G, true, 1>, A);
+    return cudaLaunchKernelEx(&cfg, k_batch_cg<G, false, U>, A);
+}
+
+template <int G, int U>
+int cg_blocks(bool fp64)
+{
+    int b = 0;
+    if (fp64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch_cg<G, true, 1>, kBlock, 0);
+    else {
+        cudaFuncSetAttribute(k_batch_cg<G, false, U>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch_cg<G, false, U>, kBlock, 0);
+    }
+    return b;
+}
+
+}  // namespace
+
+cudaError_t launch_batch_pre(bool fp64, const BatchArgs& A, int grid, cudaStream_t st)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kBlock);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (fp64) return cudaLaunchKernelEx(&cfg, k_batch_pre<true>, A);
+    return cudaLaunchKernelEx(&cfg, k_batch_pre<false>, A);
+}
+
+cudaError_t launch_batch_cg(bool fp64, int lanes, int unroll, const BatchArgs& A, int grid, cudaStream_t st)
+{
+    if (lanes == 4) return unroll == 4 ? cg_launch<4, 4>(fp64, A, grid, st) : cg_launch<4, 2>(fp64, A, grid, st);
+    return unroll == 4 ? cg_launch<8, 4>(fp64, A, grid, st) : cg_launch<8, 2>(fp64, A, grid, st);
+}
+
+int batch_pre_blocks_per_sm(bool fp64)
+{
+    int b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fp64 ? (const void*)k_batch_pre<true> : (const void*)k_batch_pre<false>,
+                                                  kBlock, 0);
+    return b;
+}
+
+int batch_cg_blocks_per_sm(bool fp64, int lanes, int unroll)
+{
+    if (lanes == 4) return unroll == 4 ? cg_blocks<4, 4>(fp64) : cg_blocks<4, 2>(fp64);
+    return unroll == 4 ? cg_blocks<8, 4>(fp64) : cg_blocks<8, 2>(fp64);
+}
+
+}  // namespace pdgb

@@ -11,7 +11,11 @@
 
 namespace pdgb {
 
+class Batch;
+
 class Engine {
+    friend class Batch;   // the multi-scene step drives the scenes' device state
+
 public:
     Engine(const pd_sim_params& sim, const pd_run_params& run, const pd_solver_options& opt);
     ~Engine();

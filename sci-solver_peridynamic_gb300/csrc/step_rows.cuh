@@ -1,0 +1,602 @@
+// step_rows.cuh -- per-particle bodies of the step kernels.
+//
+// Each function does one particle's (or one row group's) share of a kernel,
+// so the same arithmetic runs in the one-scene launches of step.cu and in the
+// persistent multi-scene kernels of batch.cu.  Reference formulas and their
+// file:line are cited at each body.
+#pragma once
+
+#include <type_traits>
+
+#include "pd_device.cuh"
+#include "pd_kernels.h"
+
+namespace pdgb {
+
+// ---- FP64 operations the compiler must not contract ---------------------------
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ double dsqrt(double a) { return __dsqrt_rn(a); }
+
+// Bond geometry exactly as calculatePDForceDerivative evaluates it
+// (cg_solver.cuh:254-260): eij = x_q - x_p, dij = sqrt(x*x + y*y + z*z),
+// d0 = length(X_p - X_q), drdivd = dij / d0 - 1.
+struct BondEval {
+    double ex, ey, ez, dij, d0, s;
+};
+
+__device__ __forceinline__ BondEval eval_bond(const dbl4& xp, const dbl4& Xp, const dbl4& xq,
+                                              const dbl4& Xq)
+{
+    BondEval b;
+    b.ex = dsub(xq.x, xp.x);
+    b.ey = dsub(xq.y, xp.y);
+    b.ez = dsub(xq.z, xp.z);
+    b.dij = dsqrt(dadd(dadd(dmul(b.ex, b.ex), dmul(b.ey, b.ey)), dmul(b.ez, b.ez)));
+    const double ox = dsub(Xp.x, Xq.x), oy = dsub(Xp.y, Xq.y), oz = dsub(Xp.z, Xq.z);
+    b.d0 = dsqrt(dadd(dadd(dmul(ox, ox), dmul(oy, oy)), dmul(oz, oz)));
+    b.s = dsub(ddiv(b.dij, b.d0), 1.0);
+    return b;
+}
+
+// Position as an FP32 offset inside its supercell plus the supercell's integer
+// coordinates (10 bits each) in the w lane.  A bond vector is then
+// (off_q - off_p) + sup * (ijk_q - ijk_p): the offsets are small, so the FP32
+// bond vector keeps ~2^-23 * sup / |xi| relative accuracy wherever the body is.
+__device__ __forceinline__ float4 encode_supercell(const StepParams& P, const dbl4& x)
+{
+    const double v[3] = {x.x - P.sup_lo[0], x.y - P.sup_lo[1], x.z - P.sup_lo[2]};
+    int c[3];
+    float o[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        int ck = (int)floor(v[k] * P.inv_sup);
+        ck = ck < 0 ? 0 : (ck > 1023 ? 1023 : ck);
+        c[k] = ck;
+        o[k] = (float)(v[k] - P.sup * (double)ck);
+    }
+    return make_float4(o[0], o[1], o[2], __int_as_float(c[0] | (c[1] << 10) | (c[2] << 20)));
+}
+
+__device__ __forceinline__ void supercell_delta(int wq, int wp, float sup, float& dx, float& dy, float& dz)
+{
+    dx = sup * (float)((wq & 1023) - (wp & 1023));
+    dy = sup * (float)(((wq >> 10) & 1023) - ((wp >> 10) & 1023));
+    dz = sup * (float)(((wq >> 20) & 1023) - ((wp >> 20) & 1023));
+}
+
+// fmaxf(stretch_p, stretch_q) of cg_solver.cuh:264: both limits rounded to float.
+__device__ __forceinline__ double break_threshold(float thp, double stq)
+{
+    const float thq = (float)stq;
+    return (double)(thp > thq ? thp : thq);
+}
+
+// ---- force / breakage ----------------------------------------------------------
+// Force pass of particle p by its G-lane group: stretch test and breakage,
+// bond force, new stretch limit, gravity and contact; FP64 mode also stores the
+// bond Jacobians and their diagonal sum.
+template <int G, bool FP64>
+__device__ __forceinline__ void force_row(const StepParams& P, const DeviceState& S, int p, int lane,
+                                          unsigned gmask)
+{
+    using Real = typename std::conditional<FP64, double, float>::type;
+    using V4 = typename Vec4<Real>::type;
+    V4* force = (V4*)S.force;
+    const int a = S.act[p] & kActMask;
+    const dbl4 xp = S.x64[p];
+    const dbl4 Xp = S.X64[p];
+    // FP32 displacement of this step's linear system (read by k_spmv)
+    if (!FP64 && lane == 0) {
+        S.u32[p] = make_float4((float)(xp.x - Xp.x), (float)(xp.y - Xp.y), (float)(xp.z - Xp.z), 0.f);
+        S.xs4[p] = encode_supercell(P, xp);
+    }
+    if (a == ACT_INVISIBLE) return;
+    const float thp = (float)S.st[p];
+    const int rs = S.row_ptr[p];
+    const int c = S.cnt[p];
+    Real fx = 0, fy = 0, fz = 0;
+    double j0 = 0, j1 = 0, j2 = 0, j3 = 0, j4 = 0, j5 = 0;   // FP64: diagonal block sum
+    double smin = 0.0;
+    int nb = 0;
+    for (int j = lane; j < c; j += G) {
+        const int q = S.col[rs + j];
+        const dbl4 xq = S.x64[q];
+        const dbl4 Xq = S.X64[q];
+        const BondEval b = eval_bond(xp, Xp, xq, Xq);
+        if (b.s > break_threshold(thp, S.st[q])) {
+            ++nb;
+            continue;
+        }
+        smin = b.s < smin ? b.s : smin;
+        if (FP64) {
+            // reference formulas: eij /= fmaxf(dij, SMALL) (float-rounded), vscale,
+            // J = (c/d0) [ (1 - d0/dij) I + (d0/dij) e e^T ]   (cg_solver.cuh:256-303)
+            const double D = (double)fmaxf((float)b.dij, (float)1e-10);
+            const double ex = ddiv(b.ex, D), ey = ddiv(b.ey, D), ez = ddiv(b.ez, D);
+            double vscale = 1.0;
+            if (b.d0 > P.vs_threshold) vscale = dadd(0.5, ddiv(ddiv(dsub(P.horizon, b.d0), 2.0), P.radius));
+            const double kk = dmul(b.s, vscale);
+            fx = dadd(fx, dmul(kk, ex));
+            fy = dadd(fy, dmul(kk, ey));
+            fz = dadd(fz, dmul(kk, ez));
+            const double r = ddiv(b.d0, b.dij);
+            const double dg = dsub(1.0, r);
+            const double cc = ddiv(P.bond_coeff, b.d0);
+            const double jxx = dmul(dadd(dg, dmul(dmul(ex, ex), r)), cc);
+            const double jyy = dmul(dadd(dg, dmul(dmul(ey, ey), r)), cc);
+            const double jzz = dmul(dadd(dg, dmul(dmul(ez, ez), r)), cc);
+            const double jxy = dmul(dmul(dmul(ex, ey), r), cc);
+            const double jxz = dmul(dmul(dmul(ex, ez), r), cc);
+            const double jyz = dmul(dmul(dmul(ey, ez), r), cc);
+            double* J = S.jac + 6ll * (rs + j);
+            J[0] = jxx; J[1] = jyy; J[2] = jzz; J[3] = jxy; J[4] = jxz; J[5] = jyz;
+            j0 += jxx; j1 += jyy; j2 += jzz; j3 += jxy; j4 += jxz; j5 += jyz;
+        } else {
+            const float inv = 1.0f / (float)b.dij;
+            const float d0f = (float)b.d0;
+            float vs = 1.0f;
+            if (b.d0 > P.vs_threshold) vs = 0.5f + ((float)P.horizon - d0f) * 0.5f / (float)P.radius;
+            const float kk = (float)b.s * vs * inv;
+            fx = fmaf(kk, (float)b.ex, (float)fx);
+            fy = fmaf(kk, (float)b.ey, (float)fy);
+            fz = fmaf(kk, (float)b.ez, (float)fz);
+        }
+    }
+    fx = group_sum<G>(fx, gmask);
+    fy = group_sum<G>(fy, gmask);
+    fz = group_sum<G>(fz, gmask);
+    smin = group_min<G>(smin, gmask);
+    nb = group_sum<G>(nb, gmask);
+    if (FP64) {
+        j0 = group_sum<G>(j0, gmask); j1 = group_sum<G>(j1, gmask); j2 = group_sum<G>(j2, gmask);
+        j3 = group_sum<G>(j3, gmask); j4 = group_sum<G>(j4, gmask); j5 = group_sum<G>(j5, gmask);
+    }
+    if (nb > 0) {
+        // Rare path: partition the row as the reference does (swap the broken
+        // bond with the last live one and retest the swapped-in bond,
+        // cg_solver.cuh:264-275), so live bonds occupy the first cnt slots.
+        int top = c - 1;
+        if (lane == 0) {
+            int bond = 0;
+            while (bond <= top) {
+                const int q = S.col[rs + bond];
+                const BondEval b = eval_bond(xp, Xp, S.x64[q], S.X64[q]);
+                if (b.s > break_threshold(thp, S.st[q])) {
+                    S.col[rs + bond] = S.col[rs + top];
+                    S.col[rs + top] = q;
+                    if (!FP64) {
+                        const float t = S.inv_d0[rs + bond];
+                        S.inv_d0[rs + bond] = S.inv_d0[rs + top];
+                        S.inv_d0[rs + top] = t;
+                    }
+                    --top;
+                    continue;
+                }
+                ++bond;
+            }
+            S.cnt[p] = top + 1;
+            S.flags[0] = 1;
+            atomicAdd(&S.flags[1], nb);
+        }
+        __syncwarp(gmask);
+        if (FP64) {
+            // bond slots moved: store each live bond's Jacobian at its new slot
+            top = __shfl_sync(gmask, top, 0, G);
+            for (int j = lane; j <= top; j += G) {
+                const int q = S.col[rs + j];
+                const BondEval b = eval_bond(xp, Xp, S.x64[q], S.X64[q]);
+                const double D = (double)fmaxf((float)b.dij, (float)1e-10);
+                const double ex = ddiv(b.ex, D), ey = ddiv(b.ey, D), ez = ddiv(b.ez, D);
+                const double r = ddiv(b.d0, b.dij);
+                const double dg = dsub(1.0, r);
+                const double cc = ddiv(P.bond_coeff, b.d0);
+                double* J = S.jac + 6ll * (rs + j);
+                J[0] = dmul(dadd(dg, dmul(dmul(ex, ex), r)), cc);
+                J[1] = dmul(dadd(dg, dmul(dmul(ey, ey), r)), cc);
+                J[2] = dmul(dadd(dg, dmul(dmul(ez, ez), r)), cc);
+                J[3] = dmul(dmul(dmul(ex, ey), r), cc);
+                J[4] = dmul(dmul(dmul(ex, ez), r), cc);
+                J[5] = dmul(dmul(dmul(ey, ez), r), cc);
+            }
+        }
+    }
+    if (lane == 0) {
+        // force *= C*V*PD_K; new stretch limit; gravity (cg_solver.cuh:325-331)
+        double f0 = (double)fx * P.bond_coeff, f1 = (double)fy * P.bond_coeff, f2 = (double)fz * P.bond_coeff;
+        if (FP64) {
+            f0 = dmul((double)fx, P.bond_coeff);
+            f1 = dmul((double)fy, P.bond_coeff);
+            f2 = dmul((double)fz, P.bond_coeff);
+        }
+        const double ss0 = dmul(dsub(P.stretch_a, dmul(P.stretch_b, P.cs)), S.ost[p]);
+        S.nst[p] = dsub(ss0, dmul(P.alpha, smin));
+        if (P.gravity[0] != 0.0) f0 = dsub(f0, dmul(dmul(P.cs, -P.gravity[0]), P.mass));
+        if (P.gravity[1] != 0.0) f1 = dsub(f1, dmul(dmul(P.cs, -P.gravity[1]), P.mass));
+        if (P.gravity[2] != 0.0) f2 = dsub(f2, dmul(dmul(P.cs, -P.gravity[2]), P.mass));
+        // rigid-sphere penalty contact at the start-of-step position (extension)
+        uint8_t actb = (uint8_t)a;
+        if (P.sphere_on) {
+            const double dx = xp.x - P.sphere_c[0], dy = xp.y - P.sphere_c[1], dz = xp.z - P.sphere_c[2];
+            const double d = sqrt(dx * dx + dy * dy + dz * dz);
+            const double pen = (P.sphere_r + P.radius) - d;
+            if (pen > 0.0 && d > 0.0) {
+                const double nx = dx / d, ny = dy / d, nz = dz / d;
+                f0 += P.sphere_k * pen * nx;
+                f1 += P.sphere_k * pen * ny;
+                f2 += P.sphere_k * pen * nz;
+                actb |= kActContact;
+                if (FP64) {
+                    j0 += P.sphere_k * nx * nx; j1 += P.sphere_k * ny * ny; j2 += P.sphere_k * nz * nz;
+                    j3 += P.sphere_k * nx * ny; j4 += P.sphere_k * nx * nz; j5 += P.sphere_k * ny * nz;
+                }
+            }
+        }
+        S.act[p] = actb;
+        force[p] = make_v4<V4>(f0, f1, f2);
+        if (FP64) {
+            double* D = S.jdiag + 6ll * p;
+            D[0] = j0; D[1] = j1; D[2] = j2; D[3] = j3; D[4] = j4; D[5] = j5;
+        }
+    }
+}
+
+// ---- A w -------------------------------------------------------------------------
+// Load paths of the SpMV gathers.  The read-only (non-coherent) path may only
+// read data that no thread writes during the kernel: a persistent kernel that
+// rewrites the CG vector or the positions between its phases (separated by a
+// gpu-scope acquire) reads them with ordinary cached loads (ld.global.ca).
+enum : int { kLdCoherent = 0, kLdCoherentIn = 1, kLdReadOnly = 2 };
+
+template <int LD, typename T>
+__device__ __forceinline__ T ld_pos(const T* p)
+{
+    if (LD == kLdCoherent) return __ldca(p);
+    return __ldg(p);
+}
+template <int LD, typename T>
+__device__ __forceinline__ T ld_in(const T* p)
+{
+    if (LD == kLdReadOnly) return __ldg(p);
+    return __ldca(p);
+}
+template <int LD>
+__device__ __forceinline__ dbl4 ld_in(const dbl4* p)
+{
+    const double2* q = (const double2*)p;
+    const double2 a = LD == kLdReadOnly ? __ldg(q) : __ldca(q);
+    const double2 b = LD == kLdReadOnly ? __ldg(q + 1) : __ldca(q + 1);
+    return make_dbl4(a.x, a.y, b.x, b.y);
+}
+
+// y_p = (A w)_p by particle p's G-lane group: mass + (beta h^2) stiffness with
+// Dirichlet rows projected out.  DOT: lane 0 adds w_p . y_p to acc.
+// LD: load path of the positions and of w (kLd*).
+template <int G, bool FP64, bool DOT, int U, int LD, typename V4, typename Acc>
+__device__ __forceinline__ void spmv_row(const StepParams& P, const DeviceState& S, const V4* __restrict__ in,
+                                         V4* __restrict__ out, int p, int lane, unsigned gmask, Acc& acc)
+{
+    using Real = typename std::conditional<FP64, double, float>::type;
+    const Real c = (Real)P.bond_coeff;
+    const Real t2 = (Real)P.t2;
+    const Real m = (Real)P.mass;
+    const uint8_t ab = S.act[p];
+    if (is_dirichlet(ab & kActMask)) {
+        if (lane == 0) out[p] = make_v4<V4>(0.0, 0.0, 0.0);
+        return;
+    }
+    const V4 w = ld_in<LD>(in + p);
+    const int rs = S.row_ptr[p];
+    const int cn = S.cnt[p];
+    Real ax = 0, ay = 0, az = 0;
+    if (FP64) {
+        for (int j = lane; j < cn; j += G) {
+            const int q = S.col[rs + j];
+            const V4 wq = ld_in<LD>(in + q);
+            const double* J = S.jac + 6ll * (rs + j);
+            ax += J[0] * wq.x + J[3] * wq.y + J[4] * wq.z;
+            ay += J[3] * wq.x + J[1] * wq.y + J[5] * wq.z;
+            az += J[4] * wq.x + J[5] * wq.y + J[2] * wq.z;
+        }
+    } else {
+        // per bond: the column index and 1/d0 stream in coalesced; the
+        // neighbour's supercell position and its CG entry are gathered
+        const float4 xp4 = ld_pos<LD>(S.xs4 + p);
+        const int wp = __float_as_int(xp4.w);
+        const float sup = (float)P.sup;
+        const float4* __restrict__ xs4 = S.xs4;
+        const float4* __restrict__ in32 = (const float4*)in;
+        for (int j0 = lane; j0 < cn; j0 += G * U) {
+            // issue every load of U bonds before any arithmetic
+            int qq[U];
+            float id0[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int j = j0 + u * G;
+                qq[u] = j < cn ? __ldcs(S.col + rs + j) : -1;
+                id0[u] = j < cn ? __ldcs(S.inv_d0 + rs + j) : 0.f;
+            }
+            float4 Xq[U], Wq[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int q = qq[u] < 0 ? p : qq[u];
+                Xq[u] = ld_pos<LD>(xs4 + q);
+                Wq[u] = ld_in<LD>(in32 + q);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (qq[u] < 0) continue;
+                float cx, cy, cz;
+                supercell_delta(__float_as_int(Xq[u].w), wp, sup, cx, cy, cz);
+                const float xs = (Xq[u].x - xp4.x) + cx, ys = (Xq[u].y - xp4.y) + cy, zs = (Xq[u].z - xp4.z) + cz;
+                const float inv_d0 = id0[u];
+                const float inv_d = rsqrtf(fmaf(xs, xs, fmaf(ys, ys, zs * zs)));
+                const float wx = (float)w.x - Wq[u].x, wy = (float)w.y - Wq[u].y, wz = (float)w.z - Wq[u].z;
+                const float a1 = inv_d0 - inv_d;
+                const float g = fmaf(xs, wx, fmaf(ys, wy, zs * wz)) * (inv_d * inv_d * inv_d);
+                ax = fmaf(a1, wx, fmaf(g, xs, (float)ax));
+                ay = fmaf(a1, wy, fmaf(g, ys, (float)ay));
+                az = fmaf(a1, wz, fmaf(g, zs, (float)az));
+            }
+        }
+    }
+    ax = group_sum<G>(ax, gmask);
+    ay = group_sum<G>(ay, gmask);
+    az = group_sum<G>(az, gmask);
+    if (lane == 0) {
+        Real kx, ky, kz;
+        if (FP64) {
+            const double* D = S.jdiag + 6ll * p;
+            kx = D[0] * w.x + D[3] * w.y + D[4] * w.z - ax;
+            ky = D[3] * w.x + D[1] * w.y + D[5] * w.z - ay;
+            kz = D[4] * w.x + D[5] * w.y + D[2] * w.z - az;
+        } else {
+            kx = c * ax; ky = c * ay; kz = c * az;
+            if (ab & kActContact) {
+                const float4 Xp = S.X32[p];
+                const float4 Up = S.u32[p];
+                const float dx = Xp.x + Up.x - (float)P.sphere_c_local[0];
+                const float dy = Xp.y + Up.y - (float)P.sphere_c_local[1];
+                const float dz = Xp.z + Up.z - (float)P.sphere_c_local[2];
+                const float inv = rsqrtf(dx * dx + dy * dy + dz * dz);
+                const float nx = dx * inv, ny = dy * inv, nz = dz * inv;
+                const float kn = (float)P.sphere_k * (nx * (float)w.x + ny * (float)w.y + nz * (float)w.z);
+                kx += kn * nx; ky += kn * ny; kz += kn * nz;
+            }
+        }
+        const Real yx = m * (Real)w.x + t2 * kx;
+        const Real yy = m * (Real)w.y + t2 * ky;
+        const Real yz = m * (Real)w.z + t2 * kz;
+        V4 yv;
+        yv.x = yx; yv.y = yy; yv.z = yz; yv.w = 0;
+        out[p] = yv;
+        if (DOT) {
+            acc.fma(w.x, yx);
+            acc.fma(w.y, yy);
+            acc.fma(w.z, yz);
+        }
+    }
+}
+
+// ---- CG vector bodies (CUSP krylov::cg, identity preconditioner) -----------------
+// Right-hand side with this step's final time step (the adaptive scheme may
+// have changed it after the force pass, simulator.cu:540-572, before
+// fillVectorB*): b = m v + h f (implicit_euler.cuh:83-84) or
+// b = h (m v + (h/2) f) (newmark_beta.cuh:264-265).
+// Dirichlet values: clamped and invisible particles 0, prescribed particles their
+// velocity (implicit Euler) or h * velocity (Newmark); ||b|| over free rows.
+template <bool FP64, typename Acc>
+__device__ __forceinline__ void cg_init_elem(const StepParams& P, const DeviceState& S, int i, Acc& acc)
+{
+    using Real = typename std::conditional<FP64, double, float>::type;
+    using V4 = typename Vec4<Real>::type;
+    V4* x = (V4*)S.sol;
+    V4* b = (V4*)S.rhs;
+    const V4* force = (const V4*)S.force;
+    const int a = S.act[i] & kActMask;
+    const dbl4 v = S.v64[i];
+    const V4 f = force[i];
+    double b0, b1, b2;
+    if (P.integrator == 0) {
+        b0 = dadd(dmul(P.mass, v.x), dmul(P.h, (double)f.x));
+        b1 = dadd(dmul(P.mass, v.y), dmul(P.h, (double)f.y));
+        b2 = dadd(dmul(P.mass, v.z), dmul(P.h, (double)f.z));
+    } else {
+        const double hh = dmul(0.5, P.h);
+        b0 = dmul(P.h, dadd(dmul(P.mass, v.x), dmul(hh, (double)f.x)));
+        b1 = dmul(P.h, dadd(dmul(P.mass, v.y), dmul(hh, (double)f.y)));
+        b2 = dmul(P.h, dadd(dmul(P.mass, v.z), dmul(hh, (double)f.z)));
+    }
+    const V4 bv = make_v4<V4>(b0, b1, b2);
+    b[i] = bv;
+    if (is_dirichlet(a)) {
+        double ux = 0, uy = 0, uz = 0;
+        if (a == ACT_PRESCRIBED) {
+            const double s = P.integrator == 0 ? 1.0 : P.h;
+            ux = v.x * s; uy = v.y * s; uz = v.z * s;
+        }
+        x[i] = make_v4<V4>(ux, uy, uz);
+    } else {
+        acc.fma(bv.x, bv.x);
+        acc.fma(bv.y, bv.y);
+        acc.fma(bv.z, bv.z);
+    }
+}
+
+// r = b - A x0 on free rows (y holds A x0), p = r
+template <bool FP64, typename Acc>
+__device__ __forceinline__ void residual_elem(const DeviceState& S, int i, Acc& acc)
+{
+    using Real = typename std::conditional<FP64, double, float>::type;
+    using V4 = typename Vec4<Real>::type;
+    const V4* b = (const V4*)S.rhs;
+    const V4* y = (const V4*)S.y;
+    V4 rv;
+    if (is_dirichlet(S.act[i] & kActMask)) {
+        rv.x = 0; rv.y = 0; rv.z = 0; rv.w = 0;
+    } else {
+        const V4 bv = b[i], yv = y[i];
+        rv.x = bv.x - yv.x; rv.y = bv.y - yv.y; rv.z = bv.z - yv.z; rv.w = 0;
+        acc.fma(rv.x, rv.x);
+        acc.fma(rv.y, rv.y);
+        acc.fma(rv.z, rv.z);
+    }
+    ((V4*)S.r)[i] = rv;
+    ((V4*)S.p)[i] = rv;
+}
+
+// x += alpha p ; r -= alpha A p ; acc += <r, r>
+template <bool FP64, typename Real, typename Acc>
+__device__ __forceinline__ void axpy_elem(const DeviceState& S, int i, Real alpha, Acc& acc)
+{
+    using V4 = typename Vec4<Real>::type;
+    V4* x = (V4*)S.sol;
+    V4* r = (V4*)S.r;
+    const V4 pi = ((const V4*)S.p)[i], yi = ((const V4*)S.y)[i];
+    V4 xi = x[i], ri = r[i];
+    xi.x += alpha * pi.x; xi.y += alpha * pi.y; xi.z += alpha * pi.z;
+    ri.x -= alpha * yi.x; ri.y -= alpha * yi.y; ri.z -= alpha * yi.z;
+    x[i] = xi;
+    r[i] = ri;
+    acc.fma(ri.x, ri.x);
+    acc.fma(ri.y, ri.y);
+    acc.fma(ri.z, ri.z);
+}
+
+// p = r + beta p
+template <bool FP64, typename Real>
+__device__ __forceinline__ void xpby_elem(const DeviceState& S, int i, Real beta)
+{
+    using V4 = typename Vec4<Real>::type;
+    V4* pv = (V4*)S.p;
+    const V4 ri = ((const V4*)S.r)[i];
+    V4 pi = pv[i];
+    pi.x = ri.x + beta * pi.x;
+    pi.y = ri.y + beta * pi.y;
+    pi.z = ri.z + beta * pi.z;
+    pv[i] = pi;
+}
+
+// Scalar updates of the CG state, run once per reduction by its finisher.
+__device__ __forceinline__ void cg_fin_init(CgScalars* sc, double bb)
+{
+    sc->bnorm2 = bb;
+    sc->tol = 0.0 + sc->rel_tol * sqrt(bb);
+    sc->iter = 0;
+    sc->done = 0;
+    sc->converged = 0;
+}
+
+// rz = <r,r>; convergence test before the first iteration
+__device__ __forceinline__ void cg_fin_residual(CgScalars* sc, double rr)
+{
+    sc->rz = rr;
+    sc->rnorm = sqrt(rr);
+    if (sc->rnorm <= sc->tol) {
+        sc->done = 1;
+        sc->converged = 1;
+    } else if (sc->iter >= sc->max_iter) {
+        sc->done = 1;
+    }
+}
+
+__device__ __forceinline__ void cg_fin_alpha(CgScalars* sc, double pAp)
+{
+    sc->pAp = pAp;
+    sc->alpha = sc->rz / pAp;
+}
+
+// rz' = <r,r> ; beta = rz'/rz ; iteration count and test
+__device__ __forceinline__ void cg_fin_axpy(CgScalars* sc, double rr)
+{
+    const double rz_old = sc->rz;
+    sc->rz = rr;
+    sc->beta = rr / rz_old;
+    sc->iter += 1;
+    sc->rnorm = sqrt(rr);
+    if (sc->rnorm <= sc->tol) {
+        sc->done = 1;
+        sc->converged = 1;
+    } else if (sc->iter >= sc->max_iter) {
+        sc->done = 1;
+    }
+}
+
+// ---- position / velocity update ------------------------------------------------
+// box reflection of updatePDPosition* (implicit_euler.cuh:116-168), FP64, same order
+__device__ __forceinline__ void reflect(const StepParams& P, double& np, double& nv, int k)
+{
+    const double mn = dadd(P.bmin[k], P.radius);
+    const double mx = dsub(P.bmax[k], P.radius);
+    if (np > mx) {
+        nv = dmul(nv, -P.restitution);
+        np = dsub(mx, dmul(P.restitution, dsub(np, mx)));
+    }
+    if (np < mn) {
+        nv = dmul(nv, -P.restitution);
+        np = dadd(mn, dmul(P.restitution, dsub(mn, np)));
+    }
+}
+
+template <bool FP64>
+__device__ __forceinline__ void update_elem(const StepParams& P, const DeviceState& S, int i)
+{
+    using Real = typename std::conditional<FP64, double, float>::type;
+    using V4 = typename Vec4<Real>::type;
+    const V4* sol = (const V4*)S.sol;
+    S.st[i] = S.nst[i];   // updatePDStretchNeighborList (simulator.cuh:2601-2620)
+    const int a = S.act[i] & kActMask;
+    const dbl4 x = S.x64[i];
+    dbl4 v = S.v64[i];
+    if (a == ACT_INVISIBLE) {
+        if (P.integrator == 0) S.v64[i] = make_dbl4(0.0, 0.0, 0.0, 0.0);
+        return;
+    }
+    double nv[3], np[3];
+    const double xs[3] = {x.x, x.y, x.z};
+    const double vs[3] = {v.x, v.y, v.z};
+    if (P.integrator == 0) {
+        // transferData(PD_VELOCITY <- PD_SYSTEM_SOLUTION); x += v * base * ticks
+        if (a == ACT_PRESCRIBED) {
+            nv[0] = vs[0]; nv[1] = vs[1]; nv[2] = vs[2];
+        } else if (a == ACT_CLAMPED) {
+            nv[0] = nv[1] = nv[2] = 0.0;
+        } else {
+            const V4 s = sol[i];
+            nv[0] = (double)s.x; nv[1] = (double)s.y; nv[2] = (double)s.z;
+        }
+        for (int k = 0; k < 3; ++k) np[k] = dadd(xs[k], dmul(dmul(nv[k], P.dt_base), (double)P.ticks));
+    } else {
+        // v = 2/h dx - v ; x += dx
+        double dx[3];
+        if (a == ACT_PRESCRIBED) {
+            for (int k = 0; k < 3; ++k) { dx[k] = dmul(P.h, vs[k]); nv[k] = vs[k]; }
+        } else if (a == ACT_CLAMPED) {
+            for (int k = 0; k < 3; ++k) { dx[k] = 0.0; nv[k] = 0.0; }
+        } else {
+            const V4 s = sol[i];
+            dx[0] = (double)s.x; dx[1] = (double)s.y; dx[2] = (double)s.z;
+            const double two_h = ddiv(2.0, P.h);
+            for (int k = 0; k < 3; ++k) nv[k] = dsub(dmul(two_h, dx[k]), vs[k]);
+        }
+        for (int k = 0; k < 3; ++k) np[k] = dadd(xs[k], dx[k]);
+    }
+    if (P.box_enabled)
+        for (int k = 0; k < 3; ++k) reflect(P, np[k], nv[k], k);
+    S.x64[i] = make_dbl4(np[0], np[1], np[2], 0.0);
+    S.v64[i] = make_dbl4(nv[0], nv[1], nv[2], 0.0);
+}
+
+// FP32 displacement and supercell position from the FP64 master positions
+// (after a rollback restore); the contact bit is cleared
+__device__ __forceinline__ void refresh_elem(const StepParams& P, const DeviceState& S, int i)
+{
+    const dbl4 x = S.x64[i], X = S.X64[i];
+    S.u32[i] = make_float4((float)(x.x - X.x), (float)(x.y - X.y), (float)(x.z - X.z), 0.f);
+    if (S.xs4) S.xs4[i] = encode_supercell(P, x);
+    S.act[i] &= kActMask;
+}
+
+}  // namespace pdgb

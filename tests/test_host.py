@@ -125,6 +125,23 @@ def test_no_gpu_fails_loudly(pdgb, scenes):
     with pytest.raises(pdgb.PdError) as e:
         scenes.make_simulator(sc)
     assert e.value.status == 5
+    with pytest.raises(pdgb.PdError) as e:
+        pdgb.Batch(0)
+    assert e.value.status == 5
+
+
+def test_batch_scene_sizes():
+    """The batched workload: 64 bodies, log-uniform sizes in [4096, 65536]
+    (about 1.4M particles), horizons 4/5/6, impact speeds 1-10 m/s."""
+    import importlib
+    scenes = importlib.import_module("sci-solver_peridynamic_gb300.scenes")
+    lst = scenes.batched_scenes()
+    ns = np.array([sc.n for sc in lst])
+    assert len(lst) == 64 and 1.2e6 < ns.sum() < 1.6e6
+    assert ns.min() >= 0.9 * 4096 and ns.max() <= 1.1 * 65536
+    assert {sc.info["coeff"] for sc in lst} == {4.0, 5.0, 6.0}
+    assert {sc.info["shape"] for sc in lst} == {"block", "ball"}
+    assert all(1.0 <= sc.info["speed"] <= 10.0 for sc in lst)
 
 
 def test_solver_option_defaults(pdgb):
