@@ -54,6 +54,7 @@ def parse_args(argv=None):
     ap.add_argument("--n", type=int, default=TARGET_N, help="target particle count")
     ap.add_argument("--lanes", type=int, default=0, help="lanes per particle row (0 = automatic)")
     ap.add_argument("--unroll", type=int, default=0, help="SpMV gather unroll 1/2/4 (0 = automatic)")
+    ap.add_argument("--spmv-path", type=int, default=0, help="1 shared-memory tiles, 2 per-bond gathers, 0 automatic")
     ap.add_argument("--workload", choices=("ellipsoid", "batched", "learned", "beam"), default="ellipsoid",
                     help="ellipsoid: the 1M-particle headline; batched: 64 scenes in one batch; learned: "
                          "learned vs plain CG warm start on the 16^3 cube; beam: FP32 vs FP64 notched beam")
@@ -223,6 +224,7 @@ def run_gb300(args):
         sc.opt.lanes_per_particle = args.lanes
     if args.unroll:
         sc.opt.spmv_unroll = args.unroll
+    sc.opt.spmv_path = args.spmv_path
     sim = scenes.make_simulator(sc, device=local)
     sim.makeReady()
     sim.advance(args.warmup)
@@ -288,9 +290,10 @@ def run_gb300(args):
             "particles": n,
             "bonds_alive": int(bonds),
             "cg_iterations_per_step": round(iters / args.steps, 2),
-            "spmv_variant": "%d lanes x %d unroll (%s)" % (sim.params()[2].lanes_per_particle,
-                                                            sim.params()[2].spmv_unroll,
-                                                            "fixed" if args.lanes and args.unroll else "autotuned"),
+            "spmv_variant": "%s, %d lanes x %d unroll (%s)" % (
+                "shared-memory tiles" if sim.params()[2].spmv_path == 1 else "per-bond gathers",
+                sim.params()[2].lanes_per_particle, sim.params()[2].spmv_unroll,
+                "fixed" if args.lanes and args.unroll and args.spmv_path else "autotuned"),
             "parallelism": "replicas x%d" % world,
             "l2": "inputs larger than L2 (bond columns + 1/d0 %.0f MB + particle state > 129 MB L2)" % (8 * bonds / 1e6),
         },

@@ -134,6 +134,11 @@ typedef struct pd_solver_options {
      * plus the learned correction of pd_ws_set_params' network (mixed
      * precision only; the CG still runs to the same tolerance) */
     int warm_start;
+    /* mixed-precision SpMV path: 0 or 2 = per-bond gathers from global
+     * memory; 1 = shared-memory tiles of 256 consecutive rows and their halos
+     * (measured slower than the gathers at 1M particles; kept as an option).
+     * Either way lanes x unroll is measured at make_ready when n >= 20000. */
+    int spmv_path;
 } pd_solver_options;
 
 /* Export selectors for pd_get. */

@@ -355,6 +355,11 @@ cudaError_t exclusive_scan(const unsigned* in, unsigned* out, long long n, cudaS
 
 }  // namespace
 
+cudaError_t scan_exclusive_u32(const unsigned* in, unsigned* out, long long n, cudaStream_t st)
+{
+    return exclusive_scan(in, out, n, st);
+}
+
 void gather_double4(const dbl4* in, const int* perm, dbl4* out, int n, cudaStream_t st)
 {
     if (n > 0) k_gather_d4<<<grid_for(n), kBlock, 0, st>>>(in, perm, out, n);

@@ -134,9 +134,10 @@ void Engine::free_all()
     ws_free();
     void* ptrs[] = {S_.act, S_.x64, S_.v64, S_.X64, S_.x64_bk, S_.v64_bk, S_.st, S_.ost, S_.nst, S_.row_ptr,
                     S_.cnt, S_.cnt_bk, S_.col, S_.X32, S_.u32, S_.xs4, S_.inv_d0, S_.jac, S_.jdiag, S_.force, S_.rhs, S_.sol,
-                    S_.r, S_.p, S_.y, S_.sc, S_.partials, S_.counters, S_.flags, d_perm_};
+                    S_.r, S_.p, S_.y, S_.sc, S_.partials, S_.counters, S_.flags, S_.lidx, d_perm_};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    free_tiles(S_);
     S_ = DeviceState{};
     d_perm_ = nullptr;
 }
@@ -263,6 +264,17 @@ pd_status Engine::make_ready()
         const double h = sim_.pd_horizon > 0 ? sim_.pd_horizon : 1.0;
         sup_ = std::ldexp(1.0, (int)std::ceil(std::log2(h)));
         for (int k = 0; k < 3; ++k) sup_lo_[k] = origin_[k] - 512.0 * sup_;
+        // tiles of consecutive rows and their halos (shared-memory SpMV),
+        // built when that path is asked for: measured at 1M particles it is
+        // slower than the per-bond gathers (307 vs 283 us per product)
+        if (n > 0 && opt_.spmv_path == 1) {
+            CK(dalloc(&S_.lidx, slots), "alloc local indices");
+            S_.tile_rows = kTileRows;
+            int max_halo = 0;
+            CK(build_tiles(S_, n, &max_halo, stream_), "build tiles");
+            launches_ += 2;
+            S_.halo_cap = std::min(max_halo, kMaxHaloCap);
+        }
     }
     // CG scalars (initPDSolutions zeroed the solution, cg_solver.cuh:184-194)
     std::memset(h_sc_, 0, sizeof(CgScalars));
@@ -318,27 +330,51 @@ int Engine::grid_for_rows(int lanes, int blocks_per_sm) const
 // keeps the fastest.  Fixed choices in the options are respected.
 pd_status Engine::tune_spmv()
 {
-    std::vector<std::pair<int, int>> cand;
+    struct Cand {
+        int tiled, g, u;
+    };
+    std::vector<Cand> cand;
     const int fixed_lanes = opt_.lanes_per_particle;
     const int fixed_unroll = opt_.spmv_unroll;
-    for (int g : {4, 8, 16}) {
-        if (fixed_lanes && g != fixed_lanes) continue;
-        for (int u : {1, 2, 4}) {
-            if (fp64_ && u != 1) continue;
-            if (fixed_unroll && u != fixed_unroll) continue;
-            cand.push_back({g, u});
+    const bool can_tile = !fp64_ && S_.n_tiles > 0 && S_.halo_cap > 0 && opt_.spmv_path != 2;
+    const bool can_rows = fp64_ || opt_.spmv_path != 1 || !can_tile;
+    if (can_tile) {
+        for (int g : {4, 8}) {
+            if (fixed_lanes && g != fixed_lanes) continue;
+            for (int u : {1, 2, 4}) {
+                if (fixed_unroll && u != fixed_unroll) continue;
+                cand.push_back({1, g, u});
+            }
         }
     }
-    if (cand.empty()) cand.push_back({fixed_lanes ? fixed_lanes : 8, fixed_unroll ? fixed_unroll : 1});
-    auto apply = [&](int g, int u) {
-        L_.lanes = g;
-        L_.unroll = u;
-        L_.grid_bonds = grid_for_rows(g, row_kernel_blocks_per_sm(fp64_, g, u));
+    if (can_rows) {
+        for (int g : {4, 8, 16}) {
+            if (fixed_lanes && g != fixed_lanes) continue;
+            for (int u : {1, 2, 4}) {
+                if (fp64_ && u != 1) continue;
+                if (fixed_unroll && u != fixed_unroll) continue;
+                cand.push_back({0, g, u});
+            }
+        }
+    }
+    if (cand.empty()) cand.push_back({0, fixed_lanes ? fixed_lanes : 8, fixed_unroll ? fixed_unroll : 1});
+    auto apply = [&](const Cand& c) {
+        L_.tiled = c.tiled;
+        L_.lanes = c.g;
+        L_.unroll = c.u;
+        if (c.tiled) {
+            const int bps = std::max(1, tile_spmv_blocks_per_sm(c.g, c.u, S_.halo_cap));
+            L_.grid_tiles = std::max(1, std::min(S_.n_tiles, bps * sm_count_));
+        } else {
+            L_.grid_bonds = grid_for_rows(c.g, row_kernel_blocks_per_sm(fp64_, c.g, c.u));
+        }
     };
     if (cand.size() == 1 || n_ < 20000) {
-        // small problems: launch overhead dominates, keep the default
-        const auto c = cand.size() == 1 ? cand[0] : std::make_pair(8, fp64_ ? 1 : 2);
-        apply(c.first, c.second);
+        // small problems: launch overhead dominates, keep the default (the
+        // tiled path when it was asked for)
+        Cand c = cand.size() == 1 ? cand[0] : Cand{0, 8, fp64_ ? 1 : 2};
+        if (opt_.spmv_path == 1 && can_tile && cand.size() > 1) c = Cand{1, fixed_lanes ? fixed_lanes : 8, fixed_unroll ? fixed_unroll : 2};
+        apply(c);
         return PD_OK;
     }
     const StepParams P = step_params();
@@ -346,26 +382,32 @@ pd_status Engine::tune_spmv()
     CK(cudaEventCreate(&e0), "event");
     CK(cudaEventCreate(&e1), "event");
     float best = 1e30f;
-    std::pair<int, int> best_c = cand[0];
+    Cand best_c = cand[0];
+    // each candidate: one warm-up launch, then the best of three timed pairs
     for (const auto& c : cand) {
-        apply(c.first, c.second);
+        apply(c);
         launch_spmv(fp64_, false, P, S_, L_, stream_);
-        CK(cudaEventRecord(e0, stream_), "event");
-        for (int k = 0; k < 3; ++k) launch_spmv(fp64_, false, P, S_, L_, stream_);
-        CK(cudaEventRecord(e1, stream_), "event");
-        CK(cudaEventSynchronize(e1), "tune sync");
-        float ms = 0.f;
-        CK(cudaEventElapsedTime(&ms, e0, e1), "event");
-        launches_ += 4;
-        if (ms < best) {
-            best = ms;
+        ++launches_;
+        float ms_c = 1e30f;
+        for (int rep = 0; rep < 3; ++rep) {
+            CK(cudaEventRecord(e0, stream_), "event");
+            for (int k = 0; k < 2; ++k) launch_spmv(fp64_, false, P, S_, L_, stream_);
+            CK(cudaEventRecord(e1, stream_), "event");
+            CK(cudaEventSynchronize(e1), "tune sync");
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, e0, e1), "event");
+            ms_c = std::min(ms_c, ms / 2.0f);
+            launches_ += 2;
+        }
+        if (ms_c < best) {
+            best = ms_c;
             best_c = c;
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    apply(best_c.first, best_c.second);
-    tuned_ms_ = best / 3.0f;
+    apply(best_c);
+    tuned_ms_ = best;
     return PD_OK;
 }
 
@@ -1002,6 +1044,7 @@ void Engine::params(pd_sim_params* s, pd_run_params* r, pd_solver_options* o) co
         if (ready_) {   // report the launch shape in use (autotuned when left at 0)
             o->lanes_per_particle = L_.lanes;
             o->spmv_unroll = L_.unroll;
+            o->spmv_path = L_.tiled ? 1 : 2;
         }
     }
 }

@@ -23,6 +23,8 @@ __host__ __device__ inline dbl4 make_dbl4(double x, double y, double z, double w
 
 // Activity byte: low 3 bits = pd_activity, bit 3 = in contact with the sphere
 // during the current step (set by the force pass, read by the SpMV).
+constexpr int kTileRows = 256;      // rows per tile of the shared-memory SpMV
+constexpr int kMaxHaloCap = 2048;   // halo entries a tile may stage (64 KB of shared memory)
 constexpr uint8_t kActMask = 7;
 constexpr uint8_t kActContact = 8;
 
@@ -101,6 +103,20 @@ struct DeviceState {
     float4* u32;       // displacement x - X (mixed)
     float4* xs4;       // mixed: position as FP32 offset in its supercell, w = packed supercell coords
     float* inv_d0;     // mixed: 1 / |X_q - X_p| per bond slot (from FP64)
+    // mixed mode, tiles of tile_rows consecutive rows for the shared-memory
+    // SpMV: halo[halo_ptr[t] .. halo_ptr[t+1]) = sorted distinct neighbour
+    // slots of tile t's rows; lidx[slot] = the bond's neighbour as an index
+    // into its tile's halo (swapped with col on breakage); tile_info[t] = halo
+    // size, or -1 when the tile's halo did not fit the builder's hash set
+    uint16_t* lidx;
+    int* halo;
+    int* halo_ptr;
+    int* tile_info;
+    int tile_rows;
+    int n_tiles;
+    int halo_cap;          // halo entries staged in shared memory (larger tiles use the global path)
+    double* tile_partials; // one FP64 partial per tile
+    unsigned* tile_ctr;    // [0] next tile, [1] arrivals (zero between launches)
     double* jac;       // FP64 mode: symmetric bond Jacobians, 6 per bond slot
     double* jdiag;     // FP64 mode: 6 per particle (sum of bond Jacobians + contact)
     void* force;       // Real4 per particle: pd_force
@@ -119,6 +135,8 @@ struct DeviceState {
 struct LaunchCfg {
     int lanes;          // SpMV lanes per particle row (4, 8, 16, 32)
     int unroll;         // SpMV bonds loaded per lane before computing (1, 2, 4)
+    int tiled;          // 1: shared-memory tile SpMV (mixed mode)
+    int grid_tiles;     // blocks of the tile SpMV
     int grid_bonds;     // SpMV blocks
     int force_lanes;    // force-pass lanes per particle row
     int grid_force;     // force-pass blocks
@@ -139,6 +157,15 @@ void launch_cg_xpby(bool fp64, const StepParams& P, const DeviceState& S, const 
 void launch_update(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
 void launch_refresh(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
 void launch_bond_geometry(const DeviceState& S, int grid, cudaStream_t st);
+// Shared-memory tile SpMV (tiles.cu).  build_tiles fills halo / halo_ptr /
+// tile_info / lidx of S (allocating them) for tiles of S.tile_rows rows and
+// returns the largest halo in *max_halo.
+cudaError_t build_tiles(DeviceState& S, int n, int* max_halo, cudaStream_t st);
+void free_tiles(DeviceState& S);
+// Tile SpMV: blocks per SM for a shared-memory halo of halo_cap entries, and the launch.
+int tile_spmv_blocks_per_sm(int lanes, int unroll, int halo_cap);
+void launch_spmv_tiled(bool dot, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
+cudaError_t scan_exclusive_u32(const unsigned* in, unsigned* out, long long n, cudaStream_t st);
 // Max resident blocks per SM of the SpMV / force kernels (for grid sizing).
 int row_kernel_blocks_per_sm(bool fp64, int lanes, int unroll);
 int force_kernel_blocks_per_sm(bool fp64, int lanes);

@@ -214,6 +214,10 @@ static void spmv_d(bool fp64, const StepParams& P, const DeviceState& S, int lan
 
 void launch_spmv(bool fp64, bool dot, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st)
 {
+    if (!fp64 && L.tiled) {
+        launch_spmv_tiled(dot, P, S, L, st);
+        return;
+    }
     if (dot) spmv_d<true>(fp64, P, S, L.lanes, L.unroll, L.grid_bonds, S.p, S.y, slot_of(S, 1), S.sc, nullptr, st);
     else spmv_d<false>(fp64, P, S, L.lanes, L.unroll, L.grid_bonds, S.sol, S.y, slot_of(S, 1), nullptr, nullptr, st);
 }

@@ -171,6 +171,11 @@ __device__ __forceinline__ void force_row(const StepParams& P, const DeviceState
                         const float t = S.inv_d0[rs + bond];
                         S.inv_d0[rs + bond] = S.inv_d0[rs + top];
                         S.inv_d0[rs + top] = t;
+                        if (S.lidx) {
+                            const uint16_t l = S.lidx[rs + bond];
+                            S.lidx[rs + bond] = S.lidx[rs + top];
+                            S.lidx[rs + top] = l;
+                        }
                     }
                     --top;
                     continue;
@@ -271,6 +276,44 @@ __device__ __forceinline__ dbl4 ld_in(const dbl4* p)
     return make_dbl4(a.x, a.y, b.x, b.y);
 }
 
+// Mixed-precision row result from the group's partial bond sums:
+// y_p = m w_p + t2 (c sum_q J'(w_p - w_q) + k_contact n n^T w_p).
+template <int G, bool DOT, typename Acc>
+__device__ __forceinline__ void spmv_finish_mixed(const StepParams& P, const DeviceState& S, int p, uint8_t ab,
+                                                  const float4& w, float ax, float ay, float az, int lane,
+                                                  unsigned gmask, float4* __restrict__ out, Acc& acc)
+{
+    const float c = (float)P.bond_coeff;
+    const float t2 = (float)P.t2;
+    const float m = (float)P.mass;
+    ax = group_sum<G>(ax, gmask);
+    ay = group_sum<G>(ay, gmask);
+    az = group_sum<G>(az, gmask);
+    if (lane == 0) {
+        float kx = c * ax, ky = c * ay, kz = c * az;
+        if (ab & kActContact) {
+            const float4 Xp = S.X32[p];
+            const float4 Up = S.u32[p];
+            const float dx = Xp.x + Up.x - (float)P.sphere_c_local[0];
+            const float dy = Xp.y + Up.y - (float)P.sphere_c_local[1];
+            const float dz = Xp.z + Up.z - (float)P.sphere_c_local[2];
+            const float inv = rsqrtf(dx * dx + dy * dy + dz * dz);
+            const float nx = dx * inv, ny = dy * inv, nz = dz * inv;
+            const float kn = (float)P.sphere_k * (nx * w.x + ny * w.y + nz * w.z);
+            kx += kn * nx; ky += kn * ny; kz += kn * nz;
+        }
+        const float yx = m * w.x + t2 * kx;
+        const float yy = m * w.y + t2 * ky;
+        const float yz = m * w.z + t2 * kz;
+        out[p] = make_float4(yx, yy, yz, 0.f);
+        if (DOT) {
+            acc.fma(w.x, yx);
+            acc.fma(w.y, yy);
+            acc.fma(w.z, yz);
+        }
+    }
+}
+
 // y_p = (A w)_p by particle p's G-lane group: mass + (beta h^2) stiffness with
 // Dirichlet rows projected out.  DOT: lane 0 adds w_p . y_p to acc.
 // LD: load path of the positions and of w (kLd*).
@@ -341,6 +384,10 @@ __device__ __forceinline__ void spmv_row(const StepParams& P, const DeviceState&
                 az = fmaf(a1, wz, fmaf(g, zs, (float)az));
             }
         }
+    }
+    if constexpr (!FP64) {
+        spmv_finish_mixed<G, DOT>(P, S, p, ab, w, ax, ay, az, lane, gmask, out, acc);
+        return;
     }
     ax = group_sum<G>(ax, gmask);
     ay = group_sum<G>(ay, gmask);

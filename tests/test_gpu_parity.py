@@ -132,3 +132,45 @@ def test_newmark_dt_halving_and_doubling(pdgb, scenes, precision, tol):
     sc.opt.precision = precision
     sim, ora = _run_pair(pdgb, scenes, sc, 90, check_every=5)
     assert rel_err(sim.get(pdgb.VAR_POSITION), ora.position) < tol
+
+
+@pytest.mark.parametrize("path", [1, 2])
+def test_spmv_paths_mixed_breaking(pdgb, scenes, path):
+    """Both mixed SpMV paths (shared-memory tiles, per-bond gathers) against
+    the oracle on a breaking, rolling-back Newmark run."""
+    sc = scenes.reference_block(n_side=8, integrator=pdgb.NEWMARK_BETA, adaptive=1, expansion=300.0,
+                                cg_tol=1e-9)
+    sc.opt.spmv_path = path
+    sim, ora = _run_pair(pdgb, scenes, sc, 60)
+    assert sim.params()[2].spmv_path == path
+    assert sim.stats().bonds_alive < sim.stats().bonds_initial
+    assert rel_err(sim.get(pdgb.VAR_POSITION), ora.position) < MIXED_TOL
+
+
+@pytest.mark.parametrize("path", [1, 2])
+def test_spmv_paths_cube(pdgb, scenes, path):
+    sc = scenes.cube_lattice(n_side=12, seed=2)
+    sc.opt.spmv_path = path
+    sim, ora = _run_pair(pdgb, scenes, sc, 40, check_every=20)
+    assert sim.params()[2].spmv_path == path
+    assert rel_err(sim.get(pdgb.VAR_POSITION), ora.position) < MIXED_TOL
+
+
+def test_spmv_tiled_large_autotuned(pdgb, scenes):
+    """Above 20000 particles the SpMV shape is measured; the tiled and the
+    gather paths give the same run (within the CG tolerance) and match the
+    oracle."""
+    runs = {}
+    for path in (1, 2):
+        sc = scenes.impact_body(24000, "ball", coeff=5.0, speed=6.0, seed=4, steps=6)
+        sc.opt.spmv_path = path
+        sim = scenes.make_simulator(sc)
+        sim.makeReady()
+        sim.advance(6)
+        assert sim.params()[2].spmv_path == path
+        runs[path] = sim
+    ora = make_oracle(sc)
+    ora.advance(6)
+    for path, sim in runs.items():
+        assert same_sets(sim.alive_sets(), ora.alive_sets())
+        assert rel_err(sim.get(pdgb.VAR_POSITION), ora.position) < MIXED_TOL, path
