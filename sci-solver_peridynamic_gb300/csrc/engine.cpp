@@ -134,7 +134,7 @@ void Engine::free_all()
     ws_free();
     void* ptrs[] = {S_.act, S_.x64, S_.v64, S_.X64, S_.x64_bk, S_.v64_bk, S_.st, S_.ost, S_.nst, S_.row_ptr,
                     S_.cnt, S_.cnt_bk, S_.col, S_.X32, S_.u32, S_.xs4, S_.inv_d0, S_.jac, S_.jdiag, S_.force, S_.rhs, S_.sol,
-                    S_.r, S_.p, S_.y, S_.sc, S_.partials, S_.counters, S_.flags, S_.lidx, d_perm_};
+                    S_.r, S_.p, S_.y, S_.sc, S_.partials, S_.counters, S_.flags, S_.lidx, S_.d0sq, d_perm_};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     free_tiles(S_);
@@ -256,6 +256,8 @@ pd_status Engine::make_ready()
         const size_t slots = (size_t)std::max<long long>(total_slots_, 1);
         CK(dalloc(&S_.inv_d0, slots), "alloc inv_d0");
         CK(cudaMemsetAsync(S_.inv_d0, 0, sizeof(float) * slots, stream_), "memset inv_d0");
+        CK(dalloc(&S_.d0sq, slots), "alloc d0sq");
+        CK(cudaMemsetAsync(S_.d0sq, 0, sizeof(double) * slots, stream_), "memset d0sq");
         if (n > 0) {
             const int g = (int)std::min<long long>(std::max<long long>(((long long)n + kBlock - 1) / kBlock, 1), kMaxPartials);
             launch_bond_geometry(S_, g, stream_);

@@ -109,6 +109,14 @@ __device__ __forceinline__ T group_sum(T v, unsigned mask)
 }
 
 template <int G>
+__device__ __forceinline__ float group_minf(float v, unsigned mask)
+{
+#pragma unroll
+    for (int off = G / 2; off > 0; off >>= 1) v = fminf(v, __shfl_xor_sync(mask, v, off, G));
+    return v;
+}
+
+template <int G>
 __device__ __forceinline__ double group_min(double v, unsigned mask)
 {
 #pragma unroll

@@ -103,6 +103,7 @@ struct DeviceState {
     float4* u32;       // displacement x - X (mixed)
     float4* xs4;       // mixed: position as FP32 offset in its supercell, w = packed supercell coords
     float* inv_d0;     // mixed: 1 / |X_q - X_p| per bond slot (from FP64)
+    double* d0sq;      // mixed: |X_p - X_q|^2 per bond slot, formed as the reference's stretch test forms it
     // mixed mode, tiles of tile_rows consecutive rows for the shared-memory
     // SpMV: halo[halo_ptr[t] .. halo_ptr[t+1]) = sorted distinct neighbour
     // slots of tile t's rows; lidx[slot] = the bond's neighbour as an index

@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(kBlock) k_refresh(StepParams P, DeviceState S)
         refresh_elem(P, S, i);
 }
 
-// 1 / d0 per bond slot from the FP64 original positions (once, after the bond build)
+// 1 / d0 and d0^2 per bond slot from the FP64 original positions (once, after the bond build)
 __global__ void __launch_bounds__(kBlock) k_bond_geometry(int n, DeviceState S)
 {
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
@@ -150,8 +150,10 @@ __global__ void __launch_bounds__(kBlock) k_bond_geometry(int n, DeviceState S)
         const int rs = S.row_ptr[p], cn = S.cnt[p];
         for (int j = 0; j < cn; ++j) {
             const dbl4 Xq = S.X64[S.col[rs + j]];
-            const double dx = Xp.x - Xq.x, dy = Xp.y - Xq.y, dz = Xp.z - Xq.z;
-            S.inv_d0[rs + j] = (float)(1.0 / sqrt(dx * dx + dy * dy + dz * dz));
+            const double dx = dsub(Xp.x, Xq.x), dy = dsub(Xp.y, Xq.y), dz = dsub(Xp.z, Xq.z);
+            const double d0s = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
+            S.inv_d0[rs + j] = (float)(1.0 / sqrt(d0s));
+            S.d0sq[rs + j] = d0s;
         }
     }
 }

@@ -75,6 +75,41 @@ __device__ __forceinline__ double break_threshold(float thp, double stq)
 }
 
 // ---- force / breakage ----------------------------------------------------------
+// Mixed precision: the reference's stretch test s = sqrt(dij2)/sqrt(d0_2) - 1 >
+// threshold costs two FP64 square roots and a division per bond, and GB300
+// runs FP64 at ~1/64 of its FP32 rate.  The test is decided instead on the
+// squares, dij2 > (1 + threshold)^2 d0_2, with dij2 and d0_2 formed in FP64
+// exactly as the reference forms them; only when the two sides are within
+// 1e-12 relative (a thousand times the rounding difference of the two forms)
+// is the reference expression itself evaluated.  Broken-bond sets stay
+// bit-exact.
+struct MixedBond {
+    double ex, ey, ez;   // x_q - x_p
+    double dd;           // dij^2
+    double num;          // dij^2 - d0^2
+    bool live;
+};
+
+__device__ __forceinline__ MixedBond classify_mixed(const DeviceState& S, const dbl4& xp, const dbl4& Xp, float thp,
+                                                    int slot, int q)
+{
+    MixedBond m;
+    const dbl4 xq = S.x64[q];
+    m.ex = dsub(xq.x, xp.x);
+    m.ey = dsub(xq.y, xp.y);
+    m.ez = dsub(xq.z, xp.z);
+    m.dd = dadd(dadd(dmul(m.ex, m.ex), dmul(m.ey, m.ey)), dmul(m.ez, m.ez));
+    const double d0s = S.d0sq[slot];
+    const double thr = break_threshold(thp, S.st[q]);
+    const double l1 = dadd(1.0, thr);
+    const double gap = dsub(m.dd, dmul(dmul(l1, l1), d0s));
+    if (l1 > 0.0 && fabs(gap) > 1e-12 * m.dd) m.live = !(gap > 0.0);
+    else m.live = !(eval_bond(xp, Xp, xq, S.X64[q]).s > thr);
+    m.num = dsub(m.dd, d0s);
+    return m;
+}
+
+
 // Force pass of particle p by its G-lane group: stretch test and breakage,
 // bond force, new stretch limit, gravity and contact; FP64 mode also stores the
 // bond Jacobians and their diagonal sum.
@@ -101,48 +136,108 @@ __device__ __forceinline__ void force_row(const StepParams& P, const DeviceState
     double j0 = 0, j1 = 0, j2 = 0, j3 = 0, j4 = 0, j5 = 0;   // FP64: diagonal block sum
     double smin = 0.0;
     int nb = 0;
-    for (int j = lane; j < c; j += G) {
-        const int q = S.col[rs + j];
-        const dbl4 xq = S.x64[q];
-        const dbl4 Xq = S.X64[q];
-        const BondEval b = eval_bond(xp, Xp, xq, Xq);
-        if (b.s > break_threshold(thp, S.st[q])) {
-            ++nb;
-            continue;
+    if constexpr (FP64) {
+        for (int j = lane; j < c; j += G) {
+            const int q = S.col[rs + j];
+            const dbl4 xq = S.x64[q];
+            const dbl4 Xq = S.X64[q];
+            const BondEval b = eval_bond(xp, Xp, xq, Xq);
+            if (b.s > break_threshold(thp, S.st[q])) {
+                ++nb;
+                continue;
+            }
+            smin = b.s < smin ? b.s : smin;
+            if (FP64) {
+                // reference formulas: eij /= fmaxf(dij, SMALL) (float-rounded), vscale,
+                // J = (c/d0) [ (1 - d0/dij) I + (d0/dij) e e^T ]   (cg_solver.cuh:256-303)
+                const double D = (double)fmaxf((float)b.dij, (float)1e-10);
+                const double ex = ddiv(b.ex, D), ey = ddiv(b.ey, D), ez = ddiv(b.ez, D);
+                double vscale = 1.0;
+                if (b.d0 > P.vs_threshold) vscale = dadd(0.5, ddiv(ddiv(dsub(P.horizon, b.d0), 2.0), P.radius));
+                const double kk = dmul(b.s, vscale);
+                fx = dadd(fx, dmul(kk, ex));
+                fy = dadd(fy, dmul(kk, ey));
+                fz = dadd(fz, dmul(kk, ez));
+                const double r = ddiv(b.d0, b.dij);
+                const double dg = dsub(1.0, r);
+                const double cc = ddiv(P.bond_coeff, b.d0);
+                const double jxx = dmul(dadd(dg, dmul(dmul(ex, ex), r)), cc);
+                const double jyy = dmul(dadd(dg, dmul(dmul(ey, ey), r)), cc);
+                const double jzz = dmul(dadd(dg, dmul(dmul(ez, ez), r)), cc);
+                const double jxy = dmul(dmul(dmul(ex, ey), r), cc);
+                const double jxz = dmul(dmul(dmul(ex, ez), r), cc);
+                const double jyz = dmul(dmul(dmul(ey, ez), r), cc);
+                double* J = S.jac + 6ll * (rs + j);
+                J[0] = jxx; J[1] = jyy; J[2] = jzz; J[3] = jxy; J[4] = jxz; J[5] = jyz;
+                j0 += jxx; j1 += jyy; j2 += jzz; j3 += jxy; j4 += jxz; j5 += jyz;
+            } else {
+                const float inv = 1.0f / (float)b.dij;
+                const float d0f = (float)b.d0;
+                float vs = 1.0f;
+                if (b.d0 > P.vs_threshold) vs = 0.5f + ((float)P.horizon - d0f) * 0.5f / (float)P.radius;
+                const float kk = (float)b.s * vs * inv;
+                fx = fmaf(kk, (float)b.ex, (float)fx);
+                fy = fmaf(kk, (float)b.ey, (float)fy);
+                fz = fmaf(kk, (float)b.ez, (float)fz);
+            }
         }
-        smin = b.s < smin ? b.s : smin;
-        if (FP64) {
-            // reference formulas: eij /= fmaxf(dij, SMALL) (float-rounded), vscale,
-            // J = (c/d0) [ (1 - d0/dij) I + (d0/dij) e e^T ]   (cg_solver.cuh:256-303)
-            const double D = (double)fmaxf((float)b.dij, (float)1e-10);
-            const double ex = ddiv(b.ex, D), ey = ddiv(b.ey, D), ez = ddiv(b.ez, D);
-            double vscale = 1.0;
-            if (b.d0 > P.vs_threshold) vscale = dadd(0.5, ddiv(ddiv(dsub(P.horizon, b.d0), 2.0), P.radius));
-            const double kk = dmul(b.s, vscale);
-            fx = dadd(fx, dmul(kk, ex));
-            fy = dadd(fy, dmul(kk, ey));
-            fz = dadd(fz, dmul(kk, ez));
-            const double r = ddiv(b.d0, b.dij);
-            const double dg = dsub(1.0, r);
-            const double cc = ddiv(P.bond_coeff, b.d0);
-            const double jxx = dmul(dadd(dg, dmul(dmul(ex, ex), r)), cc);
-            const double jyy = dmul(dadd(dg, dmul(dmul(ey, ey), r)), cc);
-            const double jzz = dmul(dadd(dg, dmul(dmul(ez, ez), r)), cc);
-            const double jxy = dmul(dmul(dmul(ex, ey), r), cc);
-            const double jxz = dmul(dmul(dmul(ex, ez), r), cc);
-            const double jyz = dmul(dmul(dmul(ey, ez), r), cc);
-            double* J = S.jac + 6ll * (rs + j);
-            J[0] = jxx; J[1] = jyy; J[2] = jzz; J[3] = jxy; J[4] = jxz; J[5] = jyz;
-            j0 += jxx; j1 += jyy; j2 += jzz; j3 += jxy; j4 += jxz; j5 += jyz;
-        } else {
-            const float inv = 1.0f / (float)b.dij;
-            const float d0f = (float)b.d0;
+    } else {
+        // live bonds: FP32 force from the FP64 bond vector; the stretch comes
+        // from dij2 - d0^2 (no cancellation) as s = (dij2 - d0^2) / (d0 (dij + d0))
+        const float* id0r = S.inv_d0 + rs;
+        float r1 = 3.0e38f, r2 = 3.0e38f;   // the lane's two smallest (dij2 - d0^2) / d0^2
+        int j1 = -1;
+        for (int j = lane; j < c; j += G) {
+            const int q = S.col[rs + j];
+            const MixedBond m = classify_mixed(S, xp, Xp, thp, rs + j, q);
+            if (!m.live) {
+                ++nb;
+                continue;
+            }
+            const float idd0 = id0r[j];
+            const float d = sqrtf((float)m.dd);
+            const float d0 = 1.0f / idd0;
+            const float sf = (float)m.num * idd0 / (d + d0);
+            const float r = (float)m.num * (idd0 * idd0);
+            if (r < r1) {
+                r2 = r1;
+                r1 = r;
+                j1 = j;
+            } else if (r < r2) {
+                r2 = r;
+            }
             float vs = 1.0f;
-            if (b.d0 > P.vs_threshold) vs = 0.5f + ((float)P.horizon - d0f) * 0.5f / (float)P.radius;
-            const float kk = (float)b.s * vs * inv;
-            fx = fmaf(kk, (float)b.ex, (float)fx);
-            fy = fmaf(kk, (float)b.ey, (float)fy);
-            fz = fmaf(kk, (float)b.ez, (float)fz);
+            if ((double)d0 > P.vs_threshold) vs = 0.5f + ((float)P.horizon - d0) * 0.5f / (float)P.radius;
+            const float kk = sf * vs / fmaxf(d, 1e-10f);   // eij /= fmaxf(dij, SMALL)
+            fx = fmaf(kk, (float)m.ex, (float)fx);
+            fy = fmaf(kk, (float)m.ey, (float)fy);
+            fz = fmaf(kk, (float)m.ez, (float)fz);
+        }
+        // smin = min(0, smallest stretch of a live bond), bit for bit: if no
+        // live bond is shorter than at rest every stretch is >= 0; otherwise
+        // the bonds whose estimate lies within its error (1e-6 relative) of the
+        // smallest are evaluated with the reference expression
+        const float rmin = group_minf<G>(r1, gmask);
+        if (rmin <= 0.f) {
+            const float band = rmin + 1e-6f * fabsf(rmin) + 1e-30f;
+            if (!__any_sync(gmask, r2 <= band)) {
+                if (r1 <= band) {
+                    const int q = S.col[rs + j1];
+                    const double s1 = eval_bond(xp, Xp, S.x64[q], S.X64[q]).s;
+                    smin = s1 < smin ? s1 : smin;
+                }
+            } else {
+                // several candidates in one lane: walk the row again
+                for (int j = lane; j < c; j += G) {
+                    const int q = S.col[rs + j];
+                    const MixedBond m = classify_mixed(S, xp, Xp, thp, rs + j, q);
+                    if (!m.live) continue;
+                    const float idd0 = id0r[j];
+                    if ((float)m.num * (idd0 * idd0) > band) continue;
+                    const double sj = eval_bond(xp, Xp, S.x64[q], S.X64[q]).s;
+                    smin = sj < smin ? sj : smin;
+                }
+            }
         }
     }
     fx = group_sum<G>(fx, gmask);
@@ -171,6 +266,9 @@ __device__ __forceinline__ void force_row(const StepParams& P, const DeviceState
                         const float t = S.inv_d0[rs + bond];
                         S.inv_d0[rs + bond] = S.inv_d0[rs + top];
                         S.inv_d0[rs + top] = t;
+                        const double t2 = S.d0sq[rs + bond];
+                        S.d0sq[rs + bond] = S.d0sq[rs + top];
+                        S.d0sq[rs + top] = t2;
                         if (S.lidx) {
                             const uint16_t l = S.lidx[rs + bond];
                             S.lidx[rs + bond] = S.lidx[rs + top];
