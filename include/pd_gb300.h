@@ -341,6 +341,30 @@ pd_status pd_get_stream(pd_handle* h, void** stream);
 /* Waits until all work of the handle has finished on the device. */
 pd_status pd_synchronize(pd_handle* h);
 
+/* ---- DataIO (src/core/dataIO.h:20-44) -------------------------------------
+ * Output under run->saving_path, as the reference's DataIO: frames
+ * DATA/<VAR>/frame.<savedFrame> (raw arrays in caller order: PD_POSITION
+ * double4 scaled by scaleFactor; with the run's dump_velocity /
+ * dump_activity / dump_pd_bond_list_top also PD_VELOCITY double4,
+ * PD_ACTIVITY int32, PD_ORIGINAL_BOND_COUNT and PD_BOND_LIST_TOP int32 as
+ * counts - 1), DATA/sim_info.dat (the reference's SimulationParameters,
+ * raw) and DATA/viz_info.dat.  Checkpoints go to DATA/STATE/state.<step>
+ * (the folder the reference creates; its saveState writes STATE/, which it
+ * never creates): the reference's leading savedFrame, then this library's
+ * own state layout. */
+/* DataIO::getDataAndWrite (dataIO.cu:82-124), creating the folders of
+ * createOutputFolders (dataIO.cu:207-249) and sim_info on first use */
+pd_status pd_dataio_get_data_and_write(pd_handle* h);
+/* DataIO::newFrame (dataIO.cu:200-204) */
+pd_status pd_dataio_new_frame(pd_handle* h);
+/* DataIO::savedFrame */
+pd_status pd_dataio_saved_frame(pd_handle* h, size_t* frame);
+/* DataIO::saveState (dataIO.cu:150-175) */
+pd_status pd_dataio_save_state(pd_handle* h, size_t timestep);
+/* DataIO::loadState (dataIO.cu:178-203): into a handle made ready on the same
+ * scene (same particles and bonds); the run then continues bit for bit. */
+pd_status pd_dataio_load_state(pd_handle* h, size_t timestep);
+
 /* ---- batched scenes (no reference counterpart) -----------------------------
  * Many independent scenes (each with the parameter surface of one Simulator)
  * stepped together: per step, two cooperative persistent launches cover every

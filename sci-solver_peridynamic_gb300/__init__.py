@@ -200,6 +200,11 @@ def library(build_if_missing: bool = True):
         "pd_abi_version": (C.c_int, []),
         "pd_sample_stretch_limits": (st, [C.c_float, C.c_int, P(C.c_double)]),
         "pd_adaptive_decide": (st, [C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_int), P(C.c_int), P(C.c_int)]),
+        "pd_dataio_get_data_and_write": (st, [vp]),
+        "pd_dataio_new_frame": (st, [vp]),
+        "pd_dataio_saved_frame": (st, [vp, P(C.c_size_t)]),
+        "pd_dataio_save_state": (st, [vp, C.c_size_t]),
+        "pd_dataio_load_state": (st, [vp, C.c_size_t]),
         "pd_batch_options_default": (st, [P(BatchOptions)]),
         "pd_batch_create": (st, [C.c_int, P(BatchOptions), P(vp)]),
         "pd_batch_destroy": (st, [vp]),
@@ -493,6 +498,24 @@ class Simulator:
         T = np.zeros((max_rows if max_rows else 1, 3), np.float32)
         _check(self.lib.pd_ws_dataset(self.h, _fp(X), _fp(T), max_rows, C.byref(rows)), self.h)
         return X[:rows.value], T[:rows.value]
+
+    # DataIO (src/core/dataIO.h:20-44): frames / sim_info / checkpoints under run.saving_path
+    def dataIO_getDataAndWrite(self):
+        _check(self.lib.pd_dataio_get_data_and_write(self.h), self.h)
+
+    def dataIO_newFrame(self):
+        _check(self.lib.pd_dataio_new_frame(self.h), self.h)
+
+    def dataIO_savedFrame(self) -> int:
+        v = C.c_size_t()
+        _check(self.lib.pd_dataio_saved_frame(self.h, C.byref(v)), self.h)
+        return v.value
+
+    def dataIO_saveState(self, timestep: int):
+        _check(self.lib.pd_dataio_save_state(self.h, int(timestep)), self.h)
+
+    def dataIO_loadState(self, timestep: int):
+        _check(self.lib.pd_dataio_load_state(self.h, int(timestep)), self.h)
 
     def stream_handle(self) -> int:
         """cudaStream_t of this simulator, as an integer (for CUDA events)."""

@@ -28,7 +28,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["step.cu", "bonds.cu", "noalloc.cu", "mlp.cu", "warmstart.cu", "batch.cu", "tiles.cu"]
-CPP_SOURCES = ["engine.cpp", "capi.cpp", "params.cpp", "batch.cpp"]
+CPP_SOURCES = ["engine.cpp", "capi.cpp", "params.cpp", "batch.cpp", "dataio.cpp"]
 
 
 def _sources_digest() -> str:

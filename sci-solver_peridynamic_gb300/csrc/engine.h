@@ -45,8 +45,15 @@ public:
     pd_status ws_collect(int samples_per_step, long long capacity);
     pd_status ws_dataset(float* X, float* T, long long max_rows, long long* rows);
     const std::string& error() const { return err_; }
+    // DataIO (dataio.cpp): frames, simulation info and checkpoints under run.saving_path
+    pd_status dataio_write_frame();
+    void dataio_new_frame() { ++saved_frame_; }
+    size_t dataio_saved_frame() const { return saved_frame_; }
+    pd_status dataio_save_state(size_t timestep);
+    pd_status dataio_load_state(size_t timestep);
 
 private:
+    pd_status dataio_write_sim_info();
     pd_status cuda_fail(cudaError_t e, const char* what);
     pd_status allocate();
     void free_all();
@@ -136,6 +143,8 @@ private:
     long long kc_launches_[PD_KC_COUNT] = {0, 0, 0, 0};
     double kc_ms_[PD_KC_COUNT] = {0, 0, 0, 0};
     long long launches_ = 0;
+    size_t saved_frame_ = 0;           // DataIO::savedFrame
+    bool wrote_sim_info_ = false;      // DataIO::writtenSimulationParameter
     std::string err_;
 };
 
