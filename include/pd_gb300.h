@@ -365,6 +365,28 @@ pd_status pd_dataio_save_state(pd_handle* h, size_t timestep);
  * scene (same particles and bonds); the run then continues bit for bit. */
 pd_status pd_dataio_load_state(pd_handle* h, size_t timestep);
 
+/* ---- example scene: an OBJ mesh filled with particles (src/examples/scene.cpp) */
+typedef struct pd_scene pd_scene;
+/* Scene(simParams, runningParams, arrangement) (scene.cpp:18-135): reads
+ * run->obj_file (cyTriMesh OBJ reading: v / f lines, polygons as fans), scales
+ * the mesh to half of 0.9 x the smallest box extent with its minimum corner at
+ * boundary_min, and keeps the points of a lattice of spacing 2 r inside the
+ * mesh -- the inside test runs on the GPU (run->gpu_device) with exact
+ * predicates.  jittered = 0: REGULAR_GRID; 1: JITTERED_GRID, offsets
+ * (frand() * 2 - 1) * 0.01 r from the C library's rand() stream after
+ * srand(jitter_seed) (1: the stream of a process that never called srand).
+ * Sets sim->num_pd_particle. */
+pd_status pd_scene_create(pd_sim_params* sim, const pd_run_params* run, int jittered, unsigned jitter_seed,
+                          pd_scene** out);
+pd_status pd_scene_particle_count(pd_scene* s, int* count);
+/* Scene::initPeridynamicsParticles (scene.cpp:360-395): positions translated
+ * by mesh_translation / scaleFactor, activity PD_ACTIVE, every velocity
+ * component pd_initial_velocity.  Arrays of num_pd_particle entries
+ * (pos4 / vel4: 4 doubles each). */
+pd_status pd_scene_init_pd_particles(pd_scene* s, int32_t* activity, double* pos4, double* vel4);
+pd_status pd_scene_destroy(pd_scene* s);
+const char* pd_scene_last_error_message(void);
+
 /* ---- batched scenes (no reference counterpart) -----------------------------
  * Many independent scenes (each with the parameter surface of one Simulator)
  * stepped together: per step, two cooperative persistent launches cover every

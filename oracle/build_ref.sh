@@ -1,5 +1,7 @@
 #!/usr/bin/env bash
-# Builds oracle/_ref/libpdref.so from the reference's own kernel source.
+# Builds oracle/_ref/libpdref.so from the reference's own kernel source, and
+# oracle/_ref/libpdscene.so from the reference's example Scene (OBJ reading,
+# mesh fill with mesh_query0.1's inside test).
 # TEST INFRASTRUCTURE ONLY: the library is a checker for the oracle
 # restatement (pd_oracle.c) and the source of tests/golden/ fixtures.
 #
@@ -37,3 +39,14 @@ mkdir -p "$OUT"
 } | g++ -std=c++17 -O2 -ffp-contract=off -fopenmp -fPIC -shared -w \
       -I"$CORE" -I"$CUDA_INC" -x c++ - -o "$OUT/libpdref.so"
 echo "built $OUT/libpdref.so"
+# The example Scene: compiled as it lies in the reference tree.  Monitor's
+# CUDA-event code is not needed; helper_cuda.h (which no longer compiles
+# against CUDA 13's cudaDeviceProp) is kept out through its include guard.
+EX="$REF/src/examples"
+MQ="$EX/mesh_query0.1"
+g++ -std=c++17 -O2 -ffp-contract=off -fPIC -shared -w -DHELPER_CUDA_H \
+    -include cstring -include vector -include cuda_runtime_api.h \
+    -I"$REF/src" -I"$CORE" -I"$EX" -I"$CUDA_INC" \
+    "$EX/scene.cpp" "$MQ/mesh_query.cpp" "$MQ/predicates.cpp" "$MQ/bounding_box_tree.cpp" \
+    "$HERE/ref_scene_driver.cpp" -o "$OUT/libpdscene.so"
+echo "built $OUT/libpdscene.so"

@@ -205,6 +205,11 @@ def library(build_if_missing: bool = True):
         "pd_dataio_saved_frame": (st, [vp, P(C.c_size_t)]),
         "pd_dataio_save_state": (st, [vp, C.c_size_t]),
         "pd_dataio_load_state": (st, [vp, C.c_size_t]),
+        "pd_scene_create": (st, [P(SimulationParameters), P(RunningParameters), C.c_int, C.c_uint, P(vp)]),
+        "pd_scene_particle_count": (st, [vp, P(C.c_int)]),
+        "pd_scene_init_pd_particles": (st, [vp, P(C.c_int32), P(C.c_double), P(C.c_double)]),
+        "pd_scene_destroy": (st, [vp]),
+        "pd_scene_last_error_message": (C.c_char_p, []),
         "pd_batch_options_default": (st, [P(BatchOptions)]),
         "pd_batch_create": (st, [C.c_int, P(BatchOptions), P(vp)]),
         "pd_batch_destroy": (st, [vp]),
@@ -653,3 +658,46 @@ class Batch:
 
     def synchronize(self):
         _bcheck(self.lib.pd_batch_synchronize(self.h), self.h)
+
+
+class Scene:
+    """The reference's example Scene (src/examples/scene.cpp) for PD particles:
+    run.obj_file is scaled into the simulation box and filled with a lattice
+    of spacing 2 r on the GPU.  Mirrors Scene(simParams, runningParams,
+    arrangement) + initPeridynamicsParticles; sets simParams.num_pd_particle."""
+
+    REGULAR_GRID = 0
+    JITTERED_GRID = 1
+
+    def __init__(self, simParams: SimulationParameters, runningParams: RunningParameters,
+                 arrangement: int = 0, jitter_seed: int = 1):
+        self.lib = library()
+        h = C.c_void_p()
+        st = self.lib.pd_scene_create(C.byref(simParams), C.byref(runningParams), int(arrangement),
+                                      int(jitter_seed), C.byref(h))
+        if st != PD_OK:
+            msg = self.lib.pd_scene_last_error_message()
+            raise PdError(st, msg.decode() if msg else "")
+        self.h = h
+        self.n = int(simParams.num_pd_particle)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pd_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def initPeridynamicsParticles(self):
+        """(activity int32[n], positions double[n,4], velocities double[n,4])"""
+        act = np.zeros(self.n, np.int32)
+        pos = np.zeros((self.n, 4), np.float64)
+        vel = np.zeros((self.n, 4), np.float64)
+        dp = C.POINTER(C.c_double)
+        _check(self.lib.pd_scene_init_pd_particles(self.h, act.ctypes.data_as(C.POINTER(C.c_int32)),
+                                                   pos.ctypes.data_as(dp), vel.ctypes.data_as(dp)))
+        return act, pos, vel

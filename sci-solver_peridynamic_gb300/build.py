@@ -27,8 +27,8 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["step.cu", "bonds.cu", "noalloc.cu", "mlp.cu", "warmstart.cu", "batch.cu", "tiles.cu"]
-CPP_SOURCES = ["engine.cpp", "capi.cpp", "params.cpp", "batch.cpp", "dataio.cpp"]
+CU_SOURCES = ["step.cu", "bonds.cu", "noalloc.cu", "mlp.cu", "warmstart.cu", "batch.cu", "tiles.cu", "mesh_fill.cu"]
+CPP_SOURCES = ["engine.cpp", "capi.cpp", "params.cpp", "batch.cpp", "dataio.cpp", "scene.cpp"]
 
 
 def _sources_digest() -> str:

@@ -150,3 +150,34 @@ def test_solver_option_defaults(pdgb):
     assert o.time_step_base == 1.0 / 8388608.0 and o.time_step_min == 100 and o.max_substep == 10
     assert o.phase_in_steps == 30 and o.pd_k == 5.0 * 2.94315e9 and o.max_bonds_per_particle == 528
     assert tuple(o.gravity) == (0.0, -9.8, 0.0) and o.restitution == 0.001
+
+
+def test_mesh_fill_golden_pinned_to_reference():
+    """The mesh-fill fixtures are the reference's own Scene output; where the
+    host build of the reference is present, regenerate and compare."""
+    import importlib.util
+    path = os.path.join(os.path.dirname(__file__), "golden", "mesh_fill.npz")
+    g = np.load(path)
+    names = sorted({k.split("/")[0] for k in g.files})
+    assert len(names) >= 5
+    for n in names:
+        assert g[n + "/pos"].shape[1] == 4 and g[n + "/pos"].shape[0] > 1000
+    lib = os.path.join(os.path.dirname(os.path.dirname(__file__)), "oracle", "_ref", "libpdscene.so")
+    if not os.path.exists(lib):
+        pytest.skip("host build of the reference scene not present")
+    spec = importlib.util.spec_from_file_location("make_mesh_golden",
+                                                  os.path.join(os.path.dirname(__file__), "golden",
+                                                               "make_mesh_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    import ctypes
+    import tempfile
+    L = ctypes.CDLL(lib)
+    with tempfile.TemporaryDirectory() as td:
+        for name, (verts, faces), bmin, bmax, radius, sf, tr, v0, arr in mg.CASES:
+            p = os.path.join(td, name + ".obj")
+            with open(p, "w") as fh:
+                fh.write(mg.obj_text(verts, faces))
+            pos, vel = mg.reference_fill(L, p, bmin, bmax, radius, sf, tr, v0, arr)
+            np.testing.assert_array_equal(pos, g[name + "/pos"])
+            np.testing.assert_array_equal(vel, g[name + "/vel"])

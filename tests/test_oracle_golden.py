@@ -11,7 +11,7 @@ import pytest
 
 from oracle import oracle as O
 
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "ref_block_*.npz")))
 
 
 def oracle_from_fixture(d):
