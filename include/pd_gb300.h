@@ -139,6 +139,17 @@ typedef struct pd_solver_options {
      * (measured slower than the gathers at 1M particles; kept as an option).
      * Either way lanes x unroll is measured at make_ready when n >= 20000. */
     int spmv_path;
+    /* PD-PD contact (collectPDParticles / collidePDParticles,
+     * src/core/simulator.cuh:606-768, compiled out in the reference): every
+     * two particles closer than contact_distance repel with
+     * contact_stiffness * (r - d)^2 / contact_volume along their separation,
+     * added to the force each step.  Defaults: off, FCELL *
+     * PERIDYNAMICS_MIN_DISTANCE = 0.75 * 0.0005, Kc = 1e7, PD_V = 0.0005^3
+     * (definitions.h:86-98). */
+    int contact_enabled;
+    double contact_distance;
+    double contact_stiffness;
+    double contact_volume;
 } pd_solver_options;
 
 /* Export selectors for pd_get. */

@@ -58,6 +58,8 @@ class PdoParams(C.Structure):
         ("max_bonds", C.c_int), ("s0", C.c_double), ("sphere_on", C.c_int),
         ("sphere_c0", C.c_double * 3), ("sphere_v", C.c_double * 3),
         ("sphere_radius", C.c_double), ("sphere_k", C.c_double),
+        ("contact_on", C.c_int), ("contact_dist", C.c_double), ("contact_k", C.c_double),
+        ("contact_vol", C.c_double),
     ]
 
 

@@ -67,6 +67,10 @@ void pdo_default_params(pdo_params* p)
     p->max_bonds = 528;               /* definitions.h:101 */
     p->box_min[0] = p->box_min[1] = p->box_min[2] = -1e300;
     p->box_max[0] = p->box_max[1] = p->box_max[2] = 1e300;
+    p->contact_on = 0;
+    p->contact_dist = 0.75 * 0.0005;   /* FCELL * PERIDYNAMICS_MIN_DISTANCE, definitions.h:86,98 */
+    p->contact_k = 1.0e7;              /* Kc, definitions.h:90 */
+    p->contact_vol = 0.0005 * 0.0005 * 0.0005;   /* PD_V, definitions.h:87 */
 }
 
 static void* xcalloc(size_t n, size_t sz) { return calloc(n ? n : 1, sz); }
@@ -365,6 +369,29 @@ static void force_particle(pdo_state* s, int p, double cs, int* broke)
     }
 }
 
+/* collidePDParticles (simulator.cuh:675-768): every pair closer than the
+ * contact distance repels with Kc (r - d)^2 / V along x_p - x_q; all pairs
+ * by brute force, in q order (test scenes are small). */
+static void contact_particle(pdo_state* s, int p)
+{
+    const pdo_params* P = &s->P;
+    if (s->act[p] == PDO_INVISIBLE) return;
+    const double* X = s->pos + 4 * p;
+    double f[3] = {0.0, 0.0, 0.0};
+    for (int q = 0; q < s->n; ++q) {
+        if (q == p || s->act[q] == PDO_INVISIBLE) continue;
+        const double* Q = s->pos + 4 * q;
+        const double pq[3] = {X[0] - Q[0], X[1] - Q[1], X[2] - Q[2]};
+        const double r = sqrt(pq[0] * pq[0] + pq[1] * pq[1] + pq[2] * pq[2]);
+        if (r >= P->contact_dist || r == 0.0) continue;
+        const double howfar = r - P->contact_dist;
+        const double mag = P->contact_k * (howfar * howfar) / P->contact_vol;
+        for (int k = 0; k < 3; ++k) f[k] += mag * (pq[k] / r);
+    }
+    if (sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]) > 1e-10)
+        for (int k = 0; k < 3; ++k) s->force[4 * p + k] += f[k];
+}
+
 int pdo_force_pass(pdo_state* s, int* has_broken)
 {
     int broke = 0;
@@ -374,6 +401,10 @@ int pdo_force_pass(pdo_state* s, int* has_broken)
         int b = 0;
         force_particle(s, p, cs, &b);
         broke |= b;
+    }
+    if (s->P.contact_on) {
+        #pragma omp parallel for schedule(dynamic, 64)
+        for (int p = 0; p < s->n; ++p) contact_particle(s, p);
     }
     if (has_broken) *has_broken = broke;
     return 0;

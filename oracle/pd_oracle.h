@@ -65,6 +65,11 @@ typedef struct pdo_params {
     double sphere_v[3];
     double sphere_radius;
     double sphere_k;
+    /* PD-PD contact (collidePDParticles, simulator.cuh:675-768; off in the reference) */
+    int    contact_on;
+    double contact_dist;     /* FCELL * PERIDYNAMICS_MIN_DISTANCE */
+    double contact_k;        /* Kc */
+    double contact_vol;      /* PD_V */
 } pdo_params;
 
 typedef struct pdo_state pdo_state;

@@ -92,7 +92,8 @@ class SolverOptions(C.Structure):
         ("sphere_center", C.c_double * 3), ("sphere_velocity", C.c_double * 3),
         ("sphere_radius", C.c_double), ("sphere_stiffness", C.c_double),
         ("lanes_per_particle", C.c_int), ("cg_check_interval", C.c_int), ("spmv_unroll", C.c_int),
-        ("warm_start", C.c_int), ("spmv_path", C.c_int),
+        ("warm_start", C.c_int), ("spmv_path", C.c_int), ("contact_enabled", C.c_int),
+        ("contact_distance", C.c_double), ("contact_stiffness", C.c_double), ("contact_volume", C.c_double),
     ]
 
 

@@ -144,6 +144,10 @@ pd_status Batch::add_scene(const pd_sim_params& sim, const pd_run_params& run, c
         err_ = "add_scene after make_ready";
         return PD_ERR_STATE;
     }
+    if (opt.contact_enabled) {
+        err_ = "PD-PD contact is not available in batches";
+        return PD_ERR_INVALID_ARGUMENT;
+    }
     pd_run_params r = run;
     r.gpu_device = device_;
     std::unique_ptr<Engine> e(new (std::nothrow) Engine(sim, r, opt));

@@ -69,6 +69,10 @@ pd_status pd_create(const pd_sim_params* sim, const pd_run_params* run, const pd
         g_create_error = "time step must be positive";
         return PD_ERR_INVALID_ARGUMENT;
     }
+    if (o.contact_enabled && !(o.contact_distance > 0 && o.contact_volume > 0)) {
+        g_create_error = "contact distance and volume must be positive";
+        return PD_ERR_INVALID_ARGUMENT;
+    }
     pd_handle* h = new (std::nothrow) pd_handle{nullptr};
     if (!h) return PD_ERR_OUT_OF_MEMORY;
     h->eng = new (std::nothrow) pdgb::Engine(*sim, *run, o);

@@ -138,6 +138,12 @@ void Engine::free_all()
     for (void* p : ptrs)
         if (p) cudaFree(p);
     free_tiles(S_);
+    cudaFree(contact_.counts);
+    cudaFree(contact_.start);
+    cudaFree(contact_.cursor);
+    cudaFree(contact_.bucket);
+    cudaFree(contact_.list);
+    contact_ = ContactBuffers{};
     S_ = DeviceState{};
     d_perm_ = nullptr;
 }
@@ -277,6 +283,17 @@ pd_status Engine::make_ready()
             launches_ += 2;
             S_.halo_cap = std::min(max_halo, kMaxHaloCap);
         }
+    }
+    // PD-PD contact hash: a power-of-two bucket count >= 2 n
+    if (opt_.contact_enabled && n > 0) {
+        unsigned nb = 1;
+        while (nb < 2u * (unsigned)n) nb <<= 1;
+        contact_.buckets = nb;
+        CK(dalloc(&contact_.counts, (size_t)nb + 1), "alloc contact");
+        CK(dalloc(&contact_.start, (size_t)nb + 1), "alloc contact");
+        CK(dalloc(&contact_.cursor, (size_t)nb), "alloc contact");
+        CK(dalloc(&contact_.bucket, N), "alloc contact");
+        CK(dalloc(&contact_.list, N), "alloc contact");
     }
     // CG scalars (initPDSolutions zeroed the solution, cg_solver.cuh:184-194)
     std::memset(h_sc_, 0, sizeof(CgScalars));
@@ -748,6 +765,15 @@ pd_status Engine::integrate(bool* advanced)
         CK(cudaMemcpyAsync(S_.cnt_bk, S_.cnt, sizeof(int) * N, cudaMemcpyDeviceToDevice, stream_), "backup cnt");
         CK(cudaMemcpyAsync(S_.x64_bk, S_.x64, sizeof(dbl4) * N, cudaMemcpyDeviceToDevice, stream_), "backup x");
         CK(cudaMemcpyAsync(S_.v64_bk, S_.v64, sizeof(dbl4) * N, cudaMemcpyDeviceToDevice, stream_), "backup v");
+    }
+    // PD-PD contact forces (collidePDParticles, after the stretch-limit
+    // update and before fillMatrix*, simulator.cu:410-426, 581-597)
+    if (opt_.contact_enabled && n_ > 0) {
+        const ContactParams C{opt_.contact_distance, opt_.contact_stiffness, opt_.contact_volume};
+        mark_begin(PD_KC_FORCE, -1);
+        CK(launch_contact(fp64_, S_, n_, C, contact_, stream_), "contact");
+        mark_end();
+        launches_ += 4;
     }
     // the assembly, solve and update of this step use the time step as the
     // adaptive decision left it (the reference doubles it in place)

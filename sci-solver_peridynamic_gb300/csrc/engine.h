@@ -143,6 +143,7 @@ private:
     long long kc_launches_[PD_KC_COUNT] = {0, 0, 0, 0};
     double kc_ms_[PD_KC_COUNT] = {0, 0, 0, 0};
     long long launches_ = 0;
+    ContactBuffers contact_{};         // PD-PD contact hash (when enabled)
     size_t saved_frame_ = 0;           // DataIO::savedFrame
     bool wrote_sim_info_ = false;      // DataIO::writtenSimulationParameter
     std::string err_;

@@ -155,6 +155,9 @@ extern "C" pd_status pd_solver_options_default(pd_solver_options* o)
     if (!o) return PD_ERR_INVALID_ARGUMENT;
     std::memset(o, 0, sizeof(*o));
     o->precision = PD_PRECISION_MIXED;
+    o->contact_distance = 0.75 * 0.0005;
+    o->contact_stiffness = 1.0e7;
+    o->contact_volume = 0.0005 * 0.0005 * 0.0005;
     o->cg_relative_tolerance = 1e-20;
     o->cg_max_iterations = 100000;
     o->time_step_base = 1.0 / 8388608.0;

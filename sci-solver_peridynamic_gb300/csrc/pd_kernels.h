@@ -167,6 +167,23 @@ void free_tiles(DeviceState& S);
 int tile_spmv_blocks_per_sm(int lanes, int unroll, int halo_cap);
 void launch_spmv_tiled(bool dot, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
 cudaError_t scan_exclusive_u32(const unsigned* in, unsigned* out, long long n, cudaStream_t st);
+
+// PD-PD contact (contact.cu)
+struct ContactParams {
+    double distance;    // d_c
+    double stiffness;   // K_c
+    double volume;      // V
+};
+struct ContactBuffers {
+    unsigned buckets;   // power of two
+    unsigned* counts;   // buckets + 1
+    unsigned* start;    // buckets + 1
+    unsigned* cursor;   // buckets
+    unsigned* bucket;   // n
+    int* list;          // n
+};
+cudaError_t launch_contact(bool fp64, const DeviceState& S, int n, const ContactParams& C, const ContactBuffers& B,
+                           cudaStream_t st);
 // Max resident blocks per SM of the SpMV / force kernels (for grid sizing).
 int row_kernel_blocks_per_sm(bool fp64, int lanes, int unroll);
 int force_kernel_blocks_per_sm(bool fp64, int lanes);

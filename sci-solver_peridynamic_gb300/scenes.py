@@ -284,6 +284,39 @@ def impact_body(n_target=8000, shape="block", coeff=5.0, speed=5.0, seed=0, spac
                  {"spacing": spacing, "seed": seed, "shape": shape, "coeff": coeff, "speed": speed})
 
 
+def two_blocks(n_side=6, spacing=0.02, gap_spacings=3.0, speed=5.0, seed=0, jitter=0.05, coeff=5.0, s0=0.02,
+               dt=1e-4, cg_tol=1e-8, precision=PRECISION_MIXED, steps=80, contact=True):
+    """Two jittered n_side^3 blocks moving toward each other along x at
+    +-speed, gap_spacings lattice spacings apart (beyond the horizon, so no
+    bond joins them), implicit Euler, no gravity.  With contact, the PD-PD
+    contact force (distance 0.75 spacing) keeps them apart."""
+    rng = np.random.default_rng(seed)
+    g = _lattice(n_side, n_side, n_side).astype(np.float64)
+    a = g * spacing
+    b = g * spacing + np.array([(n_side - 1 + gap_spacings) * spacing, 0.0, 0.0])
+    n = 2 * g.shape[0]
+    pos = np.zeros((n, 4))
+    pos[:, :3] = np.vstack([a, b]) + rng.uniform(-jitter, jitter, (n, 3)) * spacing
+    vel = np.zeros((n, 4))
+    vel[: n // 2, 0] = speed
+    vel[n // 2:, 0] = -speed
+    act = np.full(n, ACTIVE, np.int32)
+    sim, run = _si_params(n, spacing, coeff, si_mass(spacing), s0, IMPLICIT_EULER, steps)
+    opt = default_options()
+    opt.precision = precision
+    opt.cg_relative_tolerance = cg_tol
+    opt.cg_max_iterations = 20000
+    opt.time_step_base = dt / 128.0
+    opt.bond_stiffness = si_stiffness(spacing)
+    opt.gravity[:] = (0.0, 0.0, 0.0)
+    opt.box_enabled = 0
+    opt.contact_enabled = 1 if contact else 0
+    opt.contact_distance = 0.75 * spacing
+    opt.contact_stiffness = 1e7
+    opt.contact_volume = 1.0
+    return Scene("two_blocks", sim, run, opt, pos, vel, act, steps, {"spacing": spacing, "seed": seed})
+
+
 def batched_scenes(count=64, n_min=4096, n_max=65536, seed=0, precision=PRECISION_MIXED, steps=100):
     """`count` impact bodies: particle counts log-uniform in [n_min, n_max],
     blocks and balls alternating at random, pd_kernel_coeff uniform in

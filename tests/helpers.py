@@ -40,6 +40,10 @@ def oracle_params(scene):
         p.sphere_v[k] = opt.sphere_velocity[k]
     p.sphere_radius = opt.sphere_radius
     p.sphere_k = opt.sphere_stiffness
+    p.contact_on = opt.contact_enabled
+    p.contact_dist = opt.contact_distance
+    p.contact_k = opt.contact_stiffness
+    p.contact_vol = opt.contact_volume
     return p
 
 

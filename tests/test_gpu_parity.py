@@ -174,3 +174,20 @@ def test_spmv_tiled_large_autotuned(pdgb, scenes):
     for path, sim in runs.items():
         assert same_sets(sim.alive_sets(), ora.alive_sets())
         assert rel_err(sim.get(pdgb.VAR_POSITION), ora.position) < MIXED_TOL, path
+
+
+@pytest.mark.parametrize("precision,tol", [(1, FP64_TOL), (0, MIXED_TOL)])
+def test_pd_pd_contact(pdgb, scenes, precision, tol):
+    """Two blocks collide: the PD-PD contact forces (collidePDParticles,
+    off in the reference build) against the oracle's brute-force pairs."""
+    sc = scenes.two_blocks(precision=precision)
+    sim, ora = _run_pair(pdgb, scenes, sc, 80, check_every=20)
+    assert rel_err(sim.get(pdgb.VAR_POSITION), ora.position) < tol
+    assert rel_err(sim.get(pdgb.VAR_VELOCITY), ora.velocity) < max(tol, 1e-7) * 100
+    # the contact changed the motion: without it the blocks pass into each other
+    free = scenes.make_simulator(scenes.two_blocks(precision=precision, contact=False))
+    free.makeReady()
+    free.advance(80)
+    x, xf = sim.get(pdgb.VAR_POSITION), free.get(pdgb.VAR_POSITION)
+    n = x.shape[0] // 2
+    assert x[:n, 0].max() < xf[:n, 0].max() - 0.2 * sc.info["spacing"]
