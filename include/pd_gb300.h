@@ -137,7 +137,8 @@ typedef struct pd_solver_options {
     /* mixed-precision SpMV path: 0 or 2 = per-bond gathers from global
      * memory; 1 = shared-memory tiles of 256 consecutive rows and their halos
      * (measured slower than the gathers at 1M particles; kept as an option).
-     * Either way lanes x unroll is measured at make_ready when n >= 20000. */
+     * Either way lanes x unroll is measured at make_ready when n >= 20000;
+     * pd_get_options reports the path in use (1 or 2). */
     int spmv_path;
     /* PD-PD contact (collectPDParticles / collidePDParticles,
      * src/core/simulator.cuh:606-768, compiled out in the reference): every

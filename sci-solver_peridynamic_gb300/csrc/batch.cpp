@@ -35,6 +35,7 @@ public:
     Engine* scene(int s) { return (s >= 0 && s < (int)eng_.size()) ? eng_[(size_t)s].get() : nullptr; }
     int count() const { return (int)eng_.size(); }
     pd_status make_ready();
+    pd_status relayout(int lanes, int unroll);
     pd_status advance(int nsteps);
     pd_status config(pd_batch_config* c) const;
     long long launches() const { return launches_; }
@@ -223,6 +224,15 @@ pd_status Batch::enqueue_step()
     return PD_OK;
 }
 
+// Orders every scene's bond slots for the (lanes, unroll) SpMV shape (on the
+// scenes' own streams, waited for before the batch's next launch).
+pd_status Batch::relayout(int lanes, int unroll)
+{
+    for (auto& e : eng_) e->relayout_bonds(lanes, fp64_ ? 1 : unroll);
+    for (auto& e : eng_) BCK(cudaStreamSynchronize(e->stream_), "relayout sync");
+    return PD_OK;
+}
+
 // Launch shape: SpMV lanes x unroll and rows per work item, timed on the
 // batch's own SpMV phase (y = A x over all scenes, which changes no state).
 pd_status Batch::tune()
@@ -240,6 +250,8 @@ pd_status Batch::tune()
         unroll_ = unroll_c.size() == 1 ? unroll_c[0] : 2;
         const int rows = rows_c.size() == 1 ? rows_c[0] : 128;
         grid_cg_ = std::max(1, batch_cg_blocks_per_sm(fp64_, lanes_, unroll_)) * sm_count_;
+        pd_status s = relayout(lanes_, unroll_);
+        if (s != PD_OK) return s;
         return build_items(rows);
     }
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -254,6 +266,8 @@ pd_status Batch::tune()
         for (int l : lanes_c) {
             for (int u : unroll_c) {
                 const int grid = std::max(1, batch_cg_blocks_per_sm(fp64_, l, u)) * sm_count_;
+                s = relayout(l, u);
+                if (s != PD_OK) return s;
                 BCK(cudaMemsetAsync(d_sync_, 0, sizeof(BatchSync), stream_), "reset barrier");
                 BCK(launch_batch_cg(fp64_, l, u, args(1), grid, stream_), "tune launch");
                 BCK(cudaEventRecord(e0, stream_), "event");
@@ -285,6 +299,8 @@ pd_status Batch::tune()
     grid_cg_ = std::max(1, batch_cg_blocks_per_sm(fp64_, lanes_, unroll_)) * sm_count_;
     tuned_ms_ = best / reps;
     autotuned_ = true;
+    pd_status s = relayout(lanes_, unroll_);
+    if (s != PD_OK) return s;
     return build_items(br);
 }
 

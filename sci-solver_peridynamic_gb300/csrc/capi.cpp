@@ -73,6 +73,13 @@ pd_status pd_create(const pd_sim_params* sim, const pd_run_params* run, const pd
         g_create_error = "contact distance and volume must be positive";
         return PD_ERR_INVALID_ARGUMENT;
     }
+    if (o.spmv_path < 0 || o.spmv_path > 2 ||
+        (o.lanes_per_particle != 0 && o.lanes_per_particle != 4 && o.lanes_per_particle != 8 &&
+         o.lanes_per_particle != 16 && o.lanes_per_particle != 32) ||
+        (o.spmv_unroll != 0 && o.spmv_unroll != 1 && o.spmv_unroll != 2 && o.spmv_unroll != 4)) {
+        g_create_error = "SpMV options: spmv_path 0..2, lanes 0/4/8/16/32, unroll 0/1/2/4";
+        return PD_ERR_INVALID_ARGUMENT;
+    }
     pd_handle* h = new (std::nothrow) pd_handle{nullptr};
     if (!h) return PD_ERR_OUT_OF_MEMORY;
     h->eng = new (std::nothrow) pdgb::Engine(*sim, *run, o);

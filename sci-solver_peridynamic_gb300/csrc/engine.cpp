@@ -378,6 +378,8 @@ pd_status Engine::tune_spmv()
     }
     if (cand.empty()) cand.push_back({0, fixed_lanes ? fixed_lanes : 8, fixed_unroll ? fixed_unroll : 1});
     auto apply = [&](const Cand& c) {
+        if (c.tiled) relayout_bonds(1, 1);
+        else relayout_bonds(c.g, c.u);
         L_.tiled = c.tiled;
         L_.lanes = c.g;
         L_.unroll = c.u;
@@ -403,14 +405,16 @@ pd_status Engine::tune_spmv()
     float best = 1e30f;
     Cand best_c = cand[0];
     // each candidate: one warm-up launch, then the best of three timed pairs
+    // of the CG iteration's product (y = A p with <p, y>; the scalars it
+    // writes are reset by the first solve)
     for (const auto& c : cand) {
         apply(c);
-        launch_spmv(fp64_, false, P, S_, L_, stream_);
+        launch_spmv(fp64_, true, P, S_, L_, stream_);
         ++launches_;
         float ms_c = 1e30f;
         for (int rep = 0; rep < 3; ++rep) {
             CK(cudaEventRecord(e0, stream_), "event");
-            for (int k = 0; k < 2; ++k) launch_spmv(fp64_, false, P, S_, L_, stream_);
+            for (int k = 0; k < 2; ++k) launch_spmv(fp64_, true, P, S_, L_, stream_);
             CK(cudaEventRecord(e1, stream_), "event");
             CK(cudaEventSynchronize(e1), "tune sync");
             float ms = 0.f;
@@ -428,6 +432,18 @@ pd_status Engine::tune_spmv()
     apply(best_c);
     tuned_ms_ = best;
     return PD_OK;
+}
+
+void Engine::relayout_bonds(int g, int u)
+{
+    if (fp64_ || n_ <= 0) return;
+    if (u <= 1) g = 1, u = 1;
+    if (g == lay_g_ && u == lay_u_) return;
+    const int grid = (int)std::min<long long>(((long long)n_ + kBlock - 1) / kBlock, (long long)sm_count_ * 8);
+    launch_bond_relayout(S_, std::max(grid, 1), lay_g_, lay_u_, g, u, stream_);
+    ++launches_;
+    lay_g_ = g;
+    lay_u_ = u;
 }
 
 StepParams Engine::step_params() const

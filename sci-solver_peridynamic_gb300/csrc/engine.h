@@ -60,6 +60,8 @@ private:
     StepParams step_params() const;
     int grid_for_rows(int lanes, int blocks_per_sm) const;
     pd_status tune_spmv();
+    // mixed mode: reorders every row's live bonds for the (g, u) SpMV shape
+    void relayout_bonds(int g, int u);
     pd_status ws_prepare();                 // allocates the warm-start state on first use
     void ws_free();
     bool ws_features_needed() const;
@@ -109,6 +111,7 @@ private:
     LaunchCfg L_{};
     StepParams last_params_{};   // constants of the latest step (the operator's time step)
     float tuned_ms_ = 0.f;       // SpMV time of the autotuned variant
+    int lay_g_ = 1, lay_u_ = 1;  // SpMV shape the bond slots are ordered for (u = 1: build order)
     // learned warm start
     WsState W_{};
     MlpDev mlp_{};

@@ -158,6 +158,10 @@ void launch_cg_xpby(bool fp64, const StepParams& P, const DeviceState& S, const 
 void launch_update(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
 void launch_refresh(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
 void launch_bond_geometry(const DeviceState& S, int grid, cudaStream_t st);
+// mixed mode: live bonds of each row reordered from the (g_from, u_from)
+// SpMV shape's slot order to (g_to, u_to)'s (u = 1: build order)
+void launch_bond_relayout(const DeviceState& S, int grid, int g_from, int u_from, int g_to, int u_to,
+                          cudaStream_t st);
 // Shared-memory tile SpMV (tiles.cu).  build_tiles fills halo / halo_ptr /
 // tile_info / lidx of S (allocating them) for tiles of S.tile_rows rows and
 // returns the largest halo in *max_halo.

@@ -42,8 +42,12 @@ __global__ void __launch_bounds__(kBlock) k_force(StepParams P, DeviceState S)
 // alpha = rz / <p, A p> and the launch is skipped once the CG has finished;
 // with `dot_out` set the result is also stored there.
 // U: bonds each lane loads before it computes (memory-level parallelism).
+// Mixed mode keeps 4 blocks (32 warps) resident per SM: the kernel is
+// latency-bound on its gathers, and at 1M particles 64 registers and 4
+// blocks beat 73 registers and 3 blocks by 7 % (254 vs 272 us per product).
+constexpr int kSpmvMinBlocks = 4;
 template <int G, bool FP64, bool DOT, int U>
-__global__ void __launch_bounds__(kBlock) k_spmv(StepParams P, DeviceState S, const void* __restrict__ in_,
+__global__ void __launch_bounds__(kBlock, FP64 ? 1 : kSpmvMinBlocks) k_spmv(StepParams P, DeviceState S, const void* __restrict__ in_,
                                                   void* __restrict__ out_, ReduceSlot slot, CgScalars* cg,
                                                   double* dot_out)
 {
@@ -161,6 +165,52 @@ __global__ void __launch_bounds__(kBlock) k_bond_geometry(int n, DeviceState S)
 void launch_bond_geometry(const DeviceState& S, int grid, cudaStream_t st)
 {
     k_bond_geometry<<<grid, kBlock, 0, st>>>(S.n, S);
+}
+
+// Reorders the live bonds of each row for a (lanes G, unroll U) SpMV shape.
+// The SpMV's lane k loads U consecutive slots 16-byte-wise (slots b*GU + kU +
+// u, u < U) and gathers their neighbours as U instructions; so that the
+// neighbours gathered by one instruction are the row's G consecutive bonds of
+// the build order (the build scans neighbour cells, so consecutive bonds are
+// close in memory), every full block of GU live slots stores build-order bond
+// uG + k at slot kU + u.  `from` undoes a previous shape's order first.  Only
+// whole blocks inside [0, cnt) move, so the live set of every row is unchanged.
+template <typename T>
+__device__ __forceinline__ void permute_block(T* a, int G, int U, bool to_shape)
+{
+    T t[128];
+    const int B = G * U;
+    for (int i = 0; i < B; ++i) t[i] = a[i];
+    for (int k = 0; k < G; ++k)
+        for (int u = 0; u < U; ++u) {
+            if (to_shape) a[k * U + u] = t[u * G + k];
+            else a[u * G + k] = t[k * U + u];
+        }
+}
+
+__global__ void __launch_bounds__(kBlock) k_bond_relayout(int n, DeviceState S, int g_from, int u_from, int g_to,
+                                                          int u_to)
+{
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const int rs = S.row_ptr[p], cn = S.cnt[p];
+        for (int pass = 0; pass < 2; ++pass) {
+            const int G = pass == 0 ? g_from : g_to, U = pass == 0 ? u_from : u_to;
+            if (U <= 1 || G * U > 128) continue;
+            const int B = G * U;
+            for (int b = 0; b + B <= cn; b += B) {
+                permute_block(S.col + rs + b, G, U, pass == 1);
+                permute_block(S.inv_d0 + rs + b, G, U, pass == 1);
+                permute_block(S.d0sq + rs + b, G, U, pass == 1);
+                if (S.lidx) permute_block(S.lidx + rs + b, G, U, pass == 1);
+            }
+        }
+    }
+}
+
+void launch_bond_relayout(const DeviceState& S, int grid, int g_from, int u_from, int g_to, int u_to,
+                          cudaStream_t st)
+{
+    k_bond_relayout<<<grid, kBlock, 0, st>>>(S.n, S, g_from, u_from, g_to, u_to);
 }
 
 // ---- launchers ------------------------------------------------------------------

@@ -449,16 +449,35 @@ __device__ __forceinline__ void spmv_row(const StepParams& P, const DeviceState&
         const float sup = (float)P.sup;
         const float4* __restrict__ xs4 = S.xs4;
         const float4* __restrict__ in32 = (const float4*)in;
-        for (int j0 = lane; j0 < cn; j0 += G * U) {
+        // lane k takes the U consecutive slots j0 .. j0 + U - 1 of each block
+        // of G*U (one 8- or 16-byte load per stream; the bond order of the
+        // slots is arranged by launch_bond_relayout for this shape).  Rows
+        // start 32-byte aligned and hold a multiple of 8 slots, so the vector
+        // loads stay inside the row.
+        for (int j0 = lane * U; j0 < cn; j0 += G * U) {
             // issue every load of U bonds before any arithmetic
             int qq[U];
             float id0[U];
+            if constexpr (U == 4) {
+                const int4 c4 = __ldcs((const int4*)(S.col + rs + j0));
+                const float4 d4 = __ldcs((const float4*)(S.inv_d0 + rs + j0));
+                qq[0] = c4.x; qq[1] = c4.y; qq[2] = c4.z; qq[3] = c4.w;
+                id0[0] = d4.x; id0[1] = d4.y; id0[2] = d4.z; id0[3] = d4.w;
+            } else if constexpr (U == 2) {
+                const int2 c2 = __ldcs((const int2*)(S.col + rs + j0));
+                const float2 d2 = __ldcs((const float2*)(S.inv_d0 + rs + j0));
+                qq[0] = c2.x; qq[1] = c2.y;
+                id0[0] = d2.x; id0[1] = d2.y;
+            } else {
 #pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int j = j0 + u * G;
-                qq[u] = j < cn ? __ldcs(S.col + rs + j) : -1;
-                id0[u] = j < cn ? __ldcs(S.inv_d0 + rs + j) : 0.f;
+                for (int u = 0; u < U; ++u) {
+                    qq[u] = __ldcs(S.col + rs + j0 + u);
+                    id0[u] = __ldcs(S.inv_d0 + rs + j0 + u);
+                }
             }
+#pragma unroll
+            for (int u = 1; u < U; ++u)
+                if (j0 + u >= cn) qq[u] = -1;
             float4 Xq[U], Wq[U];
 #pragma unroll
             for (int u = 0; u < U; ++u) {

@@ -130,6 +130,18 @@ def test_no_gpu_fails_loudly(pdgb, scenes):
     assert e.value.status == 5
 
 
+@pytest.mark.parametrize("field,value", [("spmv_path", 3), ("lanes_per_particle", 6), ("spmv_unroll", 3)])
+def test_invalid_spmv_options_rejected(pdgb, scenes, field, value):
+    """Option checks run before any device call: an unsupported SpMV shape is
+    an invalid argument (status 1), not a silent default."""
+    sc = scenes.reference_block(n_side=3)
+    setattr(sc.opt, field, value)
+    with pytest.raises(pdgb.PdError) as e:
+        scenes.make_simulator(sc)
+    assert e.value.status == 1
+    assert "SpMV options" in str(e.value)
+
+
 def test_batch_scene_sizes():
     """The batched workload: 64 bodies, log-uniform sizes in [4096, 65536]
     (about 1.4M particles), horizons 4/5/6, impact speeds 1-10 m/s."""
