@@ -392,35 +392,67 @@ def _timed(stream_handle, fn, local):
     return ev0.elapsed_time(ev1)
 
 
-def run_batched(args):
-    """64 independent scenes (log-uniform 4096..65536 particles, horizons
-    4/5/6, impacts 1-10 m/s) stepped together by the batch API; compared with
-    the same scenes stepped one pd_handle at a time."""
-    import torch
-    pkg = importlib.import_module(PKG_NAME)
-    scenes = importlib.import_module(PKG_NAME + ".scenes")
-    local = 0
-    torch.cuda.set_device(local)
-    lst = scenes.batched_scenes(count=64, seed=0)
-    n_total = sum(sc.n for sc in lst)
-    b = pkg.Batch(local)
+def _batch_arm(pkg, scenes, lst, local, args, warm_start, params=None):
+    """One timed run of the batch: returns (ms, stats dict, config, clocks)."""
+    o = pkg.BatchOptions()
+    pkg.library().pd_batch_options_default(o)
+    o.warm_start = warm_start
+    b = pkg.Batch(local, o)
     for sc in lst:
         scenes.add_to_batch(b, sc)
     b.makeReady()
+    if params is not None:
+        b.ws_set_params(params)
     cfg = b.config()
     b.advance(args.warmup)
-    it0 = sum(b.stats(k).total_cg_iterations for k in range(len(lst)))
+    k_all = range(len(lst))
+    it0 = sum(b.stats(k).total_cg_iterations for k in k_all)
+    kept0 = sum(b.stats(k).ws_guesses_kept for k in k_all)
     l0 = b.launch_count()
     sampler = ClockSampler(local)
     sampler.start()
     ms = _timed(b.stream_handle(), lambda: b.advance(args.steps), local)
     clocks = sampler.stop()
-    launches = b.launch_count() - l0
-    iters = sum(b.stats(k).total_cg_iterations for k in range(len(lst))) - it0
-    bonds = sum(b.stats(k).bonds_alive for k in range(len(lst)))
-    max_iters = max(b.stats(k).last_cg_iterations for k in range(len(lst)))
+    st = {
+        "launches": b.launch_count() - l0,
+        "iters": sum(b.stats(k).total_cg_iterations for k in k_all) - it0,
+        "kept": sum(b.stats(k).ws_guesses_kept for k in k_all) - kept0,
+        "bonds": sum(b.stats(k).bonds_alive for k in k_all),
+        "max_iters": max(b.stats(k).last_cg_iterations for k in k_all),
+        "converged": all(b.stats(k).cg_converged for k in k_all),
+        "positions": [b.get(k, pkg.VAR_POSITION) for k in k_all],
+        "alive": [sum(len(r) for r in b.alive_sets(k)) for k in k_all],
+    }
     b.close()
-    # the same scenes, one handle each, stepped in turn
+    return ms, st, cfg, clocks
+
+
+def run_batched(args):
+    """64 independent scenes (log-uniform 4096..65536 particles, horizons
+    4/5/6, impacts 1-10 m/s) stepped together by the batch API with the
+    learned warm start on (a network trained on the GPU from plain-solver
+    data of four other scenes of the same family), beside the plain batch and
+    the same scenes stepped one pd_handle at a time."""
+    import numpy as np
+    import torch
+    pkg = importlib.import_module(PKG_NAME)
+    scenes = importlib.import_module(PKG_NAME + ".scenes")
+    ws = importlib.import_module(PKG_NAME + ".warmstart")
+    local = 0
+    torch.cuda.set_device(local)
+    lst = scenes.batched_scenes(count=64, seed=0)
+    n_total = sum(sc.n for sc in lst)
+    # training data from four scenes of another draw (plain solver), 40 steps each
+    t0 = time.perf_counter()
+    train_lst = scenes.batched_scenes(count=4, seed=1)
+    X, T = ws.collect(lambda k: train_lst[k], seeds=range(len(train_lst)), steps=40, samples_per_step=256)
+    params, loss = ws.train(X, T, iterations=2000)
+    t_train = time.perf_counter() - t0
+    ms_p, st_p, cfg_p, _ = _batch_arm(pkg, scenes, lst, local, args, 0)
+    ms, st, cfg, clocks = _batch_arm(pkg, scenes, lst, local, args, 1, params)
+    pos_diff = max(float(np.abs(a[:, :3] - b[:, :3]).max() / max(np.abs(b[:, :3]).max(), 1e-300))
+                   for a, b in zip(st["positions"], st_p["positions"]))
+    # the same scenes, one handle each, stepped in turn (plain warm start)
     sims = []
     for sc in lst:
         s = scenes.make_simulator(sc, local)
@@ -437,33 +469,46 @@ def run_batched(args):
     t_seq = time.perf_counter() - t0
     for s in sims:
         s.close()
+    bonds = st["bonds"]
     spmv_bytes = 4.0 * bonds + 64.0 * n_total
     achieved = spmv_bytes / (cfg.tuned_spmv_ms / 1e3) / 1e9 if cfg.tuned_spmv_ms > 0 else None
     peak, peak_kind = measured_peak_hbm()
     value = args.steps / (ms / 1e3)
     result = {
-        "metric": "batched implicit steps/s (64 scenes, every scene advances one step)",
+        "metric": "batched implicit steps/s (64 scenes, every scene advances one step), learned warm start on",
         "value": round(value, 4), "unit": "steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32 force/SpMV, f64 stretch test + master state, double-float->f64 dots",
+        "dtype": "f32 force/SpMV, f64 stretch test + master state, double-float->f64 dots, bf16 MLP (f32 accum)",
         "data": "synthetic (seeded jittered blocks and balls)",
         "config": {"workload": "64 impact bodies, %d particles in total (log-uniform 4096..65536 each), horizons "
                                "4/5/6 r, impacts 1-10 m/s, blocks implicit Euler dt=1e-4, balls Newmark dt=5e-5, "
-                               "CG rel 1e-6" % n_total,
+                               "CG rel 1e-6, learned warm start" % n_total,
                    "particles": n_total, "bonds_alive": int(bonds), "scenes": len(lst),
-                   "cg_iterations_per_step_all_scenes": round(iters / args.steps, 1),
-                   "cg_iterations_last_step_max": int(max_iters),
+                   "cg_iterations_per_step_all_scenes": round(st["iters"] / args.steps, 1),
+                   "cg_iterations_last_step_max": int(st["max_iters"]),
+                   "learned_guesses_kept": "%d of %d scene-steps" % (st["kept"], args.steps * len(lst)),
+                   "network": "trained on the GPU from %d plain-solver pairs of 4 other scenes in %.1f s "
+                              "(loss %.4g)" % (X.shape[0], t_train, loss),
                    "launch_shape": {"lanes": cfg.lanes_per_particle, "unroll": cfg.spmv_unroll,
                                     "item_rows": cfg.item_rows, "work_items": cfg.work_items,
                                     "grid_pre": cfg.grid_pre, "grid_cg": cfg.grid_cg,
                                     "autotuned": bool(cfg.autotuned)},
                    "l2": "inputs larger than L2 (bond columns + 1/d0 %.0f MB)" % (8 * bonds / 1e6)},
-        "gpu_launches": int(launches),
+        "gpu_launches": int(st["launches"]),
         "scene_steps_per_s": round(value * len(lst), 2),
         "particle_steps_per_s": round(value * n_total, 1),
+        "plain_warm_start": {"value": round(args.steps / (ms_p / 1e3), 4), "unit": "steps/s",
+                             "cg_iterations_per_step_all_scenes": round(st_p["iters"] / args.steps, 1),
+                             "what": "the same batch with the previous solution as the CG guess (the reference's)"},
+        "learned_vs_plain": {"cg_iteration_ratio": round(st_p["iters"] / max(st["iters"], 1), 4),
+                             "speed_ratio": round(ms_p / ms, 4),
+                             "alive_bonds_identical": st["alive"] == st_p["alive"],
+                             "max_position_difference_rel": pos_diff,
+                             "all_cg_converged": bool(st["converged"] and st_p["converged"])},
         "unbatched": {"value": round(args.steps / t_seq, 4), "unit": "steps/s",
-                      "what": "the same 64 scenes as 64 pd_handles, pd_advance(1) each in turn, wall clock"},
+                      "what": "the same 64 scenes as 64 pd_handles (plain warm start), pd_advance(1) each in turn, "
+                              "wall clock"},
         "roofline": {"kernel": "SpMV phase of k_batch_cg over all scenes (autotuner timing)", "bound": "hbm",
                      "achieved": round(achieved, 1) if achieved else None, "peak": peak, "peak_kind": peak_kind,
                      "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None, "traffic": None,

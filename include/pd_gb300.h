@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define PD_GB300_ABI_VERSION 1
+#define PD_GB300_ABI_VERSION 2
 
 typedef enum pd_status {
     PD_OK = 0,
@@ -417,6 +417,14 @@ typedef struct pd_batch_options {
     int spmv_unroll;          /* 2 or 4, 0 = autotune */
     int item_rows;            /* rows per work item: 64..4096, 0 = autotune */
     int use_graph;            /* 1 (default): replay each step from a CUDA graph */
+    /* CG initial guess of every scene (mixed precision only; the scenes'
+     * own warm_start option is not used in a batch): 0 (default) = the
+     * previous solution, as the reference; 1 = the previous solution plus the
+     * learned correction of the network set by pd_batch_ws_set_params (one
+     * network for all scenes, run once per step over the rows of every
+     * scene), kept only where its residual is not larger -- the CG still
+     * runs to each scene's tolerance.  No reference counterpart. */
+    int warm_start;
 } pd_batch_options;
 
 /* The launch shape in use after pd_batch_make_ready. */
@@ -429,6 +437,7 @@ typedef struct pd_batch_config {
     int grid_cg;              /* blocks of the CG launch */
     int autotuned;            /* 1 when the shape was measured, 0 when fixed/default */
     double tuned_spmv_ms;     /* SpMV phase time of the chosen shape (autotuned only) */
+    int warm_start;           /* the batch option in use */
 } pd_batch_config;
 
 pd_status pd_batch_options_default(pd_batch_options* opt);
@@ -442,6 +451,11 @@ pd_status pd_batch_add_scene(pd_batch* b, const pd_sim_params* sim, const pd_run
 pd_status pd_batch_set_particles(pd_batch* b, int scene, const double* pos4, const double* vel4,
                                  const int32_t* activity, int n);
 pd_status pd_batch_set_stretch_limits(pd_batch* b, int scene, const double* s0, int n);
+/* Parameters of the warm-start network (pd_mlp_param_count() floats, as
+ * pd_ws_set_params), before or after pd_batch_make_ready; without a call the
+ * network starts from pd_mlp_init's seed-1 parameters.  No reference
+ * counterpart. */
+pd_status pd_batch_ws_set_params(pd_batch* b, const float* params, size_t count);
 /* pd_make_ready of every scene, then work items, launch shape and graph. */
 pd_status pd_batch_make_ready(pd_batch* b);
 /* nsteps steps of every scene (a scene whose CG failed stops, as pd_advance). */

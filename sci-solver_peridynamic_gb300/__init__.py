@@ -131,16 +131,17 @@ _lib = None
 
 
 class BatchOptions(C.Structure):
-    """pd_batch_options: SpMV launch shape and item size (0 = autotune), graph replay."""
+    """pd_batch_options: SpMV launch shape and item size (0 = autotune), graph
+    replay, learned warm start (1: on, mixed precision)."""
     _fields_ = [("lanes_per_particle", C.c_int), ("spmv_unroll", C.c_int), ("item_rows", C.c_int),
-                ("use_graph", C.c_int)]
+                ("use_graph", C.c_int), ("warm_start", C.c_int)]
 
 
 class BatchConfig(C.Structure):
     """pd_batch_config: the launch shape in use."""
     _fields_ = [("lanes_per_particle", C.c_int), ("spmv_unroll", C.c_int), ("item_rows", C.c_int),
                 ("work_items", C.c_int), ("grid_pre", C.c_int), ("grid_cg", C.c_int), ("autotuned", C.c_int),
-                ("tuned_spmv_ms", C.c_double)]
+                ("tuned_spmv_ms", C.c_double), ("warm_start", C.c_int)]
 
 
 def library(build_if_missing: bool = True):
@@ -219,6 +220,7 @@ def library(build_if_missing: bool = True):
         "pd_batch_set_particles": (st, [vp, C.c_int, P(C.c_double), P(C.c_double), P(C.c_int32), C.c_int]),
         "pd_batch_set_stretch_limits": (st, [vp, C.c_int, P(C.c_double), C.c_int]),
         "pd_batch_make_ready": (st, [vp]),
+        "pd_batch_ws_set_params": (st, [vp, P(C.c_float), C.c_size_t]),
         "pd_batch_advance": (st, [vp, C.c_int]),
         "pd_batch_scene_count": (st, [vp, P(C.c_int)]),
         "pd_batch_scene_offsets": (st, [vp, P(C.c_int64), C.c_int]),
@@ -594,6 +596,11 @@ class Batch:
             _bcheck(self.lib.pd_batch_set_stretch_limits(self.h, k.value, s.ctypes.data_as(dp), n), self.h)
         self.sizes.append(n)
         return k.value
+
+    def ws_set_params(self, params):
+        """Parameters of the batch's warm-start network (options.warm_start = 1)."""
+        p = np.ascontiguousarray(params, np.float32)
+        _bcheck(self.lib.pd_batch_ws_set_params(self.h, _fp(p), p.size), self.h)
 
     def makeReady(self):
         _bcheck(self.lib.pd_batch_make_ready(self.h), self.h)

@@ -8,6 +8,7 @@
 // device records are copied back into the scenes' Engine objects, so every
 // per-scene query (pd_batch_get, pd_batch_get_stats) answers as a pd_handle.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -38,6 +39,7 @@ public:
     pd_status relayout(int lanes, int unroll);
     pd_status advance(int nsteps);
     pd_status config(pd_batch_config* c) const;
+    pd_status ws_set_params(const float* params, size_t count);
     long long launches() const { return launches_; }
     cudaStream_t stream() const { return stream_; }
     pd_status synchronize();
@@ -54,6 +56,7 @@ private:
     pd_status tune();
     pd_status build_graph();
     pd_status pull_state();
+    pd_status ws_setup();
 
     int device_;
     pd_batch_options opt_;
@@ -79,6 +82,14 @@ private:
     double tuned_ms_ = 0.0;
     cudaGraph_t graph_ = nullptr;
     cudaGraphExec_t exec_ = nullptr;
+    // learned warm start: one network for all scenes, run once per step over
+    // the concatenated feature rows of every scene
+    std::vector<float> ws_params_;
+    MlpDev mlp_{};
+    MlpWork mlp_work_{};
+    __nv_bfloat16* d_feat_ = nullptr;
+    float* d_ws_y_ = nullptr;
+    long long total_rows_ = 0;
     long long launches_ = 0;
     std::string err_;
 };
@@ -103,6 +114,12 @@ void Batch::free_device()
     cudaFree(d_partials_);
     cudaFree(d_counters_);
     cudaFree(d_sync_);
+    cudaFree(d_feat_);
+    cudaFree(d_ws_y_);
+    d_feat_ = nullptr;
+    d_ws_y_ = nullptr;
+    mlp_work_free(&mlp_work_);
+    mlp_free(&mlp_);
     d_desc_ = nullptr;
     d_run_ = nullptr;
     d_items_ = nullptr;
@@ -184,7 +201,7 @@ pd_status Batch::build_items(int item_rows)
         d_partials_ = nullptr;
         items_cap_ = 0;
         BCK(cudaMalloc((void**)&d_items_, sizeof(WorkItem) * n), "alloc items");
-        BCK(cudaMalloc((void**)&d_partials_, sizeof(double) * n), "alloc partials");
+        BCK(cudaMalloc((void**)&d_partials_, sizeof(double) * 3 * n), "alloc partials");
         items_cap_ = n;
     }
     if (!items_.empty())
@@ -211,6 +228,7 @@ BatchArgs Batch::args(int tune_reps) const
     A.max_rounds = 66;
     A.max_cg_iters = max_cg_iters_;
     A.tune_reps = tune_reps;
+    A.warm_start = opt_.warm_start;
     return A;
 }
 
@@ -220,7 +238,73 @@ pd_status Batch::enqueue_step()
     BCK(cudaMemsetAsync(d_sync_, 0, sizeof(BatchSync), stream_), "reset barrier");
     BCK(cudaMemsetAsync(d_counters_, 0, sizeof(unsigned) * eng_.size(), stream_), "reset counters");
     BCK(launch_batch_pre(fp64_, A, grid_pre_, stream_), "k_batch_pre launch");
+    if (opt_.warm_start && total_rows_ > 0) {
+        mlp_forward(mlp_, d_feat_, (int)total_rows_, mlp_work_, d_ws_y_, stream_);
+        BCK(cudaGetLastError(), "network launch");
+    }
     BCK(launch_batch_cg(fp64_, lanes_, unroll_, A, grid_cg_, stream_), "k_batch_cg launch");
+    return PD_OK;
+}
+
+// Learned warm start: every scene's warm-start state (without a network of
+// its own), the batch's feature and output rows, and the network.
+pd_status Batch::ws_setup()
+{
+    total_rows_ = 0;
+    for (auto& e : eng_) total_rows_ += e->n_;
+    if (total_rows_ >= (1LL << 31)) {
+        err_ = "learned warm start: more than 2^31 particles in the batch";
+        return PD_ERR_INVALID_ARGUMENT;
+    }
+    for (size_t s = 0; s < eng_.size(); ++s) {
+        Engine& e = *eng_[s];
+        pd_status st = e.ws_prepare(false);
+        if (st != PD_OK) {
+            err_ = "scene " + std::to_string(s) + ": " + e.error();
+            return st;
+        }
+    }
+    const size_t rows = (size_t)std::max<long long>(total_rows_, 1);
+    BCK(cudaMalloc((void**)&d_feat_, sizeof(__nv_bfloat16) * kMlpIn * rows), "alloc features");
+    BCK(cudaMalloc((void**)&d_ws_y_, sizeof(float) * kMlpOutPad * rows), "alloc network output");
+    BCK(cudaMemsetAsync(d_feat_, 0, sizeof(__nv_bfloat16) * kMlpIn * rows, stream_), "memset features");
+    BCK(mlp_alloc(&mlp_, false), "alloc network");
+    BCK(mlp_work_alloc(&mlp_work_, (long long)rows, false), "alloc network rows");
+    if (ws_params_.size() != mlp_param_count()) {
+        ws_params_.assign(mlp_param_count(), 0.f);
+        mlp_init_params(ws_params_.data(), 1u);
+    }
+    BCK(cudaMemcpyAsync(mlp_.params, ws_params_.data(), sizeof(float) * ws_params_.size(), cudaMemcpyHostToDevice,
+                        stream_), "upload network");
+    mlp_refresh_bf16(mlp_, stream_);
+    BCK(cudaGetLastError(), "network set-up");
+    long long off = 0;
+    for (size_t s = 0; s < eng_.size(); ++s) {
+        Engine& e = *eng_[s];
+        SceneDesc& D = h_desc_[s];
+        D.W = e.W_;
+        D.W.features = d_feat_ + (size_t)off * kMlpIn;
+        D.rsave = e.ws_rsave_;
+        D.ws_y = d_ws_y_ + (size_t)off * kMlpOutPad;
+        off += e.n_;
+    }
+    return PD_OK;
+}
+
+pd_status Batch::ws_set_params(const float* params, size_t count)
+{
+    if (!params || count != mlp_param_count()) {
+        err_ = "ws_set_params: expected pd_mlp_param_count() values";
+        return PD_ERR_INVALID_ARGUMENT;
+    }
+    ws_params_.assign(params, params + count);
+    if (mlp_.params) {
+        BCK(cudaSetDevice(device_), "cudaSetDevice");
+        BCK(cudaMemcpyAsync(mlp_.params, ws_params_.data(), sizeof(float) * count, cudaMemcpyHostToDevice, stream_),
+            "upload network");
+        mlp_refresh_bf16(mlp_, stream_);
+        BCK(cudaStreamSynchronize(stream_), "batch sync");
+    }
     return PD_OK;
 }
 
@@ -343,6 +427,10 @@ pd_status Batch::make_ready()
         }
     }
     fp64_ = eng_[0]->fp64_;
+    if (opt_.warm_start && fp64_) {
+        err_ = "the learned warm start needs mixed precision";
+        return PD_ERR_INVALID_ARGUMENT;
+    }
     const size_t ns = eng_.size();
     h_desc_.assign(ns, SceneDesc{});
     h_run_.assign(ns, SceneRun{});
@@ -374,6 +462,10 @@ pd_status Batch::make_ready()
         R.cs = e.clock_scale_;
         R.sim_time = e.sim_time_;
         max_cg_iters_ = std::max(max_cg_iters_, e.opt_.cg_max_iterations + 1);
+    }
+    if (opt_.warm_start) {
+        pd_status st = ws_setup();
+        if (st != PD_OK) return st;
     }
     BCK(cudaMalloc((void**)&d_desc_, sizeof(SceneDesc) * ns), "alloc scenes");
     BCK(cudaMalloc((void**)&d_run_, sizeof(SceneRun) * ns), "alloc run");
@@ -419,6 +511,18 @@ pd_status Batch::pull_state()
         e.retries_ = R.retries;
         e.last_params_ = h_desc_[s].P;
     }
+    if (opt_.warm_start) {
+        std::vector<CgScalars> sc(ns);
+        for (size_t s = 0; s < ns; ++s)
+            BCK(cudaMemcpyAsync(&sc[s], eng_[s]->S_.sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, stream_),
+                "read CG scalars");
+        BCK(cudaStreamSynchronize(stream_), "batch sync");
+        for (size_t s = 0; s < ns; ++s) {
+            Engine& e = *eng_[s];
+            e.ws_kept_ = sc[s].ws_kept;
+            e.last_ws_ratio_ = sc[s].rz_plain > 0 ? std::sqrt(sc[s].rz_learned / sc[s].rz_plain) : 0.0;
+        }
+    }
     if (sync.error) {
         ready_ = false;
         err_ = "batch step: a grid barrier wait timed out";
@@ -448,7 +552,7 @@ pd_status Batch::advance(int nsteps)
             pd_status s = enqueue_step();
             if (s != PD_OK) return s;
         }
-        launches_ += 2;
+        launches_ += 2 + (opt_.warm_start ? 6 : 0);   // + the network's 3 GEMMs and 3 bias/activation passes
     }
     return pull_state();
 }
@@ -464,6 +568,7 @@ pd_status Batch::config(pd_batch_config* c) const
     c->grid_cg = grid_cg_;
     c->autotuned = autotuned_ ? 1 : 0;
     c->tuned_spmv_ms = tuned_ms_;
+    c->warm_start = opt_.warm_start;
     return PD_OK;
 }
 
@@ -514,8 +619,8 @@ pd_status pd_batch_create(int device, const pd_batch_options* opt, pd_batch** ou
     else pd_batch_options_default(&o);
     if ((o.lanes_per_particle != 0 && o.lanes_per_particle != 4 && o.lanes_per_particle != 8) ||
         (o.spmv_unroll != 0 && o.spmv_unroll != 2 && o.spmv_unroll != 4) ||
-        (o.item_rows != 0 && (o.item_rows < 64 || o.item_rows > 4096))) {
-        g_batch_error = "batch options: lanes 0/4/8, unroll 0/2/4, item_rows 0 or 64..4096";
+        (o.item_rows != 0 && (o.item_rows < 64 || o.item_rows > 4096)) || (o.warm_start != 0 && o.warm_start != 1)) {
+        g_batch_error = "batch options: lanes 0/4/8, unroll 0/2/4, item_rows 0 or 64..4096, warm_start 0/1";
         return PD_ERR_INVALID_ARGUMENT;
     }
     pd_batch* h = new (std::nothrow) pd_batch{nullptr};
@@ -584,6 +689,12 @@ pd_status pd_batch_set_stretch_limits(pd_batch* b, int scene, const double* s0, 
     s = e->set_stretch(s0, n);
     if (s != PD_OK) b->b->set_error(e->error());
     return s;
+}
+
+pd_status pd_batch_ws_set_params(pd_batch* b, const float* params, size_t count)
+{
+    if (!b || !b->b) return PD_ERR_INVALID_ARGUMENT;
+    return b->b->ws_set_params(params, count);
 }
 
 pd_status pd_batch_make_ready(pd_batch* b)

@@ -13,6 +13,7 @@
 // is read through the coherent load path, never the read-only one.
 #include "batch.h"
 #include "step_rows.cuh"
+#include "warmstart_rows.cuh"
 
 namespace pdgb {
 
@@ -108,6 +109,58 @@ __device__ __forceinline__ void item_reduce(Acc acc, const BatchArgs& A, int ite
         for (int i = 0; i < (int)(blockDim.x >> 5); ++i) total += warp_sums[i];
         A.counters[s] = 0u;
         fin(total);
+        __threadfence();
+    }
+}
+
+// item_reduce for three sums at once (the learned warm start's RMS scales):
+// partial k of item i lives at partials[k * n_items + i]; one arrival count.
+template <typename Fin>
+__device__ __forceinline__ void item_reduce3(const DotAcc32 (&acc)[3], const BatchArgs& A, int item,
+                                             const SceneConst& C, int s, Fin fin)
+{
+    __shared__ double warp_sums[3][kBlock / 32];
+    __shared__ bool is_last;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double w = warp_total(acc[k]);
+        if (lane == 0) warp_sums[k][warp] = w;
+    }
+    __syncthreads();
+    const int count = C.item_end - C.item_begin;
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < 3; ++k) {
+            double t = 0.0;
+            for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += warp_sums[k][i];
+            A.partials[(size_t)k * A.n_items + item] = t;
+        }
+        __threadfence();
+        const unsigned prev = atomicAdd(A.counters + s, 1u);
+        is_last = (prev == (unsigned)count - 1u);
+    }
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    double t[3] = {0.0, 0.0, 0.0};
+    for (int i = threadIdx.x; i < count; i += blockDim.x)
+        for (int k = 0; k < 3; ++k) t[k] += __ldcg(A.partials + (size_t)k * A.n_items + C.item_begin + i);
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) t[k] += __shfl_xor_sync(0xffffffffu, t[k], off);
+    __syncthreads();
+    if (lane == 0)
+        for (int k = 0; k < 3; ++k) warp_sums[k][warp] = t[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double total[3] = {0.0, 0.0, 0.0};
+        for (int k = 0; k < 3; ++k)
+            for (int i = 0; i < (int)(blockDim.x >> 5); ++i) total[k] += warp_sums[k][i];
+        A.counters[s] = 0u;
+        fin(total[0], total[1], total[2]);
         __threadfence();
     }
 }
@@ -228,11 +281,112 @@ __device__ void spmv_item(const SceneDesc& d, const WorkItem& it, const void* in
     }
 }
 
+// ---- learned warm start (mixed precision) -------------------------------------------
+// End of k_batch_pre: x1 saved, Jacobi step and the RMS scales, features of
+// every solving scene (written into the batch's feature rows).
+__device__ void ws_features_phases(const BatchArgs& A, ItemList& L)
+{
+    constexpr int G = 8;
+    const unsigned gmask = group_mask<G>();
+    const int lane = threadIdx.x & (G - 1);
+    constexpr int gpb = kBlock / G;
+    if (!grid_barrier(A.sync)) return;
+    for_each_item(A, kSelSolving, L, [&](int i, const WorkItem& it) {
+        const SceneDesc& d = A.scenes[it.scene];
+        const float4* x = (const float4*)d.S.sol;
+        for (int r = it.lo + threadIdx.x; r < it.hi; r += blockDim.x) d.W.xsave[r] = x[r];
+        DotAcc32 acc[3];
+        for (int p0 = it.lo; p0 < it.hi; p0 += gpb) {
+            const int p = p0 + threadIdx.x / G;
+            if (p < it.hi) ws_jacobi_row<G, kLdCoherent>(d.P, d.S, d.W, p, lane, gmask, acc[0], acc[1], acc[2]);
+        }
+        WsScalars* wsc = d.W.sc;
+        item_reduce3(acc, A, i, d.C, it.scene, [wsc](double x2, double r2, double v2) {
+            wsc->sum_x2 = x2;
+            wsc->sum_r2 = r2;
+            wsc->sum_v2 = v2;
+        });
+    });
+    if (!grid_barrier(A.sync)) return;
+    for_each_item(A, kSelSolving, L, [&](int, const WorkItem& it) {
+        const SceneDesc& d = A.scenes[it.scene];
+        const volatile WsScalars* wsc = d.W.sc;
+        const float sx = safe_scale(wsc->sum_x2, wsc->n_free);
+        const float sr = safe_scale(wsc->sum_r2, wsc->n_free);
+        const float sv = safe_scale(wsc->sum_v2, wsc->n_free);
+        for (int p0 = it.lo; p0 < it.hi; p0 += gpb) {
+            const int p = p0 + threadIdx.x / G;
+            if (p < it.hi) ws_features_row<G, kLdCoherent>(d.P, d.S, d.W, p, lane, gmask, sx, sr, sv);
+        }
+    });
+}
+
+// Start of k_batch_cg, after the network ran on the feature rows: the learned
+// guess x0 = x1 + sigma MLP, its residual, and the guard that goes back to x1
+// (and its residual) where the learned guess is worse.  The running-scene
+// count follows the convergence flags the guard leaves.
+template <int G, int U>
+__device__ void ws_guess_phases(const BatchArgs& A, ItemList& L)
+{
+    using Acc = typename DotAccFor<float>::type;
+    if (threadIdx.x == 0) {
+        for (int s = blockIdx.x; s < A.n_scenes; s += gridDim.x)
+            if (A.run[s].solving) A.scenes[s].S.sc->rz_plain = A.scenes[s].S.sc->rz;
+    }
+    for_each_item(A, kSelSolving, L, [&](int, const WorkItem& it) {
+        const SceneDesc& d = A.scenes[it.scene];
+        const WsScalars* wsc = d.W.sc;
+        const float so = safe_scale(wsc->sum_x2, wsc->n_free) + safe_scale(wsc->sum_r2, wsc->n_free);
+        const float4* r = (const float4*)d.S.r;
+        for (int p = it.lo + threadIdx.x; p < it.hi; p += blockDim.x) {
+            d.rsave[p] = r[p];
+            ws_apply_elem(d.S, d.ws_y, p, so);
+        }
+    });
+    if (!grid_barrier(A.sync)) return;
+    for_each_item(A, kSelSolving, L, [&](int, const WorkItem& it) {
+        const SceneDesc& d = A.scenes[it.scene];
+        Acc acc;
+        spmv_item<G, false, false, U, kLdCoherent>(d, it, d.S.sol, d.S.y, acc);
+    });
+    if (!grid_barrier(A.sync)) return;
+    for_each_item(A, kSelSolving, L, [&](int i, const WorkItem& it) {
+        const SceneDesc& d = A.scenes[it.scene];
+        Acc acc;
+        for (int r = it.lo + threadIdx.x; r < it.hi; r += blockDim.x) residual_elem<false>(d.S, r, acc);
+        CgScalars* sc = d.S.sc;
+        BatchSync* sync = A.sync;
+        item_reduce(acc, A, i, d.C, it.scene, [sc, sync](double rr) {
+            const int was = sc->done ? 0 : 1;
+            cg_fin_residual(sc, rr);
+            ws_decide(sc);
+            const int now = sc->done ? 0 : 1;
+            if (now != was) atomicAdd(&sync->running, now - was);
+        });
+    });
+    if (!grid_barrier(A.sync)) return;
+    for_each_item(A, kSelSolving, L, [&](int, const WorkItem& it) {
+        const SceneDesc& d = A.scenes[it.scene];
+        if (!ld_volatile(&d.S.sc->ws_revert)) return;
+        float4* x = (float4*)d.S.sol;
+        float4* r = (float4*)d.S.r;
+        float4* pv = (float4*)d.S.p;
+        for (int p = it.lo + threadIdx.x; p < it.hi; p += blockDim.x) {
+            x[p] = d.W.xsave[p];
+            r[p] = d.rsave[p];
+            pv[p] = d.rsave[p];
+        }
+    });
+    grid_barrier(A.sync);
+}
+
 // ---- k_batch_pre ---------------------------------------------------------------------
 // The scenes' descriptors are read in place: their time-dependent fields are
 // rewritten by owner blocks only in phases separated from the readers by a
 // grid barrier.
-template <bool FP64>
+// WS: with the learned warm start (a separate instantiation, so the plain
+// kernels keep their register budget).
+template <bool FP64, bool WS>
 __global__ void __launch_bounds__(kBlock) k_batch_pre(BatchArgs A)
 {
     using Real = typename std::conditional<FP64, double, float>::type;
@@ -358,10 +512,11 @@ __global__ void __launch_bounds__(kBlock) k_batch_pre(BatchArgs A)
             if (!sc->done) atomicAdd(&sync->running, 1);
         });
     });
+    if constexpr (WS && !FP64) ws_features_phases(A, L);
 }
 
 // ---- k_batch_cg ----------------------------------------------------------------------
-template <int G, bool FP64, int U>
+template <int G, bool FP64, int U, bool WS>
 __global__ void __launch_bounds__(kBlock) k_batch_cg(BatchArgs A)
 {
     using Real = typename std::conditional<FP64, double, float>::type;
@@ -381,6 +536,10 @@ __global__ void __launch_bounds__(kBlock) k_batch_cg(BatchArgs A)
         return;
     }
 
+    if constexpr (WS && !FP64) {
+        ws_guess_phases<G, U>(A, L);
+        if (ld_volatile(&A.sync->error)) return;
+    }
     for (int iter = 0; iter < A.max_cg_iters; ++iter) {
         if (ld_volatile(&A.sync->running) == 0) break;
         // y = A p, alpha = rz / <p, y>
@@ -420,6 +579,13 @@ __global__ void __launch_bounds__(kBlock) k_batch_cg(BatchArgs A)
     for_each_item(A, kSelSolving, L, [&](int, const WorkItem& it) {
         const SceneDesc& d = A.scenes[it.scene];
         for (int r = it.lo + threadIdx.x; r < it.hi; r += blockDim.x) update_elem<FP64>(d.P, d.S, r);
+        if (WS && !FP64) {
+            // solution history of the features: x3 <- x2 <- x1
+            for (int r = it.lo + threadIdx.x; r < it.hi; r += blockDim.x) {
+                d.W.hist3[r] = d.W.hist2[r];
+                d.W.hist2[r] = d.W.xsave[r];
+            }
+        }
     });
     // per-scene bookkeeping (owner block): solve statistics, simulated time.
     // `solving` stays set until the next step starts: other blocks may still
@@ -452,20 +618,21 @@ cudaError_t cg_launch(bool fp64, const BatchArgs& A, int grid, cudaStream_t st)
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if (fp64) return cudaLaunchKernelEx(&cfg, k_batch_cg<G, true, 1>, A);
-    return cudaLaunchKernelEx(&cfg, k_batch_cg<G, false, U>, A);
+    if (fp64) return cudaLaunchKernelEx(&cfg, k_batch_cg<G, true, 1, false>, A);
+    if (A.warm_start) return cudaLaunchKernelEx(&cfg, k_batch_cg<G, false, U, true>, A);
+    return cudaLaunchKernelEx(&cfg, k_batch_cg<G, false, U, false>, A);
 }
 
 template <int G, int U>
 int cg_blocks(bool fp64)
 {
-    int b = 0;
-    if (fp64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch_cg<G, true, 1>, kBlock, 0);
-    else {
-        cudaFuncSetAttribute(k_batch_cg<G, false, U>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch_cg<G, false, U>, kBlock, 0);
-    }
-    return b;
+    int b = 0, c = 0;
+    if (fp64) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch_cg<G, true, 1, false>, kBlock, 0), b;
+    cudaFuncSetAttribute(k_batch_cg<G, false, U, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+    cudaFuncSetAttribute(k_batch_cg<G, false, U, true>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch_cg<G, false, U, false>, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_batch_cg<G, false, U, true>, kBlock, 0);
+    return b < c ? b : c;
 }
 
 }  // namespace
@@ -481,8 +648,9 @@ cudaError_t launch_batch_pre(bool fp64, const BatchArgs& A, int grid, cudaStream
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if (fp64) return cudaLaunchKernelEx(&cfg, k_batch_pre<true>, A);
-    return cudaLaunchKernelEx(&cfg, k_batch_pre<false>, A);
+    if (fp64) return cudaLaunchKernelEx(&cfg, k_batch_pre<true, false>, A);
+    if (A.warm_start) return cudaLaunchKernelEx(&cfg, k_batch_pre<false, true>, A);
+    return cudaLaunchKernelEx(&cfg, k_batch_pre<false, false>, A);
 }
 
 cudaError_t launch_batch_cg(bool fp64, int lanes, int unroll, const BatchArgs& A, int grid, cudaStream_t st)
@@ -493,10 +661,11 @@ cudaError_t launch_batch_cg(bool fp64, int lanes, int unroll, const BatchArgs& A
 
 int batch_pre_blocks_per_sm(bool fp64)
 {
-    int b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fp64 ? (const void*)k_batch_pre<true> : (const void*)k_batch_pre<false>,
-                                                  kBlock, 0);
-    return b;
+    int b = 0, c = 0;
+    if (fp64) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch_pre<true, false>, kBlock, 0), b;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch_pre<false, false>, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_batch_pre<false, true>, kBlock, 0);
+    return b < c ? b : c;
 }
 
 int batch_cg_blocks_per_sm(bool fp64, int lanes, int unroll)

@@ -6,6 +6,9 @@
 //   k_batch_pre  step start, rounds of { force pass ; adaptive decision ;
 //                rollback restore or backup }, CG set-up (b, x0, r0)
 //   k_batch_cg   CG iterations of every scene until all have converged, update
+// With the learned warm start on, k_batch_pre ends with the features of every
+// solving scene, one network launch over the rows of all scenes follows, and
+// k_batch_cg starts with the learned guess, its residual and the guard.
 // Per-scene CG scalars are reduced over the scene's items in item order, so
 // the sums do not depend on which block ran which item.
 #pragma once
@@ -55,6 +58,9 @@ struct SceneDesc {
     StepParams P;   // time-dependent fields rewritten on the device each step
     DeviceState S;
     SceneConst C;
+    WsState W;            // learned warm start: features point into the batch's buffer
+    float4* rsave;        // learned warm start: residual of the previous-solution guess
+    const float* ws_y;    // learned warm start: this scene's rows of the network output
 };
 
 struct WorkItem {
@@ -78,12 +84,13 @@ struct BatchArgs {
     const WorkItem* items;
     int n_items;
     int n_scenes;
-    double* partials;      // one FP64 partial per item
+    double* partials;      // three FP64 partials per item (arrays of n_items)
     unsigned int* counters;  // per-scene arrival counters (zero between reductions)
     BatchSync* sync;
     int max_rounds;        // force/decision rounds per step (rollbacks + 1)
     int max_cg_iters;      // bound of the CG loop over all scenes
     int tune_reps;         // > 0: only time the SpMV phase this many times
+    int warm_start;        // 1: learned CG initial guess (mixed precision)
 };
 
 // Launchers (batch.cu).  Both kernels are cooperative launches: `grid` must

@@ -498,13 +498,13 @@ void Engine::ws_free()
     ws_ready_ = false;
 }
 
-pd_status Engine::ws_prepare()
+pd_status Engine::ws_prepare(bool with_network)
 {
     if (ws_ready_) return PD_OK;
     const size_t N = (size_t)std::max(n_, 1);
     CK(dalloc(&W_.diag, N), "alloc ws");
     CK(dalloc(&W_.dj, N), "alloc ws");
-    CK(dalloc(&W_.features, N * kMlpIn), "alloc ws");
+    if (with_network) CK(dalloc(&W_.features, N * kMlpIn), "alloc ws");
     CK(dalloc(&W_.hist2, N), "alloc ws");
     CK(dalloc(&W_.hist3, N), "alloc ws");
     CK(dalloc(&W_.xsave, N), "alloc ws");
@@ -528,6 +528,11 @@ pd_status Engine::ws_prepare()
     sc.n_free = W_.n_free_host;
     CK(cudaMemcpyAsync(W_.sc, &sc, sizeof(sc), cudaMemcpyHostToDevice, stream_), "upload ws scalars");
     W_.max_bonds = std::max(sim_.pd_max_num_bonds, 1);
+    if (!with_network) {
+        CK(cudaStreamSynchronize(stream_), "ws prepare");
+        ws_ready_ = true;
+        return PD_OK;
+    }
     CK(mlp_alloc(&mlp_, false), "alloc mlp");
     CK(mlp_work_alloc(&mlp_work_, n_, false), "alloc mlp work");
     if (ws_params_.size() != mlp_param_count()) {

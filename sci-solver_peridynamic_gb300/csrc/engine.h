@@ -62,7 +62,9 @@ private:
     pd_status tune_spmv();
     // mixed mode: reorders every row's live bonds for the (g, u) SpMV shape
     void relayout_bonds(int g, int u);
-    pd_status ws_prepare();                 // allocates the warm-start state on first use
+    // allocates the warm-start state on first use; without the network
+    // (a batch scene: the batch owns the features, the network and its rows)
+    pd_status ws_prepare(bool with_network = true);
     void ws_free();
     bool ws_features_needed() const;
     pd_status ws_before_cg(const StepParams& P);

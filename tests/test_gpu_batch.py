@@ -143,3 +143,66 @@ def test_batch_errors(pdgb, scenes):
     assert e.value.status == 1
     with pytest.raises(pdgb.PdError):
         b.get(5, pdgb.VAR_POSITION)      # scene out of range
+
+
+def test_batch_learned_warm_start(pdgb, scenes):
+    """Batch option warm_start = 1: one network for all scenes, the guess
+    guarded per scene.  The CG still runs to each scene's tolerance, so every
+    scene matches the oracle (same time-step history, same broken bonds) and
+    its own Simulator with the same network; graph replay and direct launches
+    agree bitwise."""
+    ws = __import__("importlib").import_module("sci-solver_peridynamic_gb300.warmstart")
+    X, T = ws.collect(lambda seed: scenes.cube_lattice(n_side=10, seed=seed), seeds=(1,), steps=20,
+                      samples_per_step=256)
+    params, loss = ws.train(X, T, iterations=300, batch=1024, lr=1e-3)
+    assert np.isfinite(loss)
+    lst = _mix(pdgb, scenes, 0)
+    b = _batch(pdgb, scenes, lst, warm_start=1)
+    b.ws_set_params(params)
+    assert b.config().warm_start == 1
+    b2 = _batch(pdgb, scenes, lst, warm_start=1, use_graph=0, lanes_per_particle=b.config().lanes_per_particle,
+                spmv_unroll=b.config().spmv_unroll, item_rows=b.config().item_rows)
+    b2.ws_set_params(params)
+    oras = [make_oracle(sc) for sc in lst]
+    done = 0
+    while done < 40:
+        b.advance(10)
+        b2.advance(10)
+        for o in oras:
+            o.advance(10)
+        done += 10
+        for k, o in enumerate(oras):
+            assert b.stats(k).time_step_ticks == o.dt_ticks, f"scene {k}: time step differs at step {done}"
+            assert same_sets(b.alive_sets(k), o.alive_sets()), f"scene {k}: broken bonds differ at step {done}"
+    kept = 0
+    for k, (sc, o) in enumerate(zip(lst, oras)):
+        st = b.stats(k)
+        assert st.cg_converged == 1 and st.current_step == 40
+        x = b.get(k, pdgb.VAR_POSITION)
+        assert rel_err(x, o.position) < MIXED_TOL, f"scene {k}"
+        np.testing.assert_array_equal(x, b2.get(k, pdgb.VAR_POSITION))
+        sc.opt.warm_start = 1
+        s = scenes.make_simulator(sc)
+        s.makeReady()
+        s.ws_set_params(params)
+        s.advance(40)
+        sc.opt.warm_start = 0
+        assert same_sets(b.alive_sets(k), s.alive_sets()), f"scene {k}"
+        assert rel_err(x, s.get(pdgb.VAR_POSITION)) < MIXED_TOL, f"scene {k}"
+        kept += st.ws_guesses_kept
+    print(f"\nbatched learned warm start: guesses kept {kept} of {40 * len(lst)}, training loss {loss:.4g}")
+
+
+def test_batch_warm_start_needs_mixed_precision(pdgb, scenes):
+    o = pdgb.BatchOptions()
+    pdgb.library().pd_batch_options_default(o)
+    o.warm_start = 1
+    b = pdgb.Batch(0, o)
+    scenes.add_to_batch(b, scenes.impact_body(100, "block", precision=1))
+    with pytest.raises(pdgb.PdError) as e:
+        b.makeReady()
+    assert e.value.status == 1
+    o.warm_start = 2
+    with pytest.raises(pdgb.PdError) as e:
+        pdgb.Batch(0, o)
+    assert e.value.status == 1

@@ -32,7 +32,7 @@ def test_library_exports_every_declared_symbol(pdgb):
 
 
 def test_abi_version(pdgb):
-    assert pdgb.library().pd_abi_version() == 1
+    assert pdgb.library().pd_abi_version() == 2
 
 
 def test_params_file_and_derivation(pdgb, tmp_path):
