@@ -239,8 +239,7 @@ pd_status Batch::enqueue_step()
     BCK(cudaMemsetAsync(d_counters_, 0, sizeof(unsigned) * eng_.size(), stream_), "reset counters");
     BCK(launch_batch_pre(fp64_, A, grid_pre_, stream_), "k_batch_pre launch");
     if (opt_.warm_start && total_rows_ > 0) {
-        mlp_forward(mlp_, d_feat_, (int)total_rows_, mlp_work_, d_ws_y_, stream_);
-        BCK(cudaGetLastError(), "network launch");
+        BCK(mlp_infer_tc(mlp_, d_feat_, (int)total_rows_, d_ws_y_, stream_), "network launch");
     }
     BCK(launch_batch_cg(fp64_, lanes_, unroll_, A, grid_cg_, stream_), "k_batch_cg launch");
     return PD_OK;
@@ -528,6 +527,10 @@ pd_status Batch::pull_state()
         err_ = "batch step: a grid barrier wait timed out";
         return PD_ERR_CUDA;
     }
+    if (opt_.warm_start && mlp_tc_take_error()) {
+        err_ = "batch step: a wait of the warm-start network's tensor-core kernel ran out of time";
+        return PD_ERR_CUDA;
+    }
     for (size_t s = 0; s < ns; ++s) {
         if (h_run_[s].error) {
             err_ = "scene " + std::to_string(s) + ": adaptive time step: too many rollbacks";
@@ -552,7 +555,7 @@ pd_status Batch::advance(int nsteps)
             pd_status s = enqueue_step();
             if (s != PD_OK) return s;
         }
-        launches_ += 2 + (opt_.warm_start ? 6 : 0);   // + the network's 3 GEMMs and 3 bias/activation passes
+        launches_ += 2 + (opt_.warm_start ? 1 : 0);   // + the network's tensor-core kernel
     }
     return pull_state();
 }

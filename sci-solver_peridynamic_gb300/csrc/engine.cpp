@@ -571,7 +571,7 @@ pd_status Engine::ws_before_cg(const StepParams& P)
     if (opt_.warm_start == 1) {
         CK(cudaMemcpyAsync(ws_rsave_, S_.r, sizeof(float4) * N, cudaMemcpyDeviceToDevice, stream_), "save r");
         launch_ws_save_plain(S_, stream_);
-        mlp_forward(mlp_, W_.features, n_, mlp_work_, mlp_work_.y, stream_);
+        CK(mlp_infer_tc(mlp_, W_.features, n_, mlp_work_.y, stream_), "network launch");
         launch_ws_apply(P, S_, W_, mlp_work_.y, L_.grid_vec, stream_);
         launch_spmv(fp64_, false, P, S_, L_, stream_);
         launch_cg_residual(fp64_, P, S_, L_, stream_);
@@ -584,6 +584,10 @@ pd_status Engine::ws_before_cg(const StepParams& P)
 
 pd_status Engine::ws_after_cg(const StepParams& P)
 {
+    if (opt_.warm_start == 1 && mlp_tc_take_error()) {
+        err_ = "warm-start network: a tensor-core wait ran out of time";
+        return PD_ERR_CUDA;
+    }
     if (ws_samples_ > 0 && ws_cap_ > 0 && W_.n_free_host > 0) {
         const int count = std::min(ws_samples_, W_.n_free_host);
         const int stride = std::max(1, W_.n_free_host / count);

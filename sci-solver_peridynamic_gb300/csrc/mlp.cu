@@ -107,13 +107,15 @@ __device__ __forceinline__ float gelu_grad(float x)
     return 0.5f * (1.f + erff(x * 0.70710678118654752f)) + x * 0.3989422804014327f * expf(-0.5f * x * x);
 }
 
-// Z += bias; H = GELU(Z) as BF16 (Z kept in FP32 for the backward pass)
+// Z += bias (columns < nbias; the rest get none); H = GELU(Z) as BF16 (Z
+// kept in FP32 for the backward pass)
 __global__ void k_bias_gelu(float* __restrict__ Z, const float* __restrict__ bias, __nv_bfloat16* __restrict__ H, int M,
-                            int N, int act)
+                            int N, int nbias, int act)
 {
     const long long total = (long long)M * N;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const float z = Z[i] + bias[i % N];
+        const int c = (int)(i % N);
+        const float z = Z[i] + (c < nbias ? bias[c] : 0.f);
         Z[i] = z;
         if (H) H[i] = __float2bfloat16_rn(act ? gelu(z) : z);
     }
@@ -227,11 +229,11 @@ void mlp_forward(const MlpDev& m, const __nv_bfloat16* X, int B, MlpWork& ws, fl
     const float* b2 = b1 + kMlpHidden + kMlpHidden * kMlpHidden;
     const float* b3 = b2 + kMlpHidden + kMlpHidden * kMlpOut;
     gemm<false, false>(B, kMlpHidden, kMlpIn, X, kMlpIn, m.w1b, kMlpHidden, ws.z1, kMlpHidden, false, st);
-    k_bias_gelu<<<blocks_for((long long)B * kMlpHidden), 256, 0, st>>>(ws.z1, b1, ws.h1, B, kMlpHidden, 1);
+    k_bias_gelu<<<blocks_for((long long)B * kMlpHidden), 256, 0, st>>>(ws.z1, b1, ws.h1, B, kMlpHidden, kMlpHidden, 1);
     gemm<false, false>(B, kMlpHidden, kMlpHidden, ws.h1, kMlpHidden, m.w2b, kMlpHidden, ws.z2, kMlpHidden, false, st);
-    k_bias_gelu<<<blocks_for((long long)B * kMlpHidden), 256, 0, st>>>(ws.z2, b2, ws.h2, B, kMlpHidden, 1);
+    k_bias_gelu<<<blocks_for((long long)B * kMlpHidden), 256, 0, st>>>(ws.z2, b2, ws.h2, B, kMlpHidden, kMlpHidden, 1);
     gemm<false, false>(B, kMlpOutPad, kMlpHidden, ws.h2, kMlpHidden, m.w3b, kMlpOutPad, Y, kMlpOutPad, false, st);
-    k_bias_gelu<<<blocks_for((long long)B * kMlpOutPad), 256, 0, st>>>(Y, b3, nullptr, B, kMlpOutPad, 0);
+    k_bias_gelu<<<blocks_for((long long)B * kMlpOutPad), 256, 0, st>>>(Y, b3, nullptr, B, kMlpOutPad, kMlpOut, 0);
 }
 
 // Loss and gradients (into m.grad) for a batch; returns nothing, loss accumulates in *loss (device double).
@@ -456,9 +458,13 @@ extern "C" pd_status pd_mlp_predict(int device, const float* X, long long rows, 
     std::vector<float> yb((size_t)chunk * pdgb::kMlpOutPad);
     for (long long r0 = 0; r0 < rows; r0 += chunk) {
         const int B = (int)std::min(chunk, rows - r0);
-        pdgb::mlp_forward(s.m, s.X + (size_t)r0 * pdgb::kMlpIn, B, s.w, s.w.y, s.st);
+        MLP_TRY(pdgb::mlp_infer_tc(s.m, s.X + (size_t)r0 * pdgb::kMlpIn, B, s.w.y, s.st));
         MLP_TRY(cudaMemcpyAsync(yb.data(), s.w.y, (size_t)B * pdgb::kMlpOutPad * sizeof(float), cudaMemcpyDeviceToHost, s.st));
         MLP_TRY(cudaStreamSynchronize(s.st));
+        if (pdgb::mlp_tc_take_error()) {
+            pdgb::set_handleless_error("pd_mlp_predict: a tensor-core wait ran out of time");
+            return PD_ERR_CUDA;
+        }
         for (int i = 0; i < B; ++i)
             for (int c = 0; c < pdgb::kMlpOut; ++c) Y[(size_t)(r0 + i) * pdgb::kMlpOut + c] = yb[(size_t)i * pdgb::kMlpOutPad + c];
     }

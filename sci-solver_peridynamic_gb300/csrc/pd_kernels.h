@@ -275,6 +275,10 @@ struct WsState {
 size_t mlp_param_count();
 void mlp_refresh_bf16(MlpDev& m, cudaStream_t st);
 void mlp_forward(const MlpDev& m, const __nv_bfloat16* X, int B, MlpWork& ws, float* Y, cudaStream_t st);
+// inference only (mlp_tc.cu): all layers in one tcgen05 kernel, Y [B x 8]
+cudaError_t mlp_infer_tc(const MlpDev& m, const __nv_bfloat16* X, int B, float* Y, cudaStream_t st);
+// 1 if a wait of the tensor-core kernel ran out of time since the last call
+int mlp_tc_take_error();
 void mlp_backward(const MlpDev& m, const __nv_bfloat16* X, const float* T, int B, MlpWork& ws, const float* Y,
                   double* loss, cudaStream_t st);
 void mlp_adam(MlpDev& m, float lr, int t, cudaStream_t st);

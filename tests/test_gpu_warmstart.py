@@ -38,6 +38,23 @@ def test_mlp_forward_and_gradient_match_oracle(pdgb):
         assert err < GRAD_TOL, (name, err)
 
 
+@pytest.mark.parametrize("rows", [1, 127, 128, 129, 5000, 100003])
+def test_mlp_tensor_core_inference_matches_oracle(pdgb, rows):
+    """pd_mlp_predict runs the tcgen05 kernel (all three layers, TMEM
+    accumulators, 128-row tiles, up to two CTAs per SM looping over tiles):
+    partial tiles, one tile, and many tiles per CTA against the CPU
+    restatement with BF16 rounding at the same points."""
+    p = pdgb.mlp_init(7)
+    p[-3:] = [0.05, -0.02, 0.01]
+    X, _ = _batch(rows, 11)
+    Y = pdgb.mlp_predict(X, p)
+    Yo, _ = M.forward(X, p)
+    assert Y.shape == (rows, 3) and np.isfinite(Y).all()
+    assert np.linalg.norm(Y - Yo) / np.linalg.norm(Yo) < 2e-2
+    worst = np.abs(Y - Yo).max(axis=1) / (np.abs(Yo).max() + 1e-30)
+    assert worst.max() < 5e-2
+
+
 def test_mlp_training_reduces_loss(pdgb):
     X, T = _batch(8192, 2)
     p0 = pdgb.mlp_init(5)
