@@ -216,9 +216,13 @@ __device__ __forceinline__ void force_row(const StepParams& P, const DeviceState
         // smin = min(0, smallest stretch of a live bond), bit for bit: if no
         // live bond is shorter than at rest every stretch is >= 0; otherwise
         // the bonds whose estimate lies within its error (1e-6 relative) of the
-        // smallest are evaluated with the reference expression
+        // smallest are evaluated with the reference expression.  A bond at its
+        // rest length (dij^2 == d0^2 exactly, r == 0) has stretch exactly 0 and
+        // cannot lower smin, so rows at rest skip the exact evaluation; an r
+        // that underflows to -0 stands for a stretch below 1e-45, which moves
+        // the new limit (10 - 9 cs) s0 - 0.25 min(0, smin) by less than an ulp.
         const float rmin = group_minf<G>(r1, gmask);
-        if (rmin <= 0.f) {
+        if (rmin < 0.f) {
             const float band = rmin + 1e-6f * fabsf(rmin) + 1e-30f;
             if (!__any_sync(gmask, r2 <= band)) {
                 if (r1 <= band) {
