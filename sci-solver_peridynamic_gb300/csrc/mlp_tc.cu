@@ -29,6 +29,7 @@
 #include <cuda_bf16.h>
 
 #include <cstdint>
+#include <mutex>
 
 #include "pd_device.cuh"
 #include "pd_kernels.h"
@@ -42,6 +43,7 @@ constexpr int kTcThreads = 256;
 constexpr uint32_t kTmemCols = 256;
 constexpr int kOutN = 16;          // layer-3 MMA N
 constexpr unsigned long long kTcWaitNs = 1000000000ull;   // 1 s per wait
+constexpr int kMaxDevices = 64;
 
 constexpr int kOffW1 = 0;                                  // W1^T: 128 x 64
 constexpr int kOffW2 = kOffW1 + kMlpHidden * kMlpIn * 2;   // W2^T: 128 x 128
@@ -326,17 +328,25 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 cudaError_t mlp_infer_tc(const MlpDev& m, const __nv_bfloat16* X, int B, float* Y, cudaStream_t st)
 {
     if (B <= 0) return cudaSuccess;
-    static int configured_device = -1;
-    static int sm_count = 0;
+    // once per device (the shared-memory opt-in is a per-device attribute)
+    static std::mutex mtx;
+    static int sm_counts[kMaxDevices] = {};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    if (configured_device != dev) {
-        e = cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
-        if (e != cudaSuccess) return e;
-        e = cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev);
-        if (e != cudaSuccess) return e;
-        configured_device = dev;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    int sm_count = 0;
+    {
+        std::lock_guard<std::mutex> lock(mtx);
+        if (sm_counts[dev] == 0) {
+            e = cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+            if (e != cudaSuccess) return e;
+            int n = 0;
+            e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+            if (e != cudaSuccess) return e;
+            sm_counts[dev] = n;
+        }
+        sm_count = sm_counts[dev];
     }
     const float* b1 = m.params + kMlpIn * kMlpHidden;
     const float* b2 = b1 + kMlpHidden + kMlpHidden * kMlpHidden;
