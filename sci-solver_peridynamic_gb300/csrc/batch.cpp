@@ -240,6 +240,8 @@ pd_status Batch::enqueue_step()
     BCK(launch_batch_pre(fp64_, A, grid_pre_, stream_), "k_batch_pre launch");
     if (opt_.warm_start && total_rows_ > 0) {
         BCK(mlp_infer_tc(mlp_, d_feat_, (int)total_rows_, d_ws_y_, stream_), "network launch");
+        const int grid_ws = std::max(1, batch_ws_blocks_per_sm(lanes_, unroll_)) * sm_count_;
+        BCK(launch_batch_ws_guess(lanes_, unroll_, A, grid_ws, stream_), "k_batch_ws_guess launch");
     }
     BCK(launch_batch_cg(fp64_, lanes_, unroll_, A, grid_cg_, stream_), "k_batch_cg launch");
     return PD_OK;
@@ -555,7 +557,7 @@ pd_status Batch::advance(int nsteps)
             pd_status s = enqueue_step();
             if (s != PD_OK) return s;
         }
-        launches_ += 2 + (opt_.warm_start ? 1 : 0);   // + the network's tensor-core kernel
+        launches_ += 2 + (opt_.warm_start ? 2 : 0);   // + the network's tensor-core kernel and the guess
     }
     return pull_state();
 }

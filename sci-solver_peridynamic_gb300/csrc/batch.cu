@@ -294,7 +294,13 @@ __device__ void ws_features_phases(const BatchArgs& A, ItemList& L)
     for_each_item(A, kSelSolving, L, [&](int i, const WorkItem& it) {
         const SceneDesc& d = A.scenes[it.scene];
         const float4* x = (const float4*)d.S.sol;
-        for (int r = it.lo + threadIdx.x; r < it.hi; r += blockDim.x) d.W.xsave[r] = x[r];
+        // solution history of the features: x3 <- x2 <- the previous step's
+        // x1, then x1 <- the current guess
+        for (int r = it.lo + threadIdx.x; r < it.hi; r += blockDim.x) {
+            d.W.hist3[r] = d.W.hist2[r];
+            d.W.hist2[r] = d.W.xsave[r];
+            d.W.xsave[r] = x[r];
+        }
         DotAcc32 acc[3];
         for (int p0 = it.lo; p0 < it.hi; p0 += gpb) {
             const int p = p0 + threadIdx.x / G;
@@ -321,7 +327,7 @@ __device__ void ws_features_phases(const BatchArgs& A, ItemList& L)
     });
 }
 
-// Start of k_batch_cg, after the network ran on the feature rows: the learned
+// k_batch_ws_guess, after the network ran on the feature rows: the learned
 // guess x0 = x1 + sigma MLP, its residual, and the guard that goes back to x1
 // (and its residual) where the learned guess is worse.  The running-scene
 // count follows the convergence flags the guard leaves.
@@ -378,6 +384,15 @@ __device__ void ws_guess_phases(const BatchArgs& A, ItemList& L)
         }
     });
     grid_barrier(A.sync);
+}
+
+// The learned guess of every solving scene (a launch of its own between the
+// network and k_batch_cg, so the CG kernel keeps its register budget).
+template <int G, int U>
+__global__ void __launch_bounds__(kBlock, 4) k_batch_ws_guess(BatchArgs A)
+{
+    __shared__ ItemList L;
+    ws_guess_phases<G, U>(A, L);
 }
 
 // ---- k_batch_pre ---------------------------------------------------------------------
@@ -516,8 +531,11 @@ __global__ void __launch_bounds__(kBlock) k_batch_pre(BatchArgs A)
 }
 
 // ---- k_batch_cg ----------------------------------------------------------------------
-template <int G, bool FP64, int U, bool WS>
-__global__ void __launch_bounds__(kBlock) k_batch_cg(BatchArgs A)
+// 4 resident blocks per SM (64 registers): the CG phases are latency-bound
+// gathers, and at 64 scenes / 1.39M particles this beats 79 registers and 3
+// blocks by 16 % per step despite a few spilled registers.
+template <int G, bool FP64, int U>
+__global__ void __launch_bounds__(kBlock, 4) k_batch_cg(BatchArgs A)
 {
     using Real = typename std::conditional<FP64, double, float>::type;
     using Acc = typename DotAccFor<Real>::type;
@@ -536,10 +554,6 @@ __global__ void __launch_bounds__(kBlock) k_batch_cg(BatchArgs A)
         return;
     }
 
-    if constexpr (WS && !FP64) {
-        ws_guess_phases<G, U>(A, L);
-        if (ld_volatile(&A.sync->error)) return;
-    }
     for (int iter = 0; iter < A.max_cg_iters; ++iter) {
         if (ld_volatile(&A.sync->running) == 0) break;
         // y = A p, alpha = rz / <p, y>
@@ -579,13 +593,6 @@ __global__ void __launch_bounds__(kBlock) k_batch_cg(BatchArgs A)
     for_each_item(A, kSelSolving, L, [&](int, const WorkItem& it) {
         const SceneDesc& d = A.scenes[it.scene];
         for (int r = it.lo + threadIdx.x; r < it.hi; r += blockDim.x) update_elem<FP64>(d.P, d.S, r);
-        if (WS && !FP64) {
-            // solution history of the features: x3 <- x2 <- x1
-            for (int r = it.lo + threadIdx.x; r < it.hi; r += blockDim.x) {
-                d.W.hist3[r] = d.W.hist2[r];
-                d.W.hist2[r] = d.W.xsave[r];
-            }
-        }
     });
     // per-scene bookkeeping (owner block): solve statistics, simulated time.
     // `solving` stays set until the next step starts: other blocks may still
@@ -618,21 +625,44 @@ cudaError_t cg_launch(bool fp64, const BatchArgs& A, int grid, cudaStream_t st)
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if (fp64) return cudaLaunchKernelEx(&cfg, k_batch_cg<G, true, 1, false>, A);
-    if (A.warm_start) return cudaLaunchKernelEx(&cfg, k_batch_cg<G, false, U, true>, A);
-    return cudaLaunchKernelEx(&cfg, k_batch_cg<G, false, U, false>, A);
+    if (fp64) return cudaLaunchKernelEx(&cfg, k_batch_cg<G, true, 1>, A);
+    return cudaLaunchKernelEx(&cfg, k_batch_cg<G, false, U>, A);
+}
+
+template <int G, int U>
+cudaError_t ws_launch(const BatchArgs& A, int grid, cudaStream_t st)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kBlock);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_batch_ws_guess<G, U>, A);
 }
 
 template <int G, int U>
 int cg_blocks(bool fp64)
 {
-    int b = 0, c = 0;
-    if (fp64) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch_cg<G, true, 1, false>, kBlock, 0), b;
-    cudaFuncSetAttribute(k_batch_cg<G, false, U, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
-    cudaFuncSetAttribute(k_batch_cg<G, false, U, true>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch_cg<G, false, U, false>, kBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_batch_cg<G, false, U, true>, kBlock, 0);
-    return b < c ? b : c;
+    int b = 0;
+    if (fp64) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch_cg<G, true, 1>, kBlock, 0), b;
+    // a small shared-memory carve-out (the rest stays L1): 4 blocks of ~1.3 KB
+    // (+ 1 KB reserved each) do not fit the smallest one
+    cudaFuncSetAttribute(k_batch_cg<G, false, U>, cudaFuncAttributePreferredSharedMemoryCarveout, 10);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch_cg<G, false, U>, kBlock, 0);
+    return b;
+}
+
+template <int G, int U>
+int ws_blocks()
+{
+    int b = 0;
+    cudaFuncSetAttribute(k_batch_ws_guess<G, U>, cudaFuncAttributePreferredSharedMemoryCarveout, 10);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch_ws_guess<G, U>, kBlock, 0);
+    return b;
 }
 
 }  // namespace
@@ -672,6 +702,18 @@ int batch_cg_blocks_per_sm(bool fp64, int lanes, int unroll)
 {
     if (lanes == 4) return unroll == 4 ? cg_blocks<4, 4>(fp64) : cg_blocks<4, 2>(fp64);
     return unroll == 4 ? cg_blocks<8, 4>(fp64) : cg_blocks<8, 2>(fp64);
+}
+
+cudaError_t launch_batch_ws_guess(int lanes, int unroll, const BatchArgs& A, int grid, cudaStream_t st)
+{
+    if (lanes == 4) return unroll == 4 ? ws_launch<4, 4>(A, grid, st) : ws_launch<4, 2>(A, grid, st);
+    return unroll == 4 ? ws_launch<8, 4>(A, grid, st) : ws_launch<8, 2>(A, grid, st);
+}
+
+int batch_ws_blocks_per_sm(int lanes, int unroll)
+{
+    if (lanes == 4) return unroll == 4 ? ws_blocks<4, 4>() : ws_blocks<4, 2>();
+    return unroll == 4 ? ws_blocks<8, 4>() : ws_blocks<8, 2>();
 }
 
 }  // namespace pdgb

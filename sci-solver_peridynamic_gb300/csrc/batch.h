@@ -8,7 +8,8 @@
 //   k_batch_cg   CG iterations of every scene until all have converged, update
 // With the learned warm start on, k_batch_pre ends with the features of every
 // solving scene, one network launch over the rows of all scenes follows, and
-// k_batch_cg starts with the learned guess, its residual and the guard.
+// k_batch_ws_guess forms the learned guess, its residual and the guard before
+// k_batch_cg.
 // Per-scene CG scalars are reduced over the scene's items in item order, so
 // the sums do not depend on which block ran which item.
 #pragma once
@@ -99,5 +100,8 @@ cudaError_t launch_batch_pre(bool fp64, const BatchArgs& A, int grid, cudaStream
 cudaError_t launch_batch_cg(bool fp64, int lanes, int unroll, const BatchArgs& A, int grid, cudaStream_t st);
 int batch_pre_blocks_per_sm(bool fp64);
 int batch_cg_blocks_per_sm(bool fp64, int lanes, int unroll);
+// learned warm start (mixed precision): the guess, its residual and the guard
+cudaError_t launch_batch_ws_guess(int lanes, int unroll, const BatchArgs& A, int grid, cudaStream_t st);
+int batch_ws_blocks_per_sm(int lanes, int unroll);
 
 }  // namespace pdgb
