@@ -443,7 +443,8 @@ pd_status Engine::dataio_load_state(size_t timestep)
     const StepParams P = step_params();
     if (!fp64_ && n_ > 0) {
         launch_refresh(fp64_, P, S_, L_, stream_);
-        ++launches_;
+        launch_stretch_limits(S_, (int)std::min<long long>(((long long)n_ + kBlock - 1) / kBlock, 4096), stream_);
+        launches_ += 2;
         if (S_.lidx && S_.n_tiles > 0) {
             int max_halo = 0;
             CK(build_tiles(S_, n_, &max_halo, stream_), "rebuild tiles");

@@ -134,7 +134,7 @@ void Engine::free_all()
     ws_free();
     void* ptrs[] = {S_.act, S_.x64, S_.v64, S_.X64, S_.x64_bk, S_.v64_bk, S_.st, S_.ost, S_.nst, S_.row_ptr,
                     S_.cnt, S_.cnt_bk, S_.col, S_.X32, S_.u32, S_.xs4, S_.inv_d0, S_.jac, S_.jdiag, S_.force, S_.rhs, S_.sol,
-                    S_.r, S_.p, S_.y, S_.sc, S_.partials, S_.counters, S_.flags, S_.lidx, S_.d0sq, d_perm_};
+                    S_.r, S_.p, S_.y, S_.sc, S_.partials, S_.counters, S_.flags, S_.lidx, S_.d0sq, S_.lim, d_perm_};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     free_tiles(S_);
@@ -162,6 +162,7 @@ pd_status Engine::allocate()
     CK(dalloc(&S_.st, n), "alloc stretch");
     CK(dalloc(&S_.ost, n), "alloc original stretch");
     CK(dalloc(&S_.nst, n), "alloc new stretch");
+    CK(dalloc(&S_.lim, n), "alloc stretch limits");
     CK(dalloc(&S_.row_ptr, n + 1), "alloc row_ptr");
     CK(dalloc(&S_.cnt, n), "alloc cnt");
     CK(dalloc(&S_.cnt_bk, n), "alloc cnt backup");
@@ -249,6 +250,10 @@ pd_status Engine::make_ready()
         gather_double(d_tmp1, d_perm_, S_.ost, n, stream_);
         CK(cudaMemcpyAsync(S_.st, S_.ost, sizeof(double) * N, cudaMemcpyDeviceToDevice, stream_), "copy st");
         CK(cudaMemcpyAsync(S_.nst, S_.ost, sizeof(double) * N, cudaMemcpyDeviceToDevice, stream_), "copy nst");
+        if (!fp64_) {
+            launch_stretch_limits(S_, (int)std::min<long long>(((long long)n + kBlock - 1) / kBlock, 4096), stream_);
+            ++launches_;
+        }
         CK(cudaMemcpyAsync(S_.cnt_bk, S_.cnt, sizeof(int) * N, cudaMemcpyDeviceToDevice, stream_), "backup cnt");
         CK(cudaMemcpyAsync(S_.x64_bk, S_.x64, sizeof(dbl4) * N, cudaMemcpyDeviceToDevice, stream_), "backup x");
         CK(cudaMemcpyAsync(S_.v64_bk, S_.v64, sizeof(dbl4) * N, cudaMemcpyDeviceToDevice, stream_), "backup v");

@@ -95,6 +95,7 @@ struct DeviceState {
     double* st;        // pd_stretch
     double* ost;       // pd_original_stretch
     double* nst;       // pd_new_stretch
+    double2* lim;      // mixed: limits of the squared break test per particle (limit_pair of st)
     int* row_ptr;      // CSR row starts (32-byte aligned rows), n+1
     int* cnt;          // live bonds per particle (pd_bond_list_top + 1)
     int* cnt_bk;
@@ -158,6 +159,8 @@ void launch_cg_xpby(bool fp64, const StepParams& P, const DeviceState& S, const 
 void launch_update(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
 void launch_refresh(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
 void launch_bond_geometry(const DeviceState& S, int grid, cudaStream_t st);
+// mixed: lim[p] = limit_pair(st[p]) for every particle (after st is set)
+void launch_stretch_limits(const DeviceState& S, int grid, cudaStream_t st);
 // mixed mode: live bonds of each row reordered from the (g_from, u_from)
 // SpMV shape's slot order to (g_to, u_to)'s (u = 1: build order)
 void launch_bond_relayout(const DeviceState& S, int grid, int g_from, int u_from, int g_to, int u_to,

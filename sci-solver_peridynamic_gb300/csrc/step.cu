@@ -167,6 +167,17 @@ void launch_bond_geometry(const DeviceState& S, int grid, cudaStream_t st)
     k_bond_geometry<<<grid, kBlock, 0, st>>>(S.n, S);
 }
 
+__global__ void __launch_bounds__(kBlock) k_stretch_limits(int n, DeviceState S)
+{
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
+        S.lim[p] = limit_pair(S.st[p]);
+}
+
+void launch_stretch_limits(const DeviceState& S, int grid, cudaStream_t st)
+{
+    k_stretch_limits<<<grid, kBlock, 0, st>>>(S.n, S);
+}
+
 // Reorders the live bonds of each row for a (lanes G, unroll U) SpMV shape.
 // The SpMV's lane k loads U consecutive slots 16-byte-wise (slots b*GU + kU +
 // u, u < U) and gathers their neighbours as U instructions; so that the

@@ -90,8 +90,25 @@ struct MixedBond {
     bool live;
 };
 
+// Limits of the squared break test of a particle with stretch limit st:
+// with t = st rounded to float and L = (1 + t)^2, {L (1 - 1e-12), L (1 + 1e-12)}
+// ({-1, -1} when 1 + t <= 0).  A bond's limit is the larger of its two
+// particles' t, and (1 + t)^2 grows with t, so the bond's pair is the
+// element-wise maximum of the particles' pairs.
+__device__ __forceinline__ double2 limit_pair(double st)
+{
+    const double l1 = dadd(1.0, (double)(float)st);
+    if (!(l1 > 0.0)) return make_double2(-1.0, -1.0);
+    const double L = dmul(l1, l1);
+    return make_double2(dmul(L, 1.0 - 1e-12), dmul(L, 1.0 + 1e-12));
+}
+
+// The break test s > fmaxf(st_p, st_q) (s = dij / d0 - 1 in FP64) decided on
+// squares: broken when dij^2 > (1 + t)^2 d0^2 (1 + 1e-12), live when
+// dij^2 < (1 + t)^2 d0^2 (1 - 1e-12), both far outside the rounding of either
+// form; a bond in between takes the reference expression.
 __device__ __forceinline__ MixedBond classify_mixed(const DeviceState& S, const dbl4& xp, const dbl4& Xp, float thp,
-                                                    int slot, int q)
+                                                    double2 limp, int slot, int q)
 {
     MixedBond m;
     const dbl4 xq = S.x64[q];
@@ -100,11 +117,11 @@ __device__ __forceinline__ MixedBond classify_mixed(const DeviceState& S, const 
     m.ez = dsub(xq.z, xp.z);
     m.dd = dadd(dadd(dmul(m.ex, m.ex), dmul(m.ey, m.ey)), dmul(m.ez, m.ez));
     const double d0s = S.d0sq[slot];
-    const double thr = break_threshold(thp, S.st[q]);
-    const double l1 = dadd(1.0, thr);
-    const double gap = dsub(m.dd, dmul(dmul(l1, l1), d0s));
-    if (l1 > 0.0 && fabs(gap) > 1e-12 * m.dd) m.live = !(gap > 0.0);
-    else m.live = !(eval_bond(xp, Xp, xq, S.X64[q]).s > thr);
+    const double2 limq = S.lim[q];
+    const double lo = fmax(limp.x, limq.x), hi = fmax(limp.y, limq.y);
+    if (hi > 0.0 && m.dd > dmul(hi, d0s)) m.live = false;
+    else if (lo > 0.0 && m.dd < dmul(lo, d0s)) m.live = true;
+    else m.live = !(eval_bond(xp, Xp, xq, S.X64[q]).s > break_threshold(thp, S.st[q]));
     m.num = dsub(m.dd, d0s);
     return m;
 }
@@ -185,11 +202,14 @@ __device__ __forceinline__ void force_row(const StepParams& P, const DeviceState
         // live bonds: FP32 force from the FP64 bond vector; the stretch comes
         // from dij2 - d0^2 (no cancellation) as s = (dij2 - d0^2) / (d0 (dij + d0))
         const float* id0r = S.inv_d0 + rs;
+        const double2 limp = S.lim[p];
+        // (double)d0 > vs_threshold  <=>  d0 > (vs_threshold rounded down to float)
+        const float vs_thr = __double2float_rd(P.vs_threshold);
         float r1 = 3.0e38f, r2 = 3.0e38f;   // the lane's two smallest (dij2 - d0^2) / d0^2
         int j1 = -1;
         for (int j = lane; j < c; j += G) {
             const int q = S.col[rs + j];
-            const MixedBond m = classify_mixed(S, xp, Xp, thp, rs + j, q);
+            const MixedBond m = classify_mixed(S, xp, Xp, thp, limp, rs + j, q);
             if (!m.live) {
                 ++nb;
                 continue;
@@ -207,7 +227,7 @@ __device__ __forceinline__ void force_row(const StepParams& P, const DeviceState
                 r2 = r;
             }
             float vs = 1.0f;
-            if ((double)d0 > P.vs_threshold) vs = 0.5f + ((float)P.horizon - d0) * 0.5f / (float)P.radius;
+            if (d0 > vs_thr) vs = 0.5f + ((float)P.horizon - d0) * 0.5f / (float)P.radius;
             const float kk = sf * vs / fmaxf(d, 1e-10f);   // eij /= fmaxf(dij, SMALL)
             fx = fmaf(kk, (float)m.ex, (float)fx);
             fy = fmaf(kk, (float)m.ey, (float)fy);
@@ -234,7 +254,7 @@ __device__ __forceinline__ void force_row(const StepParams& P, const DeviceState
                 // several candidates in one lane: walk the row again
                 for (int j = lane; j < c; j += G) {
                     const int q = S.col[rs + j];
-                    const MixedBond m = classify_mixed(S, xp, Xp, thp, rs + j, q);
+                    const MixedBond m = classify_mixed(S, xp, Xp, thp, limp, rs + j, q);
                     if (!m.live) continue;
                     const float idd0 = id0r[j];
                     if ((float)m.num * (idd0 * idd0) > band) continue;
@@ -715,6 +735,7 @@ __device__ __forceinline__ void update_elem(const StepParams& P, const DeviceSta
     using V4 = typename Vec4<Real>::type;
     const V4* sol = (const V4*)S.sol;
     S.st[i] = S.nst[i];   // updatePDStretchNeighborList (simulator.cuh:2601-2620)
+    if constexpr (!FP64) S.lim[i] = limit_pair(S.nst[i]);
     const int a = S.act[i] & kActMask;
     const dbl4 x = S.x64[i];
     dbl4 v = S.v64[i];
