@@ -168,7 +168,8 @@ typedef enum pd_variable {
     PD_VAR_BOND_LIST = 10,         /* int32[total]: per particle, live neighbours ascending then broken ones ascending */
     PD_VAR_POSITION_SCALED = 11,   /* double[4n]: positions * scaleFactor (DataIO convention) */
     PD_VAR_ORIGINAL_POSITION = 12, /* double[4n]: pd_original_pos */
-    PD_VAR_SLOT_PERMUTATION = 13   /* int32[n]: caller index of each device slot (operator view order) */
+    PD_VAR_SLOT_PERMUTATION = 13,  /* int32[n]: caller index of each device slot (operator view order) */
+    PD_VAR_BROKEN_MASK = 14        /* uint8[total]: 1 where the PD_VAR_BOND_LIST entry is a broken bond */
 } pd_variable;
 
 typedef struct pd_step_stats {

@@ -38,7 +38,7 @@ PRECISION_MIXED, PRECISION_FP64 = 0, 1
 # pd_variable
 (VAR_POSITION, VAR_VELOCITY, VAR_ACTIVITY, VAR_BOND_COUNT, VAR_STRETCH, VAR_ORIGINAL_STRETCH,
  VAR_NEW_STRETCH, VAR_FORCE, VAR_SOLUTION, VAR_BOND_ROW_PTR, VAR_BOND_LIST, VAR_POSITION_SCALED,
- VAR_ORIGINAL_POSITION, VAR_SLOT_PERMUTATION) = range(14)
+ VAR_ORIGINAL_POSITION, VAR_SLOT_PERMUTATION, VAR_BROKEN_MASK) = range(15)
 # pd_kernel_class
 KC_FORCE, KC_SPMV, KC_CG_VECTOR, KC_UPDATE = range(4)
 KC_NAMES = ("force", "spmv", "cg_vector", "update")
@@ -422,7 +422,9 @@ class Simulator:
     def get(self, var: int) -> np.ndarray:
         size = C.c_size_t()
         _check(self.lib.pd_get_size(self.h, var, C.byref(size)), self.h)
-        if var in (VAR_ACTIVITY, VAR_BOND_COUNT, VAR_BOND_LIST, VAR_SLOT_PERMUTATION):
+        if var == VAR_BROKEN_MASK:
+            out = np.zeros(size.value, np.uint8)
+        elif var in (VAR_ACTIVITY, VAR_BOND_COUNT, VAR_BOND_LIST, VAR_SLOT_PERMUTATION):
             out = np.zeros(size.value // 4, np.int32)
         elif var == VAR_BOND_ROW_PTR:
             out = np.zeros(size.value // 8, np.int64)
@@ -622,7 +624,9 @@ class Batch:
     def get(self, scene: int, var: int) -> np.ndarray:
         size = C.c_size_t()
         _bcheck(self.lib.pd_batch_get_size(self.h, scene, var, C.byref(size)), self.h)
-        if var in (VAR_ACTIVITY, VAR_BOND_COUNT, VAR_BOND_LIST, VAR_SLOT_PERMUTATION):
+        if var == VAR_BROKEN_MASK:
+            out = np.zeros(size.value, np.uint8)
+        elif var in (VAR_ACTIVITY, VAR_BOND_COUNT, VAR_BOND_LIST, VAR_SLOT_PERMUTATION):
             out = np.zeros(size.value // 4, np.int32)
         elif var == VAR_BOND_ROW_PTR:
             out = np.zeros(size.value // 8, np.int64)

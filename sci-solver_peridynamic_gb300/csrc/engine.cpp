@@ -1010,6 +1010,7 @@ pd_status Engine::get_size(pd_variable var, size_t* bytes) const
     case PD_VAR_STRETCH: case PD_VAR_ORIGINAL_STRETCH: case PD_VAR_NEW_STRETCH: *bytes = N * sizeof(double); return PD_OK;
     case PD_VAR_BOND_ROW_PTR: *bytes = (N + 1) * sizeof(int64_t); return PD_OK;
     case PD_VAR_BOND_LIST: *bytes = (size_t)bonds_initial_ * sizeof(int32_t); return PD_OK;
+    case PD_VAR_BROKEN_MASK: *bytes = (size_t)bonds_initial_; return PD_OK;
     }
     return PD_ERR_INVALID_ARGUMENT;
 }
@@ -1057,6 +1058,20 @@ pd_status Engine::get(pd_variable var, void* dst, size_t bytes)
     case PD_VAR_SLOT_PERMUTATION:
         std::memcpy(dst, perm_.data(), N * sizeof(int32_t));
         return PD_OK;
+    case PD_VAR_BROKEN_MASK: {
+        // rows in caller order as PD_VAR_BOND_LIST: live bonds first, then broken
+        std::vector<int> cnt(N);
+        pd_status s = download_scatter(S_.cnt, cnt.data(), 1, N);
+        if (s != PD_OK) return s;
+        uint8_t* m = (uint8_t*)dst;
+        size_t pos = 0;
+        for (size_t o = 0; o < N; ++o) {
+            const int live = cnt[o], all = cnt_init_[inv_[o]];
+            for (int j = 0; j < all; ++j) m[pos + j] = j < live ? 0 : 1;
+            pos += all;
+        }
+        return PD_OK;
+    }
     default: return PD_ERR_INVALID_ARGUMENT;
     }
 }

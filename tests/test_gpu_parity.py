@@ -86,6 +86,14 @@ def test_step_mixed_newmark_breaking(pdgb, scenes):
                                 cg_tol=1e-9)
     sim, ora = _run_pair(pdgb, scenes, sc, 60)
     assert rel_err(sim.get(pdgb.VAR_POSITION), ora.position) < MIXED_TOL
+    # the broken-bond mask export: per row, the bond-list entries it marks are
+    # exactly the oracle's initial neighbours that are no longer alive
+    rp, bl = sim.get(pdgb.VAR_BOND_ROW_PTR), sim.get(pdgb.VAR_BOND_LIST)
+    mask, cnt = sim.get(pdgb.VAR_BROKEN_MASK), sim.get(pdgb.VAR_BOND_COUNT)
+    assert mask.shape == bl.shape and int(mask.sum()) == int(rp[-1] - cnt.sum()) > 0
+    for i, alive in enumerate(ora.alive_sets()):
+        row, m = bl[rp[i]:rp[i + 1]], mask[rp[i]:rp[i + 1]]
+        assert np.array_equal(np.sort(row[m == 1]), np.setdiff1d(row, alive)), i
 
 
 def test_cube_lattice_mixed_100_steps(pdgb, scenes):
