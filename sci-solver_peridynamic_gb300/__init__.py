@@ -419,9 +419,16 @@ class Simulator:
         return v.value
 
     # exports (MemoryManager::downloadFromDevice equivalents)
-    def get(self, var: int) -> np.ndarray:
+    def get(self, var: int, out: np.ndarray | None = None) -> np.ndarray:
+        """The variable in caller order; with `out` (C-contiguous, of the
+        variable's byte size, e.g. a pinned buffer) it is written there."""
         size = C.c_size_t()
         _check(self.lib.pd_get_size(self.h, var, C.byref(size)), self.h)
+        if out is not None:
+            if not out.flags["C_CONTIGUOUS"] or out.nbytes != size.value:
+                raise ValueError("get: out must be C-contiguous with %d bytes" % size.value)
+            _check(self.lib.pd_get(self.h, var, out.ctypes.data_as(C.c_void_p), size.value), self.h)
+            return out
         if var == VAR_BROKEN_MASK:
             out = np.zeros(size.value, np.uint8)
         elif var in (VAR_ACTIVITY, VAR_BOND_COUNT, VAR_BOND_LIST, VAR_SLOT_PERMUTATION):

@@ -307,6 +307,31 @@ __global__ void k_scatter_d4(const dbl4* __restrict__ in, const int* __restrict_
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[perm[i]] = in[i];
 }
+// exports: device slot order -> caller order, then one copy to the host
+__global__ void k_scatter_words(const uint32_t* __restrict__ in, const int* __restrict__ perm,
+                                uint32_t* __restrict__ out, int words, long long total)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long row = i / words;
+        out[(long long)perm[row] * words + (i - row * words)] = in[i];
+    }
+}
+__global__ void k_scatter_to_d4_w0(const void* __restrict__ in, bool is_float, const int* __restrict__ perm,
+                                   dbl4* __restrict__ out, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        dbl4 v;
+        if (is_float) {
+            const float4 f = ((const float4*)in)[i];
+            v = make_dbl4(f.x, f.y, f.z, 0.0);
+        } else {
+            v = ((const dbl4*)in)[i];
+            v.w = 0.0;
+        }
+        out[perm[i]] = v;
+    }
+}
 __global__ void k_local32(const dbl4* __restrict__ X, double ox, double oy, double oz, float4* __restrict__ X32,
                           float4* __restrict__ u32, int n)
 {
@@ -375,6 +400,17 @@ void gather_int_to_u8(const int* in, const int* perm, uint8_t* out, int n, cudaS
 void scatter_double4(const dbl4* in, const int* perm, dbl4* out, int n, cudaStream_t st)
 {
     if (n > 0) k_scatter_d4<<<grid_for(n), kBlock, 0, st>>>(in, perm, out, n);
+}
+void scatter_words(const void* in, const int* perm, void* out, int words_per_row, int n, cudaStream_t st)
+{
+    if (n <= 0) return;
+    const long long total = (long long)n * words_per_row;
+    const int grid = (int)std::min<long long>((total + kBlock - 1) / kBlock, 65535LL * 8);
+    k_scatter_words<<<grid, kBlock, 0, st>>>((const uint32_t*)in, perm, (uint32_t*)out, words_per_row, total);
+}
+void scatter_to_d4_w0(const void* in, bool is_float, const int* perm, dbl4* out, int n, cudaStream_t st)
+{
+    if (n > 0) k_scatter_to_d4_w0<<<grid_for(n), kBlock, 0, st>>>(in, is_float, perm, out, n);
 }
 void make_local32(const dbl4* X, double ox, double oy, double oz, float4* X32, float4* u32, int n, cudaStream_t st)
 {

@@ -134,7 +134,8 @@ void Engine::free_all()
     ws_free();
     void* ptrs[] = {S_.act, S_.x64, S_.v64, S_.X64, S_.x64_bk, S_.v64_bk, S_.st, S_.ost, S_.nst, S_.row_ptr,
                     S_.cnt, S_.cnt_bk, S_.col, S_.X32, S_.u32, S_.xs4, S_.inv_d0, S_.jac, S_.jdiag, S_.force, S_.rhs, S_.sol,
-                    S_.r, S_.p, S_.y, S_.sc, S_.partials, S_.counters, S_.flags, S_.lidx, S_.d0sq, S_.lim, d_perm_};
+                    S_.r, S_.p, S_.y, S_.sc, S_.partials, S_.counters, S_.flags, S_.lidx, S_.d0sq, S_.lim, d_perm_,
+                    d_stage_};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     free_tiles(S_);
@@ -146,6 +147,8 @@ void Engine::free_all()
     contact_ = ContactBuffers{};
     S_ = DeviceState{};
     d_perm_ = nullptr;
+    d_stage_ = nullptr;
+    stage_cap_ = 0;
 }
 
 pd_status Engine::allocate()
@@ -941,33 +944,43 @@ void Engine::reset_kernel_times()
 }
 
 // ---- exports -----------------------------------------------------------------------
+pd_status Engine::ensure_stage(size_t bytes)
+{
+    if (bytes <= stage_cap_) return PD_OK;
+    cudaFree(d_stage_);
+    d_stage_ = nullptr;
+    stage_cap_ = 0;
+    CK(cudaMalloc(&d_stage_, bytes), "alloc export staging");
+    stage_cap_ = bytes;
+    return PD_OK;
+}
+
+// Slot-order device array -> caller order on the device, then one copy into
+// the caller's buffer.
 template <typename T>
 pd_status Engine::download_scatter(const T* dev, T* host_out, size_t per, size_t count)
 {
-    std::vector<T> tmp(per * count);
-    if (count) CK(cudaMemcpyAsync(tmp.data(), dev, sizeof(T) * per * count, cudaMemcpyDeviceToHost, stream_), "download");
+    if (count == 0) return PD_OK;
+    const size_t bytes = sizeof(T) * per * count;
+    pd_status s = ensure_stage(bytes);
+    if (s != PD_OK) return s;
+    scatter_words(dev, d_perm_, d_stage_, (int)(sizeof(T) * per / 4), (int)count, stream_);
+    CK(cudaGetLastError(), "export scatter");
+    CK(cudaMemcpyAsync(host_out, d_stage_, bytes, cudaMemcpyDeviceToHost, stream_), "download");
     CK(cudaStreamSynchronize(stream_), "download sync");
-    for (size_t i = 0; i < count; ++i)
-        for (size_t j = 0; j < per; ++j) host_out[(size_t)perm_[i] * per + j] = tmp[i * per + j];
     return PD_OK;
 }
 
 pd_status Engine::export_vec4(const void* dev, bool is_float, double* dst)
 {
     const size_t N = (size_t)n_;
-    if (is_float) {
-        std::vector<float> tmp(4 * N);
-        if (N) CK(cudaMemcpyAsync(tmp.data(), dev, sizeof(float) * 4 * N, cudaMemcpyDeviceToHost, stream_), "download");
-        CK(cudaStreamSynchronize(stream_), "download sync");
-        for (size_t i = 0; i < N; ++i) {
-            double* o = dst + 4 * (size_t)perm_[i];
-            o[0] = tmp[4 * i]; o[1] = tmp[4 * i + 1]; o[2] = tmp[4 * i + 2]; o[3] = 0.0;
-        }
-        return PD_OK;
-    }
-    pd_status s = download_scatter((const double*)dev, dst, 4, N);
+    if (N == 0) return PD_OK;
+    pd_status s = ensure_stage(sizeof(dbl4) * N);
     if (s != PD_OK) return s;
-    for (size_t i = 0; i < N; ++i) dst[4 * i + 3] = 0.0;
+    scatter_to_d4_w0(dev, is_float, d_perm_, (dbl4*)d_stage_, (int)N, stream_);
+    CK(cudaGetLastError(), "export scatter");
+    CK(cudaMemcpyAsync(dst, d_stage_, sizeof(dbl4) * N, cudaMemcpyDeviceToHost, stream_), "download");
+    CK(cudaStreamSynchronize(stream_), "download sync");
     return PD_OK;
 }
 

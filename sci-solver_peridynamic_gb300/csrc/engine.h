@@ -73,6 +73,7 @@ private:
     pd_status solve(const StepParams& P);
     template <typename T>
     pd_status download_scatter(const T* dev, T* host_out, size_t count_per, size_t elem_count);
+    pd_status ensure_stage(size_t bytes);   // device staging buffer of the exports
     pd_status export_vec4(const void* dev, bool real_is_float, double* dst);
     pd_status export_bonds(int64_t* row_ptr_out, int32_t* list_out);
     // profiling
@@ -108,6 +109,8 @@ private:
     long long bonds_initial_ = 0;
     DeviceState S_{};
     int* d_perm_ = nullptr;
+    void* d_stage_ = nullptr;     // exports in caller order before the copy to the host
+    size_t stage_cap_ = 0;
     CgScalars* h_sc_ = nullptr;   // pinned
     int* h_flags_ = nullptr;      // pinned
     LaunchCfg L_{};

@@ -223,6 +223,10 @@ void gather_double(const double* in, const int* perm, double* out, int n, cudaSt
 void gather_int_to_u8(const int* in, const int* perm, uint8_t* out, int n, cudaStream_t st);
 // out[perm[i]] = in[i]
 void scatter_double4(const dbl4* in, const int* perm, dbl4* out, int n, cudaStream_t st);
+// out[perm[i]] = in[i] for rows of words_per_row 32-bit words
+void scatter_words(const void* in, const int* perm, void* out, int words_per_row, int n, cudaStream_t st);
+// out[perm[i]] = (x, y, z, 0) of a float4 (is_float) or double4 row
+void scatter_to_d4_w0(const void* in, bool is_float, const int* perm, dbl4* out, int n, cudaStream_t st);
 // FP32 copies relative to an origin
 void make_local32(const dbl4* X, double ox, double oy, double oz, float4* X32, float4* u32, int n,
                   cudaStream_t st);
