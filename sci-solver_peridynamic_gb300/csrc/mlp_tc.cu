@@ -4,7 +4,9 @@
 // No reference counterpart.  The network (64 -> 128 -> 128 -> 3, GELU, BF16
 // weights and activations, FP32 accumulation) is the one mlp.cu trains; this
 // kernel runs it over every particle row of a step.  Per 128-row tile:
-//   features (BF16, global) -> shared memory          (K-major core matrices)
+//   features (BF16, global) -> shared memory by TMA   (128-byte swizzle; the
+//                              next tile's copy is issued as soon as layer 1
+//                              has read this one, and overlaps the rest)
 //   layer 1  tcgen05.mma  X[128x64]  W1^T -> TMEM columns   0..127 (FP32)
 //   epilogue tcgen05.ld, + b1, GELU, BF16 -> shared memory H
 //   layer 2  tcgen05.mma  H[128x128] W2^T -> TMEM columns 128..255
@@ -19,13 +21,18 @@
 // CTA's whole run over its tiles; two CTAs share an SM (about 102 KB of
 // shared memory and 256 TMEM columns each).
 //
-// Shared-memory operand layout: SWIZZLE_NONE, K-major.  An R x K tile is a
+// Shared-memory operands: the feature tile as TMA writes it with the 128-byte
+// swizzle (row r at r * 128 bytes, its 16-byte chunk c at chunk c ^ (r % 8);
+// descriptor layout SWIZZLE_128B, 8-row groups 1024 bytes apart, an MMA's
+// K = 16 slice 32 bytes further).  Weights and hidden activations, written by
+// threads: SWIZZLE_NONE, K-major.  An R x K tile is a
 // grid of 8 x 8 core matrices (8 rows of 16 bytes, 128 contiguous bytes);
 // core (r/8, k/8) starts at ((r/8) * K/8 + k/8) * 128 bytes.  So the
 // descriptors' leading-dimension byte offset (next core matrix along K) is
 // 128 and the stride-dimension byte offset (next 8-row group) is K * 16; one
 // MMA (K = 16) covers two core matrices along K, the next one starts 256
 // bytes further.  Every byte an MMA reads lies inside its operand tile.
+#include <cuda.h>   // CUtensorMap and its encoder's signature (called through the runtime's entry point)
 #include <cuda_bf16.h>
 
 #include <cstdint>
@@ -51,8 +58,10 @@ constexpr int kOffW3 = kOffW2 + kMlpHidden * kMlpHidden * 2;   // W3^T: 16 x 128
 constexpr int kOffX = kOffW3 + kOutN * kMlpHidden * 2;     // features: 128 x 64
 constexpr int kOffH = kOffX + kTcRows * kMlpIn * 2;        // hidden: 128 x 128
 constexpr int kOffB = kOffH + kTcRows * kMlpHidden * 2;    // biases (f32): 128 + 128 + 16
-constexpr int kOffBar = kOffB + (2 * kMlpHidden + kOutN) * 4;   // mbarrier (8 B), TMEM address (4 B)
-constexpr int kSmemUsed = kOffBar + 16;
+constexpr int kOffBar = kOffB + (2 * kMlpHidden + kOutN) * 4;   // MMA mbarrier, TMA mbarrier, TMEM address
+constexpr int kSmemUsed = kOffBar + 24;
+constexpr uint32_t kTileBytes = kTcRows * kMlpIn * 2;      // one feature tile (16 KB)
+static_assert(kOffX % 1024 == 0, "the swizzled feature tile needs 1024-byte alignment");
 constexpr int kSmemBytes = kSmemUsed + 1024;               // + alignment of the base to 1024 B
 
 __device__ int g_tc_error;   // 1: an mbarrier wait of the tensor-core kernel ran out of time
@@ -68,6 +77,27 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
 {
     return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
            ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// the same for the TMA-written feature tile: 128-byte swizzle (bits 61-63 =
+// 2), 8-row groups 1024 bytes apart; the leading offset is not used by this
+// layout (K of one MMA stays inside the 128-byte swizzle span)
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr)
+{
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) | (1ull << 46) |
+           (2ull << 61);
+}
+
+// TMA: the 64 x 128 box at (0, row0) of the feature matrix into shared
+// memory, completing on bar (whose expected bytes are set just before)
+__device__ __forceinline__ void tma_load_tile(const CUtensorMap* tmap, uint32_t dst, uint32_t bar, int row0)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(kTileBytes) : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            dst),
+        "l"((uint64_t)tmap), "r"(0), "r"(row0), "r"(bar)
+        : "memory");
 }
 
 // instruction descriptor of kind::f16: FP32 accumulator (bits 4-5 = 1), A and
@@ -188,7 +218,7 @@ __device__ __forceinline__ void epilogue_hidden(uint32_t tmem, uint32_t col0, co
 }
 
 __global__ void __launch_bounds__(kTcThreads, 1)
-    k_mlp_infer_tc(const __nv_bfloat16* __restrict__ X, int B, const __nv_bfloat16* __restrict__ w1b,
+    k_mlp_infer_tc(const __grid_constant__ CUtensorMap tmap_x, int B, const __nv_bfloat16* __restrict__ w1b,
                    const __nv_bfloat16* __restrict__ w2b, const __nv_bfloat16* __restrict__ w3b,
                    const float* __restrict__ b1, const float* __restrict__ b2, const float* __restrict__ b3,
                    float* __restrict__ Y)
@@ -201,7 +231,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     float* sb2 = sb1 + kMlpHidden;
     float* sb3 = sb2 + kMlpHidden;
     const uint32_t bar = sbase + kOffBar;
-    const uint32_t tmem_slot = sbase + kOffBar + 8;
+    const uint32_t bar_x = sbase + kOffBar + 8;
+    const uint32_t tmem_slot = sbase + kOffBar + 16;
 
     // weights as K-major B operands (row n of W^T = column n of W) and biases
     for (int i = tid; i < kMlpIn * kMlpHidden; i += blockDim.x) {
@@ -224,6 +255,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     if (tid < kOutN) sb3[tid] = tid < kMlpOut ? b3[tid] : 0.f;
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_x) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -233,9 +265,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     bool ok = tc_sync(true);
-    const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(sm + kOffBar + 8);
-    uint32_t parity = 0;
-    bool pending = false;   // an MMA group was committed and not yet waited for
+    const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(sm + kOffBar + 16);
+    uint32_t parity = 0, parity_x = 0;
+    bool pending = false;     // an MMA group was committed and not yet waited for
+    bool pending_x = false;   // a feature tile copy was issued and not yet waited for
+    const int tiles0 = (B + kTcRows - 1) / kTcRows;
+    if (tid == 0 && (int)blockIdx.x < tiles0) tma_load_tile(&tmap_x, sbase + kOffX, bar_x, (int)blockIdx.x * kTcRows);
+    pending_x = (int)blockIdx.x < tiles0;
 
     constexpr uint32_t id_hidden = instr_desc(kTcRows, kMlpHidden);
     constexpr uint32_t id_out = instr_desc(kTcRows, kOutN);
@@ -245,22 +281,16 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const int tiles = (B + kTcRows - 1) / kTcRows;
     for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
         const int row0 = t * kTcRows;
-        // features: chunk c = 16 bytes (8 values) of row r, columns 8*k8..; a
-        // warp covers 8 rows x 4 chunks (full 32-byte sectors in global memory)
-        for (int c = tid; c < kTcRows * kMlpIn / 8; c += blockDim.x) {
-            const int r = ((c >> 5) & 15) * 8 + (c & 7);
-            const int k8 = (c >> 9) * 4 + ((c >> 3) & 3);
-            uint4 v = make_uint4(0u, 0u, 0u, 0u);
-            if (row0 + r < B) v = *reinterpret_cast<const uint4*>(X + (size_t)(row0 + r) * kMlpIn + 8 * k8);
-            *reinterpret_cast<uint4*>(sm + kOffX + core_off(r, 8 * k8, kMlpIn)) = v;
-        }
+        // this tile's features (rows past B arrive as zeros)
+        ok = mbar_wait(bar_x, parity_x);
+        if (ok) { parity_x ^= 1u; pending_x = false; }
         ok = tc_sync(ok);
         if (!ok) break;
         // layer 1
         if (tid == 0) {
 #pragma unroll
             for (int s = 0; s < kMlpIn / 16; ++s)
-                mma_bf16(tmem, smem_desc(sbase + kOffX + 2 * s * lbo, lbo, sbo_k64),
+                mma_bf16(tmem, smem_desc_sw128(sbase + kOffX + 32 * s),
                          smem_desc(sbase + kOffW1 + 2 * s * lbo, lbo, sbo_k64), id_hidden, s > 0);
             mma_commit(bar);
         }
@@ -269,6 +299,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         if (ok) { parity ^= 1u; pending = false; }
         ok = tc_sync(ok);
         if (!ok) break;
+        // layer 1 has read the feature tile: the next tile's copy overlaps the rest
+        if (t + (int)gridDim.x < tiles) {
+            if (tid == 0) tma_load_tile(&tmap_x, sbase + kOffX, bar_x, (t + (int)gridDim.x) * kTcRows);
+            pending_x = true;
+        }
         epilogue_hidden(tmem, 0, sb1, sm + kOffH, warp, lane);
         ok = tc_sync(ok);
         // layer 2
@@ -313,7 +348,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
     if (!ok) {
         if (tid == 0) atomicExch(&g_tc_error, 1);
-        if (pending) mbar_wait(bar, parity);   // the MMAs in flight, once more (bounded)
+        if (pending) mbar_wait(bar, parity);       // the MMAs in flight, once more (bounded)
+        if (pending_x) mbar_wait(bar_x, parity_x);   // and a feature copy in flight
     }
     tc_sync(true);
     if (warp == 0)
@@ -328,9 +364,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 cudaError_t mlp_infer_tc(const MlpDev& m, const __nv_bfloat16* X, int B, float* Y, cudaStream_t st)
 {
     if (B <= 0) return cudaSuccess;
-    // once per device (the shared-memory opt-in is a per-device attribute)
+    // once per device (the shared-memory opt-in is a per-device attribute);
+    // the tensor-map encoder comes from the driver through the runtime
+    using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
     static std::mutex mtx;
     static int sm_counts[kMaxDevices] = {};
+    static EncodeFn encode_fn = nullptr;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
@@ -347,13 +388,36 @@ cudaError_t mlp_infer_tc(const MlpDev& m, const __nv_bfloat16* X, int B, float* 
             sm_counts[dev] = n;
         }
         sm_count = sm_counts[dev];
+        if (!encode_fn) {
+            void* fn = nullptr;
+            cudaDriverEntryPointQueryResult q;
+            e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+            if (e != cudaSuccess) return e;
+            if (q != cudaDriverEntryPointSuccess || !fn) return cudaErrorNotSupported;
+            encode_fn = (EncodeFn)fn;
+        }
+    }
+    const EncodeFn encode = encode_fn;
+    // the feature matrix as a TMA tensor: 64 BF16 columns x B rows, boxes of
+    // 64 x 128 with the 128-byte swizzle; rows past B read as zeros
+    if (((uintptr_t)X & 15u) != 0) return cudaErrorInvalidValue;
+    CUtensorMap tmap;
+    {
+        const cuuint64_t dims[2] = {(cuuint64_t)kMlpIn, (cuuint64_t)B};
+        const cuuint64_t strides[1] = {(cuuint64_t)kMlpIn * sizeof(__nv_bfloat16)};
+        const cuuint32_t box[2] = {(cuuint32_t)kMlpIn, (cuuint32_t)kTcRows};
+        const cuuint32_t estr[2] = {1u, 1u};
+        const CUresult r = encode(&tmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)X, dims, strides, box, estr,
+                                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
     }
     const float* b1 = m.params + kMlpIn * kMlpHidden;
     const float* b2 = b1 + kMlpHidden + kMlpHidden * kMlpHidden;
     const float* b3 = b2 + kMlpHidden + kMlpHidden * kMlpOut;
     const int tiles = (B + kTcRows - 1) / kTcRows;
     const int grid = tiles < 2 * sm_count ? tiles : 2 * sm_count;
-    k_mlp_infer_tc<<<grid, kTcThreads, kSmemBytes, st>>>(X, B, m.w1b, m.w2b, m.w3b, b1, b2, b3, Y);
+    k_mlp_infer_tc<<<grid, kTcThreads, kSmemBytes, st>>>(tmap, B, m.w1b, m.w2b, m.w3b, b1, b2, b3, Y);
     return cudaGetLastError();
 }
 
