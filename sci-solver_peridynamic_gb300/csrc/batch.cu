@@ -402,7 +402,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_batch_ws_guess(BatchArgs A)
 // WS: with the learned warm start (a separate instantiation, so the plain
 // kernels keep their register budget).
 template <bool FP64, bool WS>
-__global__ void __launch_bounds__(kBlock) k_batch_pre(BatchArgs A)
+__global__ void __launch_bounds__(kBlock, FP64 ? 1 : 3) k_batch_pre(BatchArgs A)
 {
     using Real = typename std::conditional<FP64, double, float>::type;
     using Acc = typename DotAccFor<Real>::type;
