@@ -3,15 +3,15 @@
 // No reference counterpart (the reference starts each CG from the previous
 // solution, src/core/simulator.cu:745-770).  A small network
 //   64 features -> 128 -> 128 -> 3,  GELU,  BF16 weights/activations,
-//   FP32 accumulation (mma.sync m16n8k16), FP32 master weights + Adam
+//   FP32 accumulation on tcgen05 (mlp_tc.cu), FP32 master weights + Adam
 // predicts the change of the solution over its previous value; the CG then
 // runs to the same tolerance from the predicted guess, so the network only
 // changes the iteration count, never the convergence test.
 //
-// GEMMs: each warp computes a 16 x 32 tile of C = op(A) op(B) with the
-// operands read straight from global memory into mma fragments (bounds are
-// zero-filled).  The layer sizes are small (K <= 128), so the GEMMs are
-// bandwidth-bound on the activations and a plain fragment kernel suffices.
+// Training runs each layer's forward and backward products as GEMMs on the
+// 5th-generation tensor cores (gemm_tc: 128 x 128 tiles of C, K in slabs of
+// 64, TMEM accumulators); inference runs the whole network in one kernel
+// (mlp_infer_tc).
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -28,78 +28,6 @@ namespace pdgb {
 void set_handleless_error(const std::string& msg);   // capi.cpp
 
 namespace {
-
-__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
-{
-    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-    return *reinterpret_cast<const uint32_t*>(&v);
-}
-
-template <bool T>
-__device__ __forceinline__ float load_op(const __nv_bfloat16* __restrict__ P, int ld, int r, int c, int R, int Cn)
-{
-    // op(P)[r][c]: P stored row-major (T = false) or its transpose stored row-major (T = true)
-    if (r >= R || c >= Cn) return 0.f;
-    return __bfloat162float(T ? P[(size_t)c * ld + r] : P[(size_t)r * ld + c]);
-}
-
-// C[M x N] (f32, row-major, ldc) = op(A)[M x K] * op(B)[K x N] (+ C if accumulate)
-template <bool TA, bool TB>
-__global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const __nv_bfloat16* __restrict__ A, int lda,
-                                                   const __nv_bfloat16* __restrict__ B, int ldb, float* __restrict__ C,
-                                                   int ldc, int accumulate)
-{
-    const int warp = threadIdx.x >> 5;
-    const int lane = threadIdx.x & 31;
-    const int g = lane >> 2;       // group id
-    const int t = lane & 3;        // thread in group
-    const int m0 = (blockIdx.x * 4 + warp) * 16;
-    const int n0 = blockIdx.y * 32;
-    if (m0 >= M) return;
-    float acc[4][4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-        for (int i = 0; i < 4; ++i) acc[j][i] = 0.f;
-    for (int k0 = 0; k0 < K; k0 += 16) {
-        uint32_t a[4];
-        a[0] = pack_bf16(load_op<TA>(A, lda, m0 + g, k0 + 2 * t, M, K), load_op<TA>(A, lda, m0 + g, k0 + 2 * t + 1, M, K));
-        a[1] = pack_bf16(load_op<TA>(A, lda, m0 + g + 8, k0 + 2 * t, M, K),
-                         load_op<TA>(A, lda, m0 + g + 8, k0 + 2 * t + 1, M, K));
-        a[2] = pack_bf16(load_op<TA>(A, lda, m0 + g, k0 + 2 * t + 8, M, K),
-                         load_op<TA>(A, lda, m0 + g, k0 + 2 * t + 9, M, K));
-        a[3] = pack_bf16(load_op<TA>(A, lda, m0 + g + 8, k0 + 2 * t + 8, M, K),
-                         load_op<TA>(A, lda, m0 + g + 8, k0 + 2 * t + 9, M, K));
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int n = n0 + 8 * j + g;
-            uint32_t b[2];
-            b[0] = pack_bf16(load_op<TB>(B, ldb, k0 + 2 * t, n, K, N), load_op<TB>(B, ldb, k0 + 2 * t + 1, n, K, N));
-            b[1] = pack_bf16(load_op<TB>(B, ldb, k0 + 2 * t + 8, n, K, N), load_op<TB>(B, ldb, k0 + 2 * t + 9, n, K, N));
-            asm volatile(
-                "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
-                "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
-                : "+f"(acc[j][0]), "+f"(acc[j][1]), "+f"(acc[j][2]), "+f"(acc[j][3])
-                : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-        }
-    }
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const int c0 = n0 + 8 * j + 2 * t;
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int r = m0 + g + 8 * h;
-            if (r >= M) continue;
-#pragma unroll
-            for (int e = 0; e < 2; ++e) {
-                const int c = c0 + e;
-                if (c >= N) continue;
-                float* dst = C + (size_t)r * ldc + c;
-                *dst = accumulate ? *dst + acc[j][2 * h + e] : acc[j][2 * h + e];
-            }
-        }
-    }
-}
 
 __device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
 __device__ __forceinline__ float gelu_grad(float x)
@@ -197,12 +125,14 @@ int blocks_for(long long n, int threads = 256)
     return (int)b;
 }
 
+// C = op(A) op(B) (+ C) on the tensor cores (mlp_tc.cu); launch errors surface
+// at the pass's next error check, a wait that ran out of time through
+// mlp_tc_take_error
 template <bool TA, bool TB>
 void gemm(int M, int N, int K, const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, float* C, int ldc,
           bool accumulate, cudaStream_t st)
 {
-    dim3 grid((M + 63) / 64, (N + 31) / 32);
-    k_gemm_bf16<TA, TB><<<grid, 128, 0, st>>>(M, N, K, A, lda, B, ldb, C, ldc, accumulate ? 1 : 0);
+    gemm_tc(TA, TB, M, N, K, A, lda, B, ldb, C, ldc, accumulate, st);
 }
 
 }  // namespace
@@ -484,6 +414,11 @@ extern "C" pd_status pd_mlp_loss_grad(int device, const float* X, const float* T
     MLP_TRY(cudaMemcpyAsync(grad, s.m.grad, pdgb::mlp_param_count() * sizeof(float), cudaMemcpyDeviceToHost, s.st));
     MLP_TRY(cudaMemcpyAsync(loss, s.loss, sizeof(double), cudaMemcpyDeviceToHost, s.st));
     MLP_TRY(cudaStreamSynchronize(s.st));
+    MLP_TRY(cudaGetLastError());
+    if (pdgb::mlp_tc_take_error()) {
+        pdgb::set_handleless_error("pd_mlp_loss_grad: a tensor-core wait ran out of time");
+        return PD_ERR_CUDA;
+    }
     return PD_OK;
 }
 
@@ -545,5 +480,10 @@ extern "C" pd_status pd_mlp_train(int device, const float* X, const float* T, lo
     if (final_loss) *final_loss = total / (double)rows;
     MLP_TRY(cudaMemcpyAsync(params, s.m.params, pdgb::mlp_param_count() * sizeof(float), cudaMemcpyDeviceToHost, s.st));
     MLP_TRY(cudaStreamSynchronize(s.st));
+    MLP_TRY(cudaGetLastError());
+    if (pdgb::mlp_tc_take_error()) {
+        pdgb::set_handleless_error("pd_mlp_train: a tensor-core wait ran out of time");
+        return PD_ERR_CUDA;
+    }
     return PD_OK;
 }

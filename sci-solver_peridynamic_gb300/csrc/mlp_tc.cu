@@ -356,7 +356,138 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
 }
 
+// ---- general GEMM of the training passes ----------------------------------------------
+// C[M x N] (FP32, row-major, ldc) = op(A)[M x K] op(B)[K x N] (+ C), BF16
+// operands; op(P) is P (row-major) or, with TA / TB, its transpose.  One CTA
+// per 128 x 128 tile of C: K in slabs of 64, each slab's operands written by
+// the threads into K-major core-matrix tiles (transposing where asked), four
+// tcgen05.mma (K = 16) accumulating in TMEM, then the epilogue.
+constexpr int kGemmSlab = 64;
+constexpr int kGemmOffA = 0;                                   // 128 x 64
+constexpr int kGemmOffB = kGemmOffA + 128 * kGemmSlab * 2;     // 128 x 64
+constexpr int kGemmOffBar = kGemmOffB + 128 * kGemmSlab * 2;   // mbarrier, TMEM address
+// requested shared memory: limits residency to 3 CTAs per SM (3 x 128 TMEM columns)
+constexpr int kGemmSmemBytes = 58 * 1024;
+
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_gemm_tc(int M, int N, int K, const __nv_bfloat16* __restrict__ A, int lda, const __nv_bfloat16* __restrict__ B,
+              int ldb, float* __restrict__ C, int ldc, int accumulate)
+{
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(sm);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.x * 128, n0 = blockIdx.y * 128;
+    const int nt = (N - n0 < 128 ? N - n0 : 128);
+    const int nmma = (nt + 15) & ~15;   // MMA N: a multiple of 16
+    const uint32_t bar = sbase + kGemmOffBar;
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sbase + kGemmOffBar + 8),
+                     "r"(128u)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    bool ok = tc_sync(true);
+    const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(sm + kGemmOffBar + 8);
+    const uint32_t idesc = instr_desc(128, nmma);
+    uint32_t parity = 0;
+    bool pending = false;
+    for (int k0 = 0; k0 < K && ok; k0 += kGemmSlab) {
+        // op(A) rows m0.., columns k0..: consecutive threads walk the
+        // contiguous direction of A in memory
+        for (int i = tid; i < 128 * kGemmSlab; i += blockDim.x) {
+            const int m = TA ? (i & 127) : (i >> 6), kk = TA ? (i >> 7) : (i & 63);
+            const int gm = m0 + m, gk = k0 + kk;
+            __nv_bfloat16 v = __float2bfloat16_rn(0.f);
+            if (gm < M && gk < K) v = TA ? A[(size_t)gk * lda + gm] : A[(size_t)gm * lda + gk];
+            *reinterpret_cast<__nv_bfloat16*>(sm + kGemmOffA + core_off(m, kk, kGemmSlab)) = v;
+        }
+        // the B operand is op(B)^T: row n holds op(B)[k0.., n0 + n]
+        for (int i = tid; i < 128 * kGemmSlab; i += blockDim.x) {
+            const int n = TB ? (i >> 6) : (i & 127), kk = TB ? (i & 63) : (i >> 7);
+            const int gn = n0 + n, gk = k0 + kk;
+            __nv_bfloat16 v = __float2bfloat16_rn(0.f);
+            if (gn < N && gk < K) v = TB ? B[(size_t)gn * ldb + gk] : B[(size_t)gk * ldb + gn];
+            *reinterpret_cast<__nv_bfloat16*>(sm + kGemmOffB + core_off(n, kk, kGemmSlab)) = v;
+        }
+        ok = tc_sync(ok);
+        if (!ok) break;
+        if (tid == 0) {
+#pragma unroll
+            for (int s = 0; s < kGemmSlab / 16; ++s)
+                mma_bf16(tmem, smem_desc(sbase + kGemmOffA + 256 * s, 128, kGemmSlab * 16),
+                         smem_desc(sbase + kGemmOffB + 256 * s, 128, kGemmSlab * 16), idesc, (k0 > 0 || s > 0) ? 1u : 0u);
+            mma_commit(bar);
+        }
+        pending = true;
+        ok = mbar_wait(bar, parity);
+        if (ok) { parity ^= 1u; pending = false; }
+        ok = tc_sync(ok);
+    }
+    if (ok && warp < 4) {
+        const int row = 32 * warp + lane, gm = m0 + row;
+        for (int c0 = 0; c0 < nmma; c0 += 16) {
+            float v[16];
+            if (K > 0) tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
+            else
+                for (int i = 0; i < 16; ++i) v[i] = 0.f;
+            if (gm < M)
+                for (int i = 0; i < 16; ++i) {
+                    const int gn = n0 + c0 + i;
+                    if (gn >= N) break;
+                    float* dst = C + (size_t)gm * ldc + gn;
+                    *dst = accumulate ? *dst + v[i] : v[i];
+                }
+        }
+    }
+    if (!ok) {
+        if (tid == 0) atomicExch(&g_tc_error, 1);
+        if (pending) mbar_wait(bar, parity);
+    }
+    tc_sync(true);
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(128u) : "memory");
+}
+
 }  // namespace
+
+template <bool TA, bool TB>
+static cudaError_t gemm_tc_t(int M, int N, int K, const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb,
+                             float* C, int ldc, bool accumulate, cudaStream_t st)
+{
+    static std::mutex mtx;
+    static bool configured[kMaxDevices] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    {
+        std::lock_guard<std::mutex> lock(mtx);
+        if (!configured[dev]) {
+            e = cudaFuncSetAttribute(k_gemm_tc<TA, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmemBytes);
+            if (e != cudaSuccess) return e;
+            configured[dev] = true;
+        }
+    }
+    const dim3 grid((unsigned)((M + 127) / 128), (unsigned)((N + 127) / 128));
+    k_gemm_tc<TA, TB><<<grid, kTcThreads, kGemmSmemBytes, st>>>(M, N, K, A, lda, B, ldb, C, ldc, accumulate ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t gemm_tc(bool ta, bool tb, int M, int N, int K, const __nv_bfloat16* A, int lda, const __nv_bfloat16* B,
+                    int ldb, float* C, int ldc, bool accumulate, cudaStream_t st)
+{
+    if (M <= 0 || N <= 0) return cudaSuccess;
+    if (!ta && !tb) return gemm_tc_t<false, false>(M, N, K, A, lda, B, ldb, C, ldc, accumulate, st);
+    if (ta && !tb) return gemm_tc_t<true, false>(M, N, K, A, lda, B, ldb, C, ldc, accumulate, st);
+    if (!ta && tb) return gemm_tc_t<false, true>(M, N, K, A, lda, B, ldb, C, ldc, accumulate, st);
+    return gemm_tc_t<true, true>(M, N, K, A, lda, B, ldb, C, ldc, accumulate, st);
+}
 
 // Y[B x kMlpOutPad] (columns 0..2 used) = network(X[B x 64]) on the tensor
 // cores.  Launch errors are returned; a wait that ran out of time is reported

@@ -282,6 +282,9 @@ struct WsState {
 size_t mlp_param_count();
 void mlp_refresh_bf16(MlpDev& m, cudaStream_t st);
 void mlp_forward(const MlpDev& m, const __nv_bfloat16* X, int B, MlpWork& ws, float* Y, cudaStream_t st);
+// C[M x N] (f32, ldc) = op(A) op(B) (+ C) on tcgen05, op = transpose when ta / tb (mlp_tc.cu)
+cudaError_t gemm_tc(bool ta, bool tb, int M, int N, int K, const __nv_bfloat16* A, int lda, const __nv_bfloat16* B,
+                    int ldb, float* C, int ldc, bool accumulate, cudaStream_t st);
 // inference only (mlp_tc.cu): all layers in one tcgen05 kernel, Y [B x 8]
 cudaError_t mlp_infer_tc(const MlpDev& m, const __nv_bfloat16* X, int B, float* Y, cudaStream_t st);
 // 1 if a wait of the tensor-core kernel ran out of time since the last call
