@@ -327,7 +327,8 @@ pd_status pd_mlp_init(unsigned seed, float* params);
 /* Y[rows x 3] = MLP(X[rows x 64]) on `device` (inputs rounded to BF16).
  * Inference runs as one tcgen05 kernel per 128-row tile (TMEM accumulators,
  * the three layers and their bias/GELU fused), as the warm start does each
- * step; training (loss_grad, train) uses separate BF16 GEMM kernels. */
+ * step; training (loss_grad, train) runs each layer's products as separate
+ * tcgen05 GEMMs. */
 pd_status pd_mlp_predict(int device, const float* X, long long rows, const float* params, float* Y);
 /* Mean squared error over rows (sum over the 3 outputs) and its gradient. */
 pd_status pd_mlp_loss_grad(int device, const float* X, const float* T, int rows, const float* params, float* grad,
