@@ -192,7 +192,10 @@ typedef struct pd_step_stats {
 } pd_step_stats;
 
 /* Device time per kernel class, accumulated with CUDA events on the handle's
- * stream while profiling is on (pd_set_profiling). */
+ * stream while profiling is on (pd_set_profiling).  Force and update launches
+ * are each timed; the CG loop's SpMV and vector launches are timed on every
+ * 8th iteration and total_ms is their mean duration times the exact count of
+ * live launches. */
 typedef enum pd_kernel_class {
     PD_KC_FORCE = 0, PD_KC_SPMV = 1, PD_KC_CG_VECTOR = 2, PD_KC_UPDATE = 3, PD_KC_COUNT = 4
 } pd_kernel_class;

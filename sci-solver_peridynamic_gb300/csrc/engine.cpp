@@ -839,13 +839,17 @@ pd_status Engine::solve(const StepParams& P)
     int launched = 0;
     for (;;) {
         for (int k = 0; k < batch; ++k) {
-            mark_begin(PD_KC_SPMV, launched);
+            // profiling times every kMarkStride-th iteration so that the
+            // event records barely perturb the solve they measure; the mean
+            // sampled duration is scaled to the exact launch count
+            const bool sample = (launched % kMarkStride) == 0;
+            if (sample) mark_begin(PD_KC_SPMV, launched);
             launch_spmv(fp64_, true, P, S_, L_, stream_);
-            mark_end();
-            mark_begin(PD_KC_CG_VECTOR, launched);
+            if (sample) mark_end();
+            if (sample) mark_begin(PD_KC_CG_VECTOR, launched);
             launch_cg_axpy(fp64_, P, S_, L_, stream_);
             launch_cg_xpby(fp64_, P, S_, L_, stream_);
-            mark_end();
+            if (sample) mark_end();
             ++launched;
         }
         launches_ += 3LL * batch;
@@ -865,6 +869,10 @@ pd_status Engine::solve(const StepParams& P)
     total_iters_ += last_iters_;
     predicted_iters_ = std::max(1, last_iters_);
     flush_marks(last_iters_);
+    if (profiling_) {
+        kc_launches_[PD_KC_SPMV] += last_iters_;
+        kc_launches_[PD_KC_CG_VECTOR] += 2LL * last_iters_;
+    }
     if (!h_sc_->converged) cg_converged_ = false;
     if (ws_features_needed()) return ws_after_cg(P);
     return PD_OK;
@@ -912,8 +920,14 @@ void Engine::flush_marks(int live_iters)
         if (!dead) {
             float ms = 0.f;
             if (cudaEventElapsedTime(&ms, m.a, m.b) == cudaSuccess) {
-                kc_ms_[m.kc] += ms;
-                kc_launches_[m.kc] += (m.kc == PD_KC_CG_VECTOR) ? 2 : 1;
+                if (m.kc == PD_KC_SPMV || m.kc == PD_KC_CG_VECTOR) {
+                    // a sampled CG iteration; launches are counted per solve
+                    kc_sample_ms_[m.kc] += ms;
+                    kc_samples_[m.kc] += 1;
+                } else {
+                    kc_ms_[m.kc] += ms;
+                    kc_launches_[m.kc] += 1;
+                }
             }
         }
         event_pool_.push_back(m.a);
@@ -930,6 +944,11 @@ pd_status Engine::kernel_times(pd_kernel_times* t)
     for (int k = 0; k < PD_KC_COUNT; ++k) {
         t->launches[k] = kc_launches_[k];
         t->total_ms[k] = kc_ms_[k];
+        if (k == PD_KC_SPMV || k == PD_KC_CG_VECTOR) {
+            // mean duration of the sampled iterations x live iterations
+            const long long iters = k == PD_KC_CG_VECTOR ? kc_launches_[k] / 2 : kc_launches_[k];
+            t->total_ms[k] = kc_samples_[k] ? kc_sample_ms_[k] / (double)kc_samples_[k] * (double)iters : 0.0;
+        }
     }
     return PD_OK;
 }
@@ -940,6 +959,8 @@ void Engine::reset_kernel_times()
     for (int k = 0; k < PD_KC_COUNT; ++k) {
         kc_launches_[k] = 0;
         kc_ms_[k] = 0.0;
+        kc_samples_[k] = 0;
+        kc_sample_ms_[k] = 0.0;
     }
 }
 

@@ -13,6 +13,9 @@ namespace pdgb {
 
 class Batch;
 
+// profiling: CG-loop kernels are timed on every kMarkStride-th iteration
+constexpr int kMarkStride = 8;
+
 class Engine {
     friend class Batch;   // the multi-scene step drives the scenes' device state
 
@@ -150,6 +153,8 @@ private:
     int open_mark_ = -1;
     long long kc_launches_[PD_KC_COUNT] = {0, 0, 0, 0};
     double kc_ms_[PD_KC_COUNT] = {0, 0, 0, 0};
+    long long kc_samples_[PD_KC_COUNT] = {0, 0, 0, 0};   // sampled CG iterations
+    double kc_sample_ms_[PD_KC_COUNT] = {0, 0, 0, 0};
     long long launches_ = 0;
     ContactBuffers contact_{};         // PD-PD contact hash (when enabled)
     size_t saved_frame_ = 0;           // DataIO::savedFrame
