@@ -80,6 +80,7 @@ def _load():
         lib.pdo_destroy.argtypes = [C.c_void_p]
         lib.pdo_set_particles.argtypes = [C.c_void_p, dp, dp, ip]
         lib.pdo_set_stretch.argtypes = [C.c_void_p, dp]
+        lib.pdo_set_position.argtypes = [C.c_void_p, dp]
         lib.pdo_make_ready.argtypes = [C.c_void_p]
         lib.pdo_advance.argtypes = [C.c_void_p]
         lib.pdo_force_pass.argtypes = [C.c_void_p, ip]
@@ -148,6 +149,12 @@ class OracleSim:
         act = np.zeros(self.n, np.int32) if act is None else np.ascontiguousarray(act, np.int32)
         self._keep = (pos4, vel4, act)
         self.lib.pdo_set_particles(self.h, _dp(pos4), _dp(vel4), _ip(act))
+
+    def set_position(self, pos4):
+        """Current positions only (test hook); reference positions are kept."""
+        pos4 = np.ascontiguousarray(pos4, np.float64).reshape(self.n, 4)
+        self._pos_keep = pos4
+        self.lib.pdo_set_position(self.h, _dp(pos4))
 
     def set_stretch(self, s0):
         s0 = np.ascontiguousarray(s0, np.float64)

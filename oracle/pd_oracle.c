@@ -130,6 +130,15 @@ int pdo_set_particles(pdo_state* s, const double* pos4, const double* vel4, cons
     return 0;
 }
 
+/* Test hook with no reference counterpart: overwrite the current positions
+ * (pd_position) after make_ready, keeping the reference positions, so that a
+ * force pass can be evaluated at a chosen deformed state. */
+int pdo_set_position(pdo_state* s, const double* pos4)
+{
+    memcpy(s->pos, pos4, 4 * (size_t)s->n * sizeof(double));
+    return 0;
+}
+
 int pdo_set_stretch(pdo_state* s, const double* s0)
 {
     memcpy(s->ost, s0, (size_t)s->n * sizeof(double));

@@ -84,6 +84,8 @@ void pdo_destroy(pdo_state* s);
 /* pos4/vel4: n*4 doubles (x,y,z,w).  act: n ints (may be NULL = all ACTIVE). */
 int pdo_set_particles(pdo_state* s, const double* pos4, const double* vel4, const int* act);
 /* Optional caller-supplied per-particle stretch limits (else srand(1973) procedure). */
+/* test hook: current positions only (reference positions unchanged) */
+int pdo_set_position(pdo_state* s, const double* pos4);
 int pdo_set_stretch(pdo_state* s, const double* s0);
 /* Bond construction + s0 sampling.  Returns 0, or -1 if a row exceeds max_bonds. */
 int pdo_make_ready(pdo_state* s);

@@ -4,34 +4,9 @@ assembled matrix A = M + beta h^2 K applied by computeAx's restatement
 import numpy as np
 import pytest
 
-from helpers import make_oracle
+from helpers import apply_on_device, make_oracle
 
 pytestmark = pytest.mark.gpu
-
-
-def apply_on_device(pdgb, sim, x_caller, entry=None):
-    """y = A x through the C ABI; x, y in caller order.  Returns (y, <x, A x>)."""
-    import torch
-    v = sim.operator_view()
-    n = v.n
-    dt = torch.float32 if v.precision == pdgb.PRECISION_MIXED else torch.float64
-    perm = sim.get(pdgb.VAR_SLOT_PERMUTATION)
-    x_slot = torch.zeros((n, 4), dtype=dt, device="cuda")
-    x_slot[:, :3] = torch.as_tensor(x_caller[perm, :3], dtype=dt, device="cuda")
-    y_slot = torch.full_like(x_slot, float("nan"))
-    dot = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda")
-    torch.cuda.synchronize()
-    if entry is None:
-        sim.apply_operator(x_slot.data_ptr(), y_slot.data_ptr(), dot.data_ptr())
-    else:
-        entry(v, x_slot.data_ptr(), y_slot.data_ptr(), dot.data_ptr())
-    sim.synchronize()
-    torch.cuda.synchronize()
-    y = np.zeros((n, 4))
-    y[perm] = y_slot.double().cpu().numpy()
-    xs = np.zeros((n, 4))
-    xs[perm] = x_slot.double().cpu().numpy()
-    return y, float(dot.item()), xs
 
 
 def _scene(pdgb, scenes, precision):

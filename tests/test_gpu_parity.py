@@ -8,7 +8,7 @@ velocities within the stated tolerances:
 import numpy as np
 import pytest
 
-from helpers import make_oracle, rel_err, same_sets
+from helpers import apply_on_device, make_oracle, rel_err, same_sets
 
 pytestmark = pytest.mark.gpu
 
@@ -199,3 +199,66 @@ def test_pd_pd_contact(pdgb, scenes, precision, tol):
     x, xf = sim.get(pdgb.VAR_POSITION), free.get(pdgb.VAR_POSITION)
     n = x.shape[0] // 2
     assert x[:n, 0].max() < xf[:n, 0].max() - 0.2 * sc.info["spacing"]
+
+
+@pytest.mark.parametrize("precision", [1, 0])
+def test_small_block_closed_form(pdgb, scenes, precision):
+    """Known answer through the C ABI, no oracle: a jittered 2 x 2 x 2 block
+    in which every pair is a bond shorter than horizon - r (vscale 1).  After
+    one step, the next force pass and the operator A = m I + t2 K equal the
+    closed forms of calculatePDForceDerivative (cg_solver.cuh:200-339) at the
+    positions read back: f_p = c sum_q (d/d0 - 1) e_pq, K_pq = -J_pq,
+    K_pp = sum_q J_pq, J = (c/d0)[(1 - d0/d) I + (d0/d) e e^T], with e the
+    bond vector over its float-rounded length."""
+    sc = scenes.reference_block(n_side=2, jitter=0.05, s0=0.5, drop=0.0)
+    sc.opt.precision = precision
+    for k in range(3):
+        sc.opt.gravity[k] = 0.0
+    sim = scenes.make_simulator(sc)
+    sim.makeReady()
+    sim.advance(1)
+    x = sim.get(pdgb.VAR_POSITION)[:, :3]
+    X = sim.get(pdgb.VAR_ORIGINAL_POSITION)[:, :3]
+    sim.advance(1)
+    F = sim.get(pdgb.VAR_FORCE)[:, :3]
+    n = sc.n
+    assert list(sim.get(pdgb.VAR_BOND_COUNT)) == [n - 1] * n
+    v = sim.operator_view()
+    c, m, t2 = v.bond_coeff, v.mass, v.t2
+    horizon = sc.sim.pd_horizon
+    f = np.zeros((n, 3))
+    K = np.zeros((3 * n, 3 * n))
+    smin = 1.0
+    for p in range(n):
+        for q in range(n):
+            if q == p:
+                continue
+            dx = x[q] - x[p]
+            d = np.sqrt(np.dot(dx, dx))
+            e = dx / float(np.float32(d))
+            d0 = np.sqrt(np.dot(X[p] - X[q], X[p] - X[q]))
+            assert d0 <= horizon - sc.sim.pd_particle_radius
+            s = d / d0 - 1.0
+            smin = min(smin, abs(s))
+            f[p] += c * s * e
+            J = (c / d0) * ((1.0 - d0 / d) * np.eye(3) + (d0 / d) * np.outer(e, e))
+            K[3 * p:3 * p + 3, 3 * p:3 * p + 3] += J
+            K[3 * p:3 * p + 3, 3 * q:3 * q + 3] -= J
+    assert smin > 1e-5   # the block is deformed: every bond carries a force
+    rng = np.random.default_rng(2)
+    w = np.zeros((n, 4))
+    w[:, :3] = rng.standard_normal((n, 3))
+    y, dot, ws = apply_on_device(pdgb, sim, w)
+    ws = ws[:, :3]
+    y_ref = m * ws + t2 * (K @ ws.reshape(-1)).reshape(n, 3)
+    fscale = np.abs(f).max()
+    if precision == pdgb.PRECISION_FP64:
+        # s = d/d0 - 1 carries the rounding of d and d0 amplified by 1/s
+        assert np.abs(F - f).max() <= 1e-14 / smin * fscale
+        assert np.abs(y[:, :3] - y_ref).max() <= 1e-12 * np.abs(y_ref).max()
+        assert abs(dot - float(np.sum(ws * y_ref))) <= 1e-12 * abs(dot)
+    else:
+        # FP32 positions: each stretch within ~1e-6 of its FP64 value
+        assert np.abs(F - f).max() <= 1e-6 * (n - 1) * c
+        assert np.abs(y[:, :3] - y_ref).max() <= 2e-5 * np.abs(y_ref).max()
+        assert abs(dot - float(np.sum(ws * y_ref))) <= 2e-5 * abs(dot)
