@@ -436,6 +436,40 @@ __device__ __forceinline__ void spmv_finish_mixed(const StepParams& P, const Dev
     }
 }
 
+// U bonds of one lane in mixed precision: gathers of the neighbours'
+// supercell positions and CG entries (every load issued before any
+// arithmetic), then each bond's Jacobian applied to w_p - w_q and added to
+// (ax, ay, az).  qq[u] < 0 marks an empty slot.
+template <int U, int LD, typename Real>
+__device__ __forceinline__ void mixed_bond_chunk(const float4* __restrict__ xs4, const float4* __restrict__ in32,
+                                                 const float4& xp4, int wp, float sup, const float4& w, int p,
+                                                 const int (&qq)[U], const float (&id0)[U], Real& ax, Real& ay,
+                                                 Real& az)
+{
+    float4 Xq[U], Wq[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int q = qq[u] < 0 ? p : qq[u];
+        Xq[u] = ld_pos<LD>(xs4 + q);
+        Wq[u] = ld_in<LD>(in32 + q);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        if (qq[u] < 0) continue;
+        float cx, cy, cz;
+        supercell_delta(__float_as_int(Xq[u].w), wp, sup, cx, cy, cz);
+        const float xs = (Xq[u].x - xp4.x) + cx, ys = (Xq[u].y - xp4.y) + cy, zs = (Xq[u].z - xp4.z) + cz;
+        const float inv_d0 = id0[u];
+        const float inv_d = rsqrtf(fmaf(xs, xs, fmaf(ys, ys, zs * zs)));
+        const float wx = w.x - Wq[u].x, wy = w.y - Wq[u].y, wz = w.z - Wq[u].z;
+        const float a1 = inv_d0 - inv_d;
+        const float g = fmaf(xs, wx, fmaf(ys, wy, zs * wz)) * (inv_d * inv_d * inv_d);
+        ax = fmaf(a1, wx, fmaf(g, xs, (float)ax));
+        ay = fmaf(a1, wy, fmaf(g, ys, (float)ay));
+        az = fmaf(a1, wz, fmaf(g, zs, (float)az));
+    }
+}
+
 // y_p = (A w)_p by particle p's G-lane group: mass + (beta h^2) stiffness with
 // Dirichlet rows projected out.  DOT: lane 0 adds w_p . y_p to acc.
 // LD: load path of the positions and of w (kLd*).
@@ -502,28 +536,8 @@ __device__ __forceinline__ void spmv_row(const StepParams& P, const DeviceState&
 #pragma unroll
             for (int u = 1; u < U; ++u)
                 if (j0 + u >= cn) qq[u] = -1;
-            float4 Xq[U], Wq[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int q = qq[u] < 0 ? p : qq[u];
-                Xq[u] = ld_pos<LD>(xs4 + q);
-                Wq[u] = ld_in<LD>(in32 + q);
-            }
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                if (qq[u] < 0) continue;
-                float cx, cy, cz;
-                supercell_delta(__float_as_int(Xq[u].w), wp, sup, cx, cy, cz);
-                const float xs = (Xq[u].x - xp4.x) + cx, ys = (Xq[u].y - xp4.y) + cy, zs = (Xq[u].z - xp4.z) + cz;
-                const float inv_d0 = id0[u];
-                const float inv_d = rsqrtf(fmaf(xs, xs, fmaf(ys, ys, zs * zs)));
-                const float wx = (float)w.x - Wq[u].x, wy = (float)w.y - Wq[u].y, wz = (float)w.z - Wq[u].z;
-                const float a1 = inv_d0 - inv_d;
-                const float g = fmaf(xs, wx, fmaf(ys, wy, zs * wz)) * (inv_d * inv_d * inv_d);
-                ax = fmaf(a1, wx, fmaf(g, xs, (float)ax));
-                ay = fmaf(a1, wy, fmaf(g, ys, (float)ay));
-                az = fmaf(a1, wz, fmaf(g, zs, (float)az));
-            }
+            mixed_bond_chunk<U, LD>(xs4, in32, xp4, wp, sup, make_float4((float)w.x, (float)w.y, (float)w.z, 0.f), p,
+                                    qq, id0, ax, ay, az);
         }
     }
     if constexpr (!FP64) {
