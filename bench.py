@@ -59,6 +59,9 @@ def parse_args(argv=None):
                     help="ellipsoid: the 1M-particle headline; batched: 64 scenes in one batch; learned: "
                          "learned vs plain CG warm start on the 16^3 cube; beam: FP32 vs FP64 notched beam")
     ap.add_argument("--check-every", type=int, default=10, help="beam: steps between FP32/FP64 comparisons")
+    ap.add_argument("--warm-start", type=int, default=0, choices=(0, 2),
+                    help="ellipsoid: CG initial guess, 0 previous solution (the reference's), 2 history projection")
+    ap.add_argument("--history", type=int, default=0, help="warm start 2: solutions kept (0 = 8)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args(argv)
@@ -225,6 +228,8 @@ def run_gb300(args):
     if args.unroll:
         sc.opt.spmv_unroll = args.unroll
     sc.opt.spmv_path = args.spmv_path
+    sc.opt.warm_start = args.warm_start
+    sc.opt.history_size = args.history
     sim = scenes.make_simulator(sc, device=local)
     sim.makeReady()
     sim.advance(args.warmup)
@@ -290,6 +295,9 @@ def run_gb300(args):
             "particles": n,
             "bonds_alive": int(bonds),
             "cg_iterations_per_step": round(iters / args.steps, 2),
+            "cg_initial_guess": ("previous solution (the reference's)" if args.warm_start == 0 else
+                                 "history projection: previous solution + Galerkin correction in the span of "
+                                 "the last %d solutions" % (sim.params()[2].history_size or 8)),
             "spmv_variant": "%s, %d lanes x %d unroll (%s)" % (
                 "shared-memory tiles" if sim.params()[2].spmv_path == 1 else "per-bond gathers",
                 sim.params()[2].lanes_per_particle, sim.params()[2].spmv_unroll,

@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define PD_GB300_ABI_VERSION 2
+#define PD_GB300_ABI_VERSION 3
 
 typedef enum pd_status {
     PD_OK = 0,
@@ -129,10 +129,12 @@ typedef struct pd_solver_options {
     int lanes_per_particle;        /* 4, 8, 16 or 32 lanes cooperate on one bond row of the SpMV */
     int cg_check_interval;         /* CG iterations launched between convergence read-backs */
     int spmv_unroll;               /* 1, 2 or 4 bonds loaded per lane before computing */
-    /* CG initial guess (no reference counterpart for 1): 0 = the previous
-     * solution, as the reference (simulator.cu:745-770); 1 = previous solution
-     * plus the learned correction of pd_ws_set_params' network (mixed
-     * precision only; the CG still runs to the same tolerance) */
+    /* CG initial guess (no reference counterpart for 1 and 2): 0 = the
+     * previous solution, as the reference (simulator.cu:745-770); 1 = previous
+     * solution plus the learned correction of pd_ws_set_params' network (mixed
+     * precision only); 2 = previous solution plus its Galerkin correction in
+     * the span of the last history_size solutions (history projection, either
+     * precision).  The CG still runs to the same tolerance. */
     int warm_start;
     /* mixed-precision SpMV path: 0 or 2 = per-bond gathers from global
      * memory; 1 = shared-memory tiles of 256 consecutive rows and their halos
@@ -151,6 +153,8 @@ typedef struct pd_solver_options {
     double contact_distance;
     double contact_stiffness;
     double contact_volume;
+    /* warm_start = 2: solutions kept for the projection, 1..8; 0 = 8 */
+    int history_size;
 } pd_solver_options;
 
 /* Export selectors for pd_get. */
@@ -187,8 +191,9 @@ typedef struct pd_step_stats {
     int max_bonds_per_particle;    /* pd_max_num_bonds */
     double clock_scale;
     double sim_time;               /* simulated seconds */
-    long long ws_guesses_kept;     /* steps whose learned guess beat the previous solution */
-    double last_ws_residual_ratio; /* ||r(learned guess)|| / ||r(previous solution)|| of the last step */
+    long long ws_guesses_kept;     /* steps whose learned guess beat the previous solution, or
+                                      (warm_start 2) whose history projection was applied */
+    double last_ws_residual_ratio; /* ||r(guess)|| / ||r(previous solution)|| of the last step */
 } pd_step_stats;
 
 /* Device time per kernel class, accumulated with CUDA events on the handle's
@@ -197,7 +202,9 @@ typedef struct pd_step_stats {
  * 8th iteration and total_ms is their mean duration times the exact count of
  * live launches. */
 typedef enum pd_kernel_class {
-    PD_KC_FORCE = 0, PD_KC_SPMV = 1, PD_KC_CG_VECTOR = 2, PD_KC_UPDATE = 3, PD_KC_COUNT = 4
+    PD_KC_FORCE = 0, PD_KC_SPMV = 1, PD_KC_CG_VECTOR = 2, PD_KC_UPDATE = 3,
+    PD_KC_GUESS = 4,               /* initial-guess work of warm_start 2 (its products, Gram passes, update) */
+    PD_KC_COUNT = 5
 } pd_kernel_class;
 
 typedef struct pd_kernel_times {

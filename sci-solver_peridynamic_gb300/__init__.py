@@ -41,7 +41,7 @@ PRECISION_MIXED, PRECISION_FP64 = 0, 1
  VAR_ORIGINAL_POSITION, VAR_SLOT_PERMUTATION, VAR_BROKEN_MASK) = range(15)
 # pd_kernel_class
 KC_FORCE, KC_SPMV, KC_CG_VECTOR, KC_UPDATE = range(4)
-KC_NAMES = ("force", "spmv", "cg_vector", "update")
+KC_NAMES = ("force", "spmv", "cg_vector", "update", "guess")
 
 
 class PdError(RuntimeError):
@@ -94,6 +94,7 @@ class SolverOptions(C.Structure):
         ("lanes_per_particle", C.c_int), ("cg_check_interval", C.c_int), ("spmv_unroll", C.c_int),
         ("warm_start", C.c_int), ("spmv_path", C.c_int), ("contact_enabled", C.c_int),
         ("contact_distance", C.c_double), ("contact_stiffness", C.c_double), ("contact_volume", C.c_double),
+        ("history_size", C.c_int),
     ]
 
 
@@ -124,7 +125,7 @@ class OperatorView(C.Structure):
 
 
 class KernelTimes(C.Structure):
-    _fields_ = [("launches", C.c_longlong * 4), ("total_ms", C.c_double * 4)]
+    _fields_ = [("launches", C.c_longlong * 5), ("total_ms", C.c_double * 5)]
 
 
 _lib = None
@@ -480,7 +481,7 @@ class Simulator:
     def kernel_times(self):
         t = KernelTimes()
         _check(self.lib.pd_get_kernel_times(self.h, C.byref(t)), self.h)
-        return {KC_NAMES[k]: (t.launches[k], t.total_ms[k]) for k in range(4)}
+        return {KC_NAMES[k]: (t.launches[k], t.total_ms[k]) for k in range(len(KC_NAMES))}
 
     def reset_kernel_times(self):
         _check(self.lib.pd_reset_kernel_times(self.h), self.h)

@@ -69,6 +69,10 @@ pd_status pd_create(const pd_sim_params* sim, const pd_run_params* run, const pd
         g_create_error = "time step must be positive";
         return PD_ERR_INVALID_ARGUMENT;
     }
+    if (o.warm_start < 0 || o.warm_start > 2 || o.history_size < 0 || o.history_size > pdgb::kHistMax) {
+        g_create_error = "warm_start 0..2, history_size 0..8";
+        return PD_ERR_INVALID_ARGUMENT;
+    }
     if (o.contact_enabled && !(o.contact_distance > 0 && o.contact_volume > 0)) {
         g_create_error = "contact distance and volume must be positive";
         return PD_ERR_INVALID_ARGUMENT;

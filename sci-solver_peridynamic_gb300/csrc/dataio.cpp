@@ -438,6 +438,7 @@ pd_status Engine::dataio_load_state(size_t timestep)
     last_res_ = last_res;
     last_tol_ = last_tol;
     predicted_iters_ = 0;
+    hist_reset();   // the projection history belongs to the state that was replaced
     retries_ = 0;
     // derived device data: FP32 positions, tile local indices
     const StepParams P = step_params();

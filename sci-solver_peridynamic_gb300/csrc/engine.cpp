@@ -132,6 +132,7 @@ pd_status Engine::set_stretch(const double* s0, int n)
 void Engine::free_all()
 {
     ws_free();
+    hist_free();
     void* ptrs[] = {S_.act, S_.x64, S_.v64, S_.X64, S_.x64_bk, S_.v64_bk, S_.st, S_.ost, S_.nst, S_.row_ptr,
                     S_.cnt, S_.cnt_bk, S_.col, S_.X32, S_.u32, S_.xs4, S_.inv_d0, S_.jac, S_.jdiag, S_.force, S_.rhs, S_.sol,
                     S_.r, S_.p, S_.y, S_.sc, S_.partials, S_.counters, S_.flags, S_.lidx, S_.d0sq, S_.lim, d_perm_,
@@ -329,6 +330,10 @@ pd_status Engine::make_ready()
     }
     s = tune_spmv();
     if (s != PD_OK) return s;
+    if (opt_.warm_start == 2) {
+        s = hist_prepare();
+        if (s != PD_OK) return s;
+    }
     // step state
     step_ = 0;
     substep_ = 0;
@@ -830,6 +835,10 @@ pd_status Engine::solve(const StepParams& P)
     launch_spmv(fp64_, false, P, S_, L_, stream_);
     launch_cg_residual(fp64_, P, S_, L_, stream_);
     launches_ += 3;
+    if (opt_.warm_start == 2) {
+        pd_status s = hist_project(P);
+        if (s != PD_OK) return s;
+    }
     if (ws_features_needed()) {
         pd_status s = ws_before_cg(P);
         if (s != PD_OK) return s;
@@ -869,12 +878,121 @@ pd_status Engine::solve(const StepParams& P)
     total_iters_ += last_iters_;
     predicted_iters_ = std::max(1, last_iters_);
     flush_marks(last_iters_);
+    if (opt_.warm_start == 2) {
+        if (hist_pending_ratio_) {   // the projected residual's scalars arrived with the loop's syncs
+            last_ws_ratio_ = hist_rz1_ > 0.0 ? std::sqrt(h_sc_hist_->rz / hist_rz1_) : 0.0;
+            hist_pending_ratio_ = false;
+        }
+        pd_status s = hist_push();
+        if (s != PD_OK) return s;
+    }
     if (profiling_) {
         kc_launches_[PD_KC_SPMV] += last_iters_;
         kc_launches_[PD_KC_CG_VECTOR] += 2LL * last_iters_;
     }
     if (!h_sc_->converged) cg_converged_ = false;
     if (ws_features_needed()) return ws_after_cg(P);
+    return PD_OK;
+}
+
+// ---- history projection (warm_start = 2) ---------------------------------------------
+// The guess x1 + H y of history.cu: H holds the last hist_cap_ accepted
+// solutions, y is the Galerkin solution over the well-conditioned part of
+// span H.  Per solve: m products A h_j, two Gram passes, one host sync for the
+// m x m solve, x += H y and a fresh residual.
+pd_status Engine::hist_prepare()
+{
+    hist_free();
+    hist_cap_ = opt_.history_size > 0 ? std::min(opt_.history_size, kHistMax) : kHistMax;
+    const size_t vec = (size_t)std::max(n_, 1) * (fp64_ ? sizeof(dbl4) : sizeof(float4));
+    hist_blocks_ = (int)std::max<long long>(1, std::min<long long>(((long long)n_ + kBlock - 1) / kBlock,
+                                                                  2LL * sm_count_));
+    CK(cudaMalloc(&d_hist_, vec * hist_cap_), "alloc history");
+    CK(cudaMalloc(&d_ahist_, vec * hist_cap_), "alloc history products");
+    CK(cudaMalloc((void**)&d_hpart_, sizeof(double) * (size_t)hist_blocks_ * hist_dots_count(0)),
+       "alloc history partials");
+    CK(cudaMalloc((void**)&d_hdots_, sizeof(double) * 128), "alloc history dots");
+    CK(cudaMallocHost((void**)&h_hdots_, sizeof(double) * 128), "alloc history dots (host)");
+    CK(cudaMallocHost((void**)&h_sc_hist_, sizeof(CgScalars)), "alloc history scalars (host)");
+    hist_reset();
+    return PD_OK;
+}
+
+void Engine::hist_free()
+{
+    if (d_hist_) cudaFree(d_hist_);
+    if (d_ahist_) cudaFree(d_ahist_);
+    if (d_hpart_) cudaFree(d_hpart_);
+    if (d_hdots_) cudaFree(d_hdots_);
+    if (h_hdots_) cudaFreeHost(h_hdots_);
+    if (h_sc_hist_) cudaFreeHost(h_sc_hist_);
+    d_hist_ = d_ahist_ = nullptr;
+    d_hpart_ = d_hdots_ = h_hdots_ = nullptr;
+    h_sc_hist_ = nullptr;
+    hist_cap_ = 0;
+    hist_reset();
+}
+
+void* Engine::hist_vec(int j) const
+{
+    const size_t vec = (size_t)std::max(n_, 1) * (fp64_ ? sizeof(dbl4) : sizeof(float4));
+    return (char*)d_hist_ + vec * (size_t)j;
+}
+
+pd_status Engine::hist_project(const StepParams& P)
+{
+    const int m = hist_m_;
+    if (m == 0 || n_ == 0 || !d_hist_) return PD_OK;
+    const size_t vec = (size_t)n_ * (fp64_ ? sizeof(dbl4) : sizeof(float4));
+    HistPtrs H{}, W{};
+    for (int j = 0; j < m; ++j) {
+        H.v[j] = hist_vec(j);
+        W.v[j] = (const char*)d_ahist_ + vec * (size_t)j;
+    }
+    mark_begin(PD_KC_GUESS, -1);
+    // products with this step's operator (counter 4 of the reduction scratch is unused without a dot)
+    const ReduceSlot slot{S_.partials, S_.counters + 4};
+    for (int j = 0; j < m; ++j)
+        launch_operator_u(fp64_, P, S_, L_.lanes, L_.unroll, L_.grid_bonds, H.v[j], (void*)W.v[j], slot, nullptr,
+                          stream_);
+    const int na = hist_dots_count(0);
+    launch_hist_dots(fp64_, 0, n_, m, H, W, S_.r, d_hpart_, hist_blocks_, d_hdots_, stream_);
+    launch_hist_dots(fp64_, 1, n_, m, H, W, nullptr, d_hpart_, hist_blocks_, d_hdots_ + na, stream_);
+    launches_ += m + 4;
+    CK(cudaGetLastError(), "history products");
+    CK(cudaMemcpyAsync(h_hdots_, d_hdots_, sizeof(double) * (na + hist_dots_count(1)), cudaMemcpyDeviceToHost,
+                       stream_), "read history dots");
+    CK(cudaMemcpyAsync(h_sc_, S_.sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, stream_), "read cg scalars");
+    CK(cudaStreamSynchronize(stream_), "history sync");
+    HistCoef Y{};
+    // columns whose part outside the others' span is below sqrt(rel) of the
+    // largest norm are rounding noise of the stored precision
+    const double rel = fp64_ ? 1e-26 : 1e-14;
+    const int used = hist_solve(m, h_hdots_, h_hdots_ + na, h_hdots_ + hist_dots_count(1), rel, Y.y);
+    if (used > 0 && !h_sc_->done) {
+        hist_rz1_ = h_sc_->rz;
+        launch_hist_apply(fp64_, n_, m, H, Y, S_.sol, L_.grid_vec, stream_);
+        launch_spmv(fp64_, false, P, S_, L_, stream_);
+        launch_cg_residual(fp64_, P, S_, L_, stream_);
+        launches_ += 3;
+        CK(cudaMemcpyAsync(h_sc_hist_, S_.sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, stream_),
+           "read projected residual");
+        hist_pending_ratio_ = true;
+        ++ws_kept_;
+    }
+    mark_end();
+    CK(cudaGetLastError(), "history guess");
+    return PD_OK;
+}
+
+pd_status Engine::hist_push()
+{
+    if (!d_hist_ || hist_cap_ == 0 || n_ == 0) return PD_OK;
+    launch_hist_push(fp64_, n_, S_.act, S_.sol, hist_vec(hist_next_), L_.grid_vec, stream_);
+    ++launches_;
+    hist_next_ = (hist_next_ + 1) % hist_cap_;
+    hist_m_ = std::min(hist_m_ + 1, hist_cap_);
+    CK(cudaGetLastError(), "history push");
     return PD_OK;
 }
 

@@ -72,6 +72,14 @@ private:
     bool ws_features_needed() const;
     pd_status ws_before_cg(const StepParams& P);
     pd_status ws_after_cg(const StepParams& P);
+    // history projection (warm_start = 2): buffers, the guess, the push of an
+    // accepted solution, and forgetting the history (new state)
+    pd_status hist_prepare();
+    void hist_free();
+    pd_status hist_project(const StepParams& P);
+    pd_status hist_push();
+    void hist_reset() { hist_m_ = 0, hist_next_ = 0; }
+    void* hist_vec(int j) const;
     pd_status integrate(bool* advanced);
     pd_status solve(const StepParams& P);
     template <typename T>
@@ -133,6 +141,16 @@ private:
     unsigned long long ws_rng_ = 88172645463325252ull;
     double last_ws_ratio_ = 0.0;
     long long ws_kept_ = 0;
+    // history projection
+    int hist_cap_ = 0, hist_m_ = 0, hist_next_ = 0, hist_blocks_ = 0;
+    void* d_hist_ = nullptr;      // hist_cap_ vectors of n entries: accepted solutions, Dirichlet rows 0
+    void* d_ahist_ = nullptr;     // their products with this step's operator
+    double* d_hpart_ = nullptr;   // per-block partial sums of a Gram pass
+    double* d_hdots_ = nullptr;   // S (36), c (8), G (36)
+    double* h_hdots_ = nullptr;   // pinned copy
+    CgScalars* h_sc_hist_ = nullptr;   // pinned: scalars after the projected residual
+    bool hist_pending_ratio_ = false;
+    double hist_rz1_ = 0.0;
     // step state (Simulator members)
     int step_ = 0;
     int substep_ = 0;
@@ -151,10 +169,10 @@ private:
     std::vector<cudaEvent_t> event_pool_;
     std::vector<Mark> marks_;
     int open_mark_ = -1;
-    long long kc_launches_[PD_KC_COUNT] = {0, 0, 0, 0};
-    double kc_ms_[PD_KC_COUNT] = {0, 0, 0, 0};
-    long long kc_samples_[PD_KC_COUNT] = {0, 0, 0, 0};   // sampled CG iterations
-    double kc_sample_ms_[PD_KC_COUNT] = {0, 0, 0, 0};
+    long long kc_launches_[PD_KC_COUNT] = {};
+    double kc_ms_[PD_KC_COUNT] = {};
+    long long kc_samples_[PD_KC_COUNT] = {};   // sampled CG iterations
+    double kc_sample_ms_[PD_KC_COUNT] = {};
     long long launches_ = 0;
     ContactBuffers contact_{};         // PD-PD contact hash (when enabled)
     size_t saved_frame_ = 0;           // DataIO::savedFrame

@@ -193,6 +193,21 @@ cudaError_t launch_contact(bool fp64, const DeviceState& S, int n, const Contact
                            cudaStream_t st);
 // Max resident blocks per SM of the SpMV / force kernels (for grid sizing).
 int row_kernel_blocks_per_sm(bool fp64, int lanes, int unroll);
+
+// ---- history-projection initial guess (history.cu) --------------------------------
+constexpr int kHistMax = 8;                 // history vectors kept at most
+struct HistPtrs { const void* v[kHistMax]; };
+struct HistCoef { double y[kHistMax]; };
+// entries of a Gram pass: 0 -> S = H^T H (upper) then c = H^T r; 1 -> G = H^T W (upper)
+int hist_dots_count(int pass);
+void launch_hist_dots(bool fp64, int pass, int n, int m, const HistPtrs& H, const HistPtrs& W, const void* r,
+                      double* partials, int blocks, double* out, cudaStream_t st);
+void launch_hist_apply(bool fp64, int n, int m, const HistPtrs& H, const HistCoef& Y, void* x, int blocks,
+                       cudaStream_t st);
+void launch_hist_push(bool fp64, int n, const uint8_t* act, const void* x, void* dst, int blocks, cudaStream_t st);
+// host: coefficients y of x1 + H y (Galerkin over the well-conditioned part of
+// span H); returns the number of history columns used, 0 for no guess
+int hist_solve(int m, const double* S_up, const double* G_up, const double* c, double rel_tol, double* y);
 int force_kernel_blocks_per_sm(bool fp64, int lanes);
 void launch_operator_u(bool fp64, const StepParams& P, const DeviceState& S, int lanes, int unroll, int grid,
                        const void* in, void* out, ReduceSlot slot, double* dot_out, cudaStream_t st);
