@@ -434,7 +434,15 @@ __global__ void __launch_bounds__(kBlock, FP64 ? 1 : 3) k_batch_pre(BatchArgs A)
     if (!grid_barrier(A.sync)) return;
 
     for (int round = 0; round < A.max_rounds; ++round) {
-        // force pass of the scenes still pending
+        // force pass of the scenes still pending (mixed precision: their
+        // supercell words first, which the rows read for their neighbours)
+        if (!FP64) {
+            for_each_item(A, kSelForce, L, [&](int, const WorkItem& it) {
+                const SceneDesc& d = A.scenes[it.scene];
+                for (int r = it.lo + threadIdx.x; r < it.hi; r += blockDim.x) supercell_elem(d.P, d.S, r);
+            });
+            if (!grid_barrier(A.sync)) return;
+        }
         for_each_item(A, kSelForce, L, [&](int, const WorkItem& it) {
             force_item<kForceLanes, FP64>(A.scenes[it.scene], it);
         });

@@ -316,7 +316,7 @@ pd_status Engine::dataio_save_state(size_t timestep)
     };
     if (!fp64_) {
         arrs.push_back({S_.inv_d0, sizeof(float) * slots});
-        arrs.push_back({S_.d0sq, sizeof(double) * slots});
+        arrs.push_back({S_.d0sq, sizeof(float2) * slots});
     }
     std::vector<char> buf;
     for (const Arr& a : arrs) {
@@ -400,7 +400,7 @@ pd_status Engine::dataio_load_state(size_t timestep)
     };
     if (!fp64_) {
         arrs.push_back({S_.inv_d0, sizeof(float) * nslots});
-        arrs.push_back({S_.d0sq, sizeof(double) * nslots});
+        arrs.push_back({S_.d0sq, sizeof(float2) * nslots});
     }
     CK(cudaSetDevice(device_), "cudaSetDevice");
     CK(cudaStreamSynchronize(stream_), "state sync");

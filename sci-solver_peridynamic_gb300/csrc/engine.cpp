@@ -135,7 +135,7 @@ void Engine::free_all()
     hist_free();
     void* ptrs[] = {S_.act, S_.x64, S_.v64, S_.X64, S_.x64_bk, S_.v64_bk, S_.st, S_.ost, S_.nst, S_.row_ptr,
                     S_.cnt, S_.cnt_bk, S_.col, S_.X32, S_.u32, S_.xs4, S_.inv_d0, S_.jac, S_.jdiag, S_.force, S_.rhs, S_.sol,
-                    S_.r, S_.p, S_.y, S_.sc, S_.partials, S_.counters, S_.flags, S_.lidx, S_.d0sq, S_.lim, d_perm_,
+                    S_.r, S_.p, S_.y, S_.sc, S_.partials, S_.counters, S_.flags, S_.lidx, S_.d0sq, S_.lim, S_.xlo4, d_perm_,
                     d_stage_};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -173,6 +173,7 @@ pd_status Engine::allocate()
     CK(dalloc(&S_.X32, n), "alloc X32");
     CK(dalloc(&S_.u32, n), "alloc u32");
     if (!fp64_) CK(dalloc(&S_.xs4, n), "alloc xs4");
+    if (!fp64_) CK(dalloc(&S_.xlo4, n), "alloc xlo4");
     void** vecs[] = {&S_.force, &S_.rhs, &S_.sol, &S_.r, &S_.p, &S_.y};
     for (void** v : vecs) {
         CK(cudaMalloc(v, r4 * (n ? n : 1)), "alloc vector");
@@ -272,7 +273,7 @@ pd_status Engine::make_ready()
         CK(dalloc(&S_.inv_d0, slots), "alloc inv_d0");
         CK(cudaMemsetAsync(S_.inv_d0, 0, sizeof(float) * slots, stream_), "memset inv_d0");
         CK(dalloc(&S_.d0sq, slots), "alloc d0sq");
-        CK(cudaMemsetAsync(S_.d0sq, 0, sizeof(double) * slots, stream_), "memset d0sq");
+        CK(cudaMemsetAsync(S_.d0sq, 0, sizeof(float2) * slots, stream_), "memset d0sq");
         if (n > 0) {
             const int g = (int)std::min<long long>(std::max<long long>(((long long)n + kBlock - 1) / kBlock, 1), kMaxPartials);
             launch_bond_geometry(S_, g, stream_);
@@ -783,7 +784,7 @@ pd_status Engine::integrate(bool* advanced)
     mark_begin(PD_KC_FORCE, -1);
     launch_force(fp64_, Pf, S_, L_, stream_);
     mark_end();
-    ++launches_;
+    launches_ += fp64_ ? 1 : 2;   // mixed: the supercell words, then the pass
     const bool adaptive = run_.integrator == PD_NEWMARK_BETA || run_.adaptive_integration != 0;
     if (adaptive) {
         CK(cudaMemcpyAsync(h_flags_, S_.flags, sizeof(int) * 2, cudaMemcpyDeviceToHost, stream_), "read flag");

@@ -95,7 +95,7 @@ struct DeviceState {
     double* st;        // pd_stretch
     double* ost;       // pd_original_stretch
     double* nst;       // pd_new_stretch
-    double2* lim;      // mixed: limits of the squared break test per particle (limit_pair of st)
+    float4* lim;       // mixed: limits of the squared break test per particle (limit_pair of st), double-float
     int* row_ptr;      // CSR row starts (32-byte aligned rows), n+1
     int* cnt;          // live bonds per particle (pd_bond_list_top + 1)
     int* cnt_bk;
@@ -103,8 +103,10 @@ struct DeviceState {
     float4* X32;       // original positions relative to origin (mixed)
     float4* u32;       // displacement x - X (mixed)
     float4* xs4;       // mixed: position as FP32 offset in its supercell, w = packed supercell coords
+    float4* xlo4;      // mixed: the offset's low-order FP32 word (double-float with xs4)
     float* inv_d0;     // mixed: 1 / |X_q - X_p| per bond slot (from FP64)
-    double* d0sq;      // mixed: |X_p - X_q|^2 per bond slot, formed as the reference's stretch test forms it
+    float2* d0sq;      // mixed: |X_p - X_q|^2 per bond slot, formed as the reference's stretch test forms it,
+                       // as a double-float pair
     // mixed mode, tiles of tile_rows consecutive rows for the shared-memory
     // SpMV: halo[halo_ptr[t] .. halo_ptr[t+1]) = sorted distinct neighbour
     // slots of tile t's rows; lidx[slot] = the bond's neighbour as an index

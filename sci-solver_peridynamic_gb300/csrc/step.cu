@@ -22,6 +22,14 @@
 namespace pdgb {
 
 // ---- force / breakage ----------------------------------------------------------
+// mixed precision: every particle's supercell words from x64, read by the
+// force pass for the particle's own row and as a neighbour
+__global__ void __launch_bounds__(kBlock) k_supercell_words(StepParams P, DeviceState S)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x)
+        supercell_elem(P, S, i);
+}
+
 template <int G, bool FP64>
 __global__ void __launch_bounds__(kBlock) k_force(StepParams P, DeviceState S)
 {
@@ -157,7 +165,8 @@ __global__ void __launch_bounds__(kBlock) k_bond_geometry(int n, DeviceState S)
             const double dx = dsub(Xp.x, Xq.x), dy = dsub(Xp.y, Xq.y), dz = dsub(Xp.z, Xq.z);
             const double d0s = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
             S.inv_d0[rs + j] = (float)(1.0 / sqrt(d0s));
-            S.d0sq[rs + j] = d0s;
+            const F2 w = f2_of(d0s);
+            S.d0sq[rs + j] = make_float2(w.h, w.l);
         }
     }
 }
@@ -236,6 +245,7 @@ static void force_g(bool fp64, const StepParams& P, const DeviceState& S, int gr
 
 void launch_force(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st)
 {
+    if (!fp64 && P.n > 0) k_supercell_words<<<L.grid_vec, kBlock, 0, st>>>(P, S);
     switch (L.force_lanes) {
     case 4: force_g<4>(fp64, P, S, L.grid_force, st); break;
     case 16: force_g<16>(fp64, P, S, L.grid_force, st); break;

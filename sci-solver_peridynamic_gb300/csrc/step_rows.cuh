@@ -60,11 +60,81 @@ __device__ __forceinline__ float4 encode_supercell(const StepParams& P, const db
     return make_float4(o[0], o[1], o[2], __int_as_float(c[0] | (c[1] << 10) | (c[2] << 20)));
 }
 
+// The same offset split into two FP32 words, x = sup_lo + sup * ijk + hi + lo:
+// x - sup_lo is formed error-free (two-difference in FP64), the offset inside
+// the supercell is then exact in FP64, hi is it rounded to FP32 (the
+// encode_supercell word, so the SpMV sees the same positions) and lo the rest
+// rounded to FP32.  The representation error is below 2^-48 sup, so a bond
+// vector built from (hi, lo) words carries ~1e-14 relative error -- double-float
+// accuracy without FP64 arithmetic per bond.
+__device__ __forceinline__ void encode_supercell_df(const StepParams& P, const dbl4& x, float4& hi, float4& lo)
+{
+    const double xv[3] = {x.x, x.y, x.z};
+    int c[3];
+    float o[3], l[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double v = dsub(xv[k], P.sup_lo[k]);
+        const double bb = dsub(v, xv[k]);
+        const double ve = dadd(dsub(xv[k], dsub(v, bb)), dsub(-P.sup_lo[k], bb));   // v + ve == x - sup_lo
+        int ck = (int)floor(v * P.inv_sup);
+        ck = ck < 0 ? 0 : (ck > 1023 ? 1023 : ck);
+        c[k] = ck;
+        const double off = dsub(v, dmul(P.sup, (double)ck));   // exact
+        o[k] = (float)off;
+        l[k] = (float)dadd(dsub(off, (double)o[k]), ve);
+    }
+    hi = make_float4(o[0], o[1], o[2], __int_as_float(c[0] | (c[1] << 10) | (c[2] << 20)));
+    lo = make_float4(l[0], l[1], l[2], 0.f);
+}
+
 __device__ __forceinline__ void supercell_delta(int wq, int wp, float sup, float& dx, float& dy, float& dz)
 {
     dx = sup * (float)((wq & 1023) - (wp & 1023));
     dy = sup * (float)(((wq >> 10) & 1023) - ((wp >> 10) & 1023));
     dz = sup * (float)(((wq >> 20) & 1023) - ((wp >> 20) & 1023));
+}
+
+// ---- double-float (unevaluated sum of two FP32 words) -------------------------------
+struct F2 {
+    float h, l;
+};
+__device__ __forceinline__ F2 two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return F2{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ F2 quick_two_sum(float a, float b)   // |a| >= |b|
+{
+    const float s = __fadd_rn(a, b);
+    return F2{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b)
+{
+    const F2 s = two_sum(a.h, b.h);
+    return quick_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ F2 f2_mul(F2 a, F2 b)
+{
+    const float p = __fmul_rn(a.h, b.h);
+    const float e = __fmaf_rn(a.h, b.h, -p);
+    return quick_two_sum(p, __fadd_rn(e, __fadd_rn(__fmul_rn(a.h, b.l), __fmul_rn(a.l, b.h))));
+}
+__device__ __forceinline__ F2 f2_sqr(F2 a)
+{
+    const float p = __fmul_rn(a.h, a.h);
+    const float e = __fmaf_rn(a.h, a.h, -p);
+    return quick_two_sum(p, __fadd_rn(e, __fmul_rn(2.f * a.h, a.l)));
+}
+__device__ __forceinline__ F2 f2_of(double d)   // FP64 to double-float: per particle, or per bond at set-up
+{
+    const float h = (float)d;
+    return F2{h, (float)(d - (double)h)};
+}
+__device__ __forceinline__ float f2_sign_diff(F2 a, F2 b)   // the sign of a - b
+{
+    return __fadd_rn(__fsub_rn(a.h, b.h), __fsub_rn(a.l, b.l));
 }
 
 // fmaxf(stretch_p, stretch_q) of cg_solver.cuh:264: both limits rounded to float.
@@ -78,51 +148,73 @@ __device__ __forceinline__ double break_threshold(float thp, double stq)
 // Mixed precision: the reference's stretch test s = sqrt(dij2)/sqrt(d0_2) - 1 >
 // threshold costs two FP64 square roots and a division per bond, and GB300
 // runs FP64 at ~1/64 of its FP32 rate.  The test is decided instead on the
-// squares, dij2 > (1 + threshold)^2 d0_2, with dij2 and d0_2 formed in FP64
-// exactly as the reference forms them; only when the two sides are within
-// 1e-12 relative (a thousand times the rounding difference of the two forms)
-// is the reference expression itself evaluated.  Broken-bond sets stay
-// bit-exact.
+// squares, dij2 > (1 + threshold)^2 d0_2, evaluated in double-float from the
+// (hi, lo) position words (relative error ~1e-13); only when the two sides are
+// within 1e-12 relative (far above that error and the rounding difference of
+// the two forms) is the reference FP64 expression itself evaluated.
+// Broken-bond sets stay bit-exact, and no FP64 arithmetic runs per bond.
 struct MixedBond {
-    double ex, ey, ez;   // x_q - x_p
-    double dd;           // dij^2
-    double num;          // dij^2 - d0^2
+    float ex, ey, ez;    // x_q - x_p
+    float dd;            // dij^2
+    float num;           // dij^2 - d0^2, from the double-float difference (no cancellation)
     bool live;
 };
 
 // Limits of the squared break test of a particle with stretch limit st:
 // with t = st rounded to float and L = (1 + t)^2, {L (1 - 1e-12), L (1 + 1e-12)}
-// ({-1, -1} when 1 + t <= 0).  A bond's limit is the larger of its two
-// particles' t, and (1 + t)^2 grows with t, so the bond's pair is the
-// element-wise maximum of the particles' pairs.
-__device__ __forceinline__ double2 limit_pair(double st)
+// as double-float words {lo.h, lo.l, hi.h, hi.l} ({-1, 0, -1, 0} when
+// 1 + t <= 0).  A bond's limit is the larger of its two particles' t, and
+// (1 + t)^2 grows with t, so the bond's pair is the element-wise maximum of
+// the particles' pairs.
+__device__ __forceinline__ float4 limit_pair(double st)
 {
     const double l1 = dadd(1.0, (double)(float)st);
-    if (!(l1 > 0.0)) return make_double2(-1.0, -1.0);
+    if (!(l1 > 0.0)) return make_float4(-1.f, 0.f, -1.f, 0.f);
     const double L = dmul(l1, l1);
-    return make_double2(dmul(L, 1.0 - 1e-12), dmul(L, 1.0 + 1e-12));
+    const F2 lo = f2_of(dmul(L, 1.0 - 1e-12)), hi = f2_of(dmul(L, 1.0 + 1e-12));
+    return make_float4(lo.h, lo.l, hi.h, hi.l);
+}
+
+__device__ __forceinline__ F2 f2_max(F2 a, F2 b) { return f2_sign_diff(a, b) >= 0.f ? a : b; }
+
+// One component of the bond vector from the (hi, lo) words and the supercell
+// coordinates: (hi_q - hi_p) + sup (c_q - c_p) + (lo_q - lo_p) in double-float.
+__device__ __forceinline__ F2 bond_component(float hq, float hp, float lq, float lp, float cdelta)
+{
+    const F2 d = two_sum(hq, -hp);          // exact
+    const F2 s = two_sum(d.h, cdelta);      // exact (cdelta is a power of two times a small integer)
+    return quick_two_sum(s.h, __fadd_rn(__fadd_rn(d.l, s.l), __fsub_rn(lq, lp)));
 }
 
 // The break test s > fmaxf(st_p, st_q) (s = dij / d0 - 1 in FP64) decided on
 // squares: broken when dij^2 > (1 + t)^2 d0^2 (1 + 1e-12), live when
-// dij^2 < (1 + t)^2 d0^2 (1 - 1e-12), both far outside the rounding of either
-// form; a bond in between takes the reference expression.
-__device__ __forceinline__ MixedBond classify_mixed(const DeviceState& S, const dbl4& xp, const dbl4& Xp, float thp,
-                                                    double2 limp, int slot, int q)
+// dij^2 < (1 + t)^2 d0^2 (1 - 1e-12); a bond in between takes the reference
+// expression.
+__device__ __forceinline__ MixedBond classify_mixed(const StepParams& P, const DeviceState& S, const float4& hp,
+                                                    const float4& lp, const dbl4& xp, const dbl4& Xp, float thp,
+                                                    const float4& limp, int slot, int q)
 {
     MixedBond m;
-    const dbl4 xq = S.x64[q];
-    m.ex = dsub(xq.x, xp.x);
-    m.ey = dsub(xq.y, xp.y);
-    m.ez = dsub(xq.z, xp.z);
-    m.dd = dadd(dadd(dmul(m.ex, m.ex), dmul(m.ey, m.ey)), dmul(m.ez, m.ez));
-    const double d0s = S.d0sq[slot];
-    const double2 limq = S.lim[q];
-    const double lo = fmax(limp.x, limq.x), hi = fmax(limp.y, limq.y);
-    if (hi > 0.0 && m.dd > dmul(hi, d0s)) m.live = false;
-    else if (lo > 0.0 && m.dd < dmul(lo, d0s)) m.live = true;
-    else m.live = !(eval_bond(xp, Xp, xq, S.X64[q]).s > break_threshold(thp, S.st[q]));
-    m.num = dsub(m.dd, d0s);
+    const float4 hq = S.xs4[q], lq = S.xlo4[q];
+    float cx, cy, cz;
+    supercell_delta(__float_as_int(hq.w), __float_as_int(hp.w), (float)P.sup, cx, cy, cz);
+    const F2 ex = bond_component(hq.x, hp.x, lq.x, lp.x, cx);
+    const F2 ey = bond_component(hq.y, hp.y, lq.y, lp.y, cy);
+    const F2 ez = bond_component(hq.z, hp.z, lq.z, lp.z, cz);
+    const F2 dd = f2_add(f2_add(f2_sqr(ex), f2_sqr(ey)), f2_sqr(ez));
+    const float2 d0w = S.d0sq[slot];
+    const F2 d0s{d0w.x, d0w.y};
+    const float4 limq = S.lim[q];
+    const F2 lo = f2_max(F2{limp.x, limp.y}, F2{limq.x, limq.y});
+    const F2 hi = f2_max(F2{limp.z, limp.w}, F2{limq.z, limq.w});
+    if (hi.h > 0.f && f2_sign_diff(dd, f2_mul(hi, d0s)) > 0.f) m.live = false;
+    else if (lo.h > 0.f && f2_sign_diff(dd, f2_mul(lo, d0s)) < 0.f) m.live = true;
+    else m.live = !(eval_bond(xp, Xp, S.x64[q], S.X64[q]).s > break_threshold(thp, S.st[q]));
+    m.ex = ex.h;
+    m.ey = ey.h;
+    m.ez = ez.h;
+    m.dd = dd.h;
+    m.num = f2_sign_diff(dd, d0s);
     return m;
 }
 
@@ -140,11 +232,11 @@ __device__ __forceinline__ void force_row(const StepParams& P, const DeviceState
     const int a = S.act[p] & kActMask;
     const dbl4 xp = S.x64[p];
     const dbl4 Xp = S.X64[p];
-    // FP32 displacement of this step's linear system (read by k_spmv)
-    if (!FP64 && lane == 0) {
+    // FP32 displacement of this step's linear system (read by k_spmv).  The
+    // supercell words of the positions (xs4, xlo4) were written from x64 by
+    // the launch before this one (supercell_elem), as the neighbours read them.
+    if (!FP64 && lane == 0)
         S.u32[p] = make_float4((float)(xp.x - Xp.x), (float)(xp.y - Xp.y), (float)(xp.z - Xp.z), 0.f);
-        S.xs4[p] = encode_supercell(P, xp);
-    }
     if (a == ACT_INVISIBLE) return;
     const float thp = (float)S.st[p];
     const int rs = S.row_ptr[p];
@@ -202,14 +294,15 @@ __device__ __forceinline__ void force_row(const StepParams& P, const DeviceState
         // live bonds: FP32 force from the FP64 bond vector; the stretch comes
         // from dij2 - d0^2 (no cancellation) as s = (dij2 - d0^2) / (d0 (dij + d0))
         const float* id0r = S.inv_d0 + rs;
-        const double2 limp = S.lim[p];
+        const float4 limp = S.lim[p];
+        const float4 hp = S.xs4[p], lp = S.xlo4[p];
         // (double)d0 > vs_threshold  <=>  d0 > (vs_threshold rounded down to float)
         const float vs_thr = __double2float_rd(P.vs_threshold);
         float r1 = 3.0e38f, r2 = 3.0e38f;   // the lane's two smallest (dij2 - d0^2) / d0^2
         int j1 = -1;
         for (int j = lane; j < c; j += G) {
             const int q = S.col[rs + j];
-            const MixedBond m = classify_mixed(S, xp, Xp, thp, limp, rs + j, q);
+            const MixedBond m = classify_mixed(P, S, hp, lp, xp, Xp, thp, limp, rs + j, q);
             if (!m.live) {
                 ++nb;
                 continue;
@@ -254,7 +347,7 @@ __device__ __forceinline__ void force_row(const StepParams& P, const DeviceState
                 // several candidates in one lane: walk the row again
                 for (int j = lane; j < c; j += G) {
                     const int q = S.col[rs + j];
-                    const MixedBond m = classify_mixed(S, xp, Xp, thp, limp, rs + j, q);
+                    const MixedBond m = classify_mixed(P, S, hp, lp, xp, Xp, thp, limp, rs + j, q);
                     if (!m.live) continue;
                     const float idd0 = id0r[j];
                     if ((float)m.num * (idd0 * idd0) > band) continue;
@@ -290,7 +383,7 @@ __device__ __forceinline__ void force_row(const StepParams& P, const DeviceState
                         const float t = S.inv_d0[rs + bond];
                         S.inv_d0[rs + bond] = S.inv_d0[rs + top];
                         S.inv_d0[rs + top] = t;
-                        const double t2 = S.d0sq[rs + bond];
+                        const float2 t2 = S.d0sq[rs + bond];
                         S.d0sq[rs + bond] = S.d0sq[rs + top];
                         S.d0sq[rs + top] = t2;
                         if (S.lidx) {
@@ -792,13 +885,19 @@ __device__ __forceinline__ void update_elem(const StepParams& P, const DeviceSta
     S.v64[i] = make_dbl4(nv[0], nv[1], nv[2], 0.0);
 }
 
+// The supercell words of one particle's position, before a force pass
+__device__ __forceinline__ void supercell_elem(const StepParams& P, const DeviceState& S, int i)
+{
+    encode_supercell_df(P, S.x64[i], S.xs4[i], S.xlo4[i]);
+}
+
 // FP32 displacement and supercell position from the FP64 master positions
 // (after a rollback restore); the contact bit is cleared
 __device__ __forceinline__ void refresh_elem(const StepParams& P, const DeviceState& S, int i)
 {
     const dbl4 x = S.x64[i], X = S.X64[i];
     S.u32[i] = make_float4((float)(x.x - X.x), (float)(x.y - X.y), (float)(x.z - X.z), 0.f);
-    if (S.xs4) S.xs4[i] = encode_supercell(P, x);
+    if (S.xs4) encode_supercell_df(P, x, S.xs4[i], S.xlo4[i]);
     S.act[i] &= kActMask;
 }
 

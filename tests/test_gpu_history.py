@@ -80,3 +80,30 @@ def test_history_sizes(pdgb, scenes, history):
     assert same_sets(sim.alive_sets(), ora.alive_sets())
     assert rel_err(sim.get(pdgb.VAR_POSITION), ora.position) < 1e-5
     assert sim.params()[2].history_size == history
+
+
+@pytest.mark.parametrize("precision,tol", [(1, 1e-9), (0, 1e-5)])
+def test_history_guess_with_breaking_and_rollbacks(pdgb, scenes, precision, tol):
+    """The reference block under Newmark with bond breaking and adaptive
+    rollbacks (the time step halves and doubles): the projection's history
+    spans solutions of different time steps, and a rolled-back attempt pushes
+    nothing.  Bond sets and dt sequence as the oracle's."""
+    sc = scenes.reference_block(n_side=7, seed=5, integrator=pdgb.NEWMARK_BETA, adaptive=1, expansion=150.0,
+                                cg_tol=1e-12 if precision == 1 else 1e-10)
+    sc.opt.precision = precision
+    sc.opt.warm_start = 2
+    sim = scenes.make_simulator(sc)
+    sim.makeReady()
+    ora = make_oracle(sc)
+    ticks = set()
+    for step in range(1, 91):
+        sim.advance(1)
+        ora.advance(1)
+        assert sim.stats().time_step_ticks == ora.dt_ticks
+        ticks.add(ora.dt_ticks)
+        if step % 5 == 0:
+            assert same_sets(sim.alive_sets(), ora.alive_sets())
+    assert len(ticks) > 1   # the time step changed during the run
+    assert sim.stats().bonds_alive < sim.stats().bonds_initial
+    assert rel_err(sim.get(pdgb.VAR_POSITION), ora.position) < tol
+    assert sim.stats().ws_guesses_kept > 0
