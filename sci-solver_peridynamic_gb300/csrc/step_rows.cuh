@@ -88,11 +88,19 @@ __device__ __forceinline__ void encode_supercell_df(const StepParams& P, const d
     lo = make_float4(l[0], l[1], l[2], 0.f);
 }
 
+// A small integer as float without an int-to-float conversion (those issue
+// at 1/8 of the FP32 rate): the integer added to the mantissa of 1.5 * 2^23,
+// then 1.5 * 2^23 subtracted -- exact for |i| < 2^22.
+__device__ __forceinline__ float small_int_to_float(int i)
+{
+    return __fsub_rn(__int_as_float(0x4B400000 + i), 12582912.0f);
+}
+
 __device__ __forceinline__ void supercell_delta(int wq, int wp, float sup, float& dx, float& dy, float& dz)
 {
-    dx = sup * (float)((wq & 1023) - (wp & 1023));
-    dy = sup * (float)(((wq >> 10) & 1023) - ((wp >> 10) & 1023));
-    dz = sup * (float)(((wq >> 20) & 1023) - ((wp >> 20) & 1023));
+    dx = sup * small_int_to_float((wq & 1023) - (wp & 1023));
+    dy = sup * small_int_to_float(((wq >> 10) & 1023) - ((wp >> 10) & 1023));
+    dz = sup * small_int_to_float(((wq >> 20) & 1023) - ((wp >> 20) & 1023));
 }
 
 // ---- double-float (unevaluated sum of two FP32 words) -------------------------------
@@ -190,14 +198,14 @@ __device__ __forceinline__ F2 bond_component(float hq, float hp, float lq, float
 // squares: broken when dij^2 > (1 + t)^2 d0^2 (1 + 1e-12), live when
 // dij^2 < (1 + t)^2 d0^2 (1 - 1e-12); a bond in between takes the reference
 // expression.
-__device__ __forceinline__ MixedBond classify_mixed(const StepParams& P, const DeviceState& S, const float4& hp,
+__device__ __forceinline__ MixedBond classify_mixed(float sup, const DeviceState& S, const float4& hp,
                                                     const float4& lp, const dbl4& xp, const dbl4& Xp, float thp,
                                                     const float4& limp, int slot, int q)
 {
     MixedBond m;
     const float4 hq = S.xs4[q], lq = S.xlo4[q];
     float cx, cy, cz;
-    supercell_delta(__float_as_int(hq.w), __float_as_int(hp.w), (float)P.sup, cx, cy, cz);
+    supercell_delta(__float_as_int(hq.w), __float_as_int(hp.w), sup, cx, cy, cz);
     const F2 ex = bond_component(hq.x, hp.x, lq.x, lp.x, cx);
     const F2 ey = bond_component(hq.y, hp.y, lq.y, lp.y, cy);
     const F2 ez = bond_component(hq.z, hp.z, lq.z, lp.z, cz);
@@ -296,13 +304,14 @@ __device__ __forceinline__ void force_row(const StepParams& P, const DeviceState
         const float* id0r = S.inv_d0 + rs;
         const float4 limp = S.lim[p];
         const float4 hp = S.xs4[p], lp = S.xlo4[p];
+        const float supf = (float)P.sup, hor = (float)P.horizon, radf = (float)P.radius;
         // (double)d0 > vs_threshold  <=>  d0 > (vs_threshold rounded down to float)
         const float vs_thr = __double2float_rd(P.vs_threshold);
         float r1 = 3.0e38f, r2 = 3.0e38f;   // the lane's two smallest (dij2 - d0^2) / d0^2
         int j1 = -1;
         for (int j = lane; j < c; j += G) {
             const int q = S.col[rs + j];
-            const MixedBond m = classify_mixed(P, S, hp, lp, xp, Xp, thp, limp, rs + j, q);
+            const MixedBond m = classify_mixed(supf, S, hp, lp, xp, Xp, thp, limp, rs + j, q);
             if (!m.live) {
                 ++nb;
                 continue;
@@ -320,7 +329,7 @@ __device__ __forceinline__ void force_row(const StepParams& P, const DeviceState
                 r2 = r;
             }
             float vs = 1.0f;
-            if (d0 > vs_thr) vs = 0.5f + ((float)P.horizon - d0) * 0.5f / (float)P.radius;
+            if (d0 > vs_thr) vs = 0.5f + (hor - d0) * 0.5f / radf;
             const float kk = sf * vs / fmaxf(d, 1e-10f);   // eij /= fmaxf(dij, SMALL)
             fx = fmaf(kk, (float)m.ex, (float)fx);
             fy = fmaf(kk, (float)m.ey, (float)fy);
@@ -347,7 +356,7 @@ __device__ __forceinline__ void force_row(const StepParams& P, const DeviceState
                 // several candidates in one lane: walk the row again
                 for (int j = lane; j < c; j += G) {
                     const int q = S.col[rs + j];
-                    const MixedBond m = classify_mixed(P, S, hp, lp, xp, Xp, thp, limp, rs + j, q);
+                    const MixedBond m = classify_mixed(supf, S, hp, lp, xp, Xp, thp, limp, rs + j, q);
                     if (!m.live) continue;
                     const float idd0 = id0r[j];
                     if ((float)m.num * (idd0 * idd0) > band) continue;
