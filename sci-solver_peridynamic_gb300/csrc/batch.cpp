@@ -166,6 +166,10 @@ pd_status Batch::add_scene(const pd_sim_params& sim, const pd_run_params& run, c
         err_ = "PD-PD contact is not available in batches";
         return PD_ERR_INVALID_ARGUMENT;
     }
+    if (opt.warm_start == 2) {
+        err_ = "the history-projection guess (warm_start 2) is not available in batches";
+        return PD_ERR_INVALID_ARGUMENT;
+    }
     pd_run_params r = run;
     r.gpu_device = device_;
     std::unique_ptr<Engine> e(new (std::nothrow) Engine(sim, r, opt));

@@ -143,6 +143,11 @@ def test_batch_errors(pdgb, scenes):
     assert e.value.status == 1
     with pytest.raises(pdgb.PdError):
         b.get(5, pdgb.VAR_POSITION)      # scene out of range
+    sch = scenes.impact_body(100, "block", precision=0)
+    sch.opt.warm_start = 2
+    with pytest.raises(pdgb.PdError) as e:
+        scenes.add_to_batch(b, sch)      # the history projection is per handle only
+    assert e.value.status == 1
 
 
 def test_batch_learned_warm_start(pdgb, scenes):
