@@ -146,3 +146,33 @@ def test_load_state_errors(pdgb, scenes, tmp_path):
     with pytest.raises(pdgb.PdError) as e:
         fresh.dataIO_loadState(2)        # before make_ready
     assert e.value.status == 3
+
+
+def test_checkpoint_restart_with_history_guess(pdgb, scenes, tmp_path):
+    """warm_start = 2: a restored handle starts with an empty projection
+    history (the history is not part of the checkpoint), so it continues
+    within the CG tolerance of the uninterrupted run rather than bit for bit:
+    the same bond sets and time steps, positions to 1e-7 relative."""
+    def scene():
+        sc = scenes.reference_block(n_side=7, seed=5, integrator=pdgb.NEWMARK_BETA, adaptive=1, expansion=150.0,
+                                    cg_tol=1e-10)
+        sc.opt.warm_start = 2
+        return _with_output(sc, tmp_path)
+
+    ref = scenes.make_simulator(scene())
+    ref.makeReady()
+    ref.advance(50)
+    a = scenes.make_simulator(scene())
+    a.makeReady()
+    a.advance(25)
+    a.dataIO_saveState(25)
+    a.close()
+    b = scenes.make_simulator(scene())
+    b.makeReady()
+    b.dataIO_loadState(25)
+    b.advance(25)
+    assert same_sets(b.alive_sets(), ref.alive_sets())
+    assert b.stats().time_step_ticks == ref.stats().time_step_ticks
+    x, xr = b.get(pdgb.VAR_POSITION)[:, :3], ref.get(pdgb.VAR_POSITION)[:, :3]
+    assert np.abs(x - xr).max() <= 1e-7 * np.abs(xr).max()
+    assert b.stats().ws_guesses_kept > 0
