@@ -20,7 +20,7 @@ namespace pdgb {
 namespace {
 
 constexpr unsigned long long kBarrierTimeoutNs = 5000000000ull;   // 5 s
-constexpr int kForceLanes = 8;
+constexpr int kForceLanes = 4;   // as the single-scene force pass (fastest of 4 / 8 / 16 at 1M)
 
 __device__ __forceinline__ unsigned long long global_ns()
 {

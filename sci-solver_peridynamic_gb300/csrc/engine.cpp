@@ -323,7 +323,8 @@ pd_status Engine::make_ready()
     // launch geometry
     const long long need_vec = ((long long)n + kBlock - 1) / kBlock;
     L_.grid_vec = (int)std::max<long long>(1, std::min<long long>({need_vec, (long long)sm_count_ * 8, (long long)kMaxPartials}));
-    L_.force_lanes = 8;
+    // 4 lanes per row: at 1M particles 1.25 ms per force pass against 1.74 (8) and 2.9 (16)
+    L_.force_lanes = 4;
     L_.grid_force = grid_for_rows(L_.force_lanes, force_kernel_blocks_per_sm(fp64_, L_.force_lanes));
     if (!fp64_ && n > 0) {   // supercell positions of the initial state (read by the SpMV)
         launch_refresh(fp64_, step_params(), S_, L_, stream_);
