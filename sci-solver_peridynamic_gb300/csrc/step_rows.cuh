@@ -66,18 +66,22 @@ __device__ __forceinline__ float4 encode_supercell(const StepParams& P, const db
 // encode_supercell word, so the SpMV sees the same positions) and lo the rest
 // rounded to FP32.  The representation error is below 2^-48 sup, so a bond
 // vector built from (hi, lo) words carries ~1e-14 relative error -- double-float
-// accuracy without FP64 arithmetic per bond.
+// accuracy without FP64 arithmetic per bond.  A position outside the 1024^3
+// supercell window (its cell index clamped) has an offset of many supercells
+// and no such bound: lo.w = 1 marks it, and its bonds take the exact test.
 __device__ __forceinline__ void encode_supercell_df(const StepParams& P, const dbl4& x, float4& hi, float4& lo)
 {
     const double xv[3] = {x.x, x.y, x.z};
     int c[3];
     float o[3], l[3];
+    bool clamped = false;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         const double v = dsub(xv[k], P.sup_lo[k]);
         const double bb = dsub(v, xv[k]);
         const double ve = dadd(dsub(xv[k], dsub(v, bb)), dsub(-P.sup_lo[k], bb));   // v + ve == x - sup_lo
         int ck = (int)floor(v * P.inv_sup);
+        if (ck < 0 || ck > 1023) clamped = true;
         ck = ck < 0 ? 0 : (ck > 1023 ? 1023 : ck);
         c[k] = ck;
         const double off = dsub(v, dmul(P.sup, (double)ck));   // exact
@@ -85,7 +89,7 @@ __device__ __forceinline__ void encode_supercell_df(const StepParams& P, const d
         l[k] = (float)dadd(dsub(off, (double)o[k]), ve);
     }
     hi = make_float4(o[0], o[1], o[2], __int_as_float(c[0] | (c[1] << 10) | (c[2] << 20)));
-    lo = make_float4(l[0], l[1], l[2], 0.f);
+    lo = make_float4(l[0], l[1], l[2], clamped ? 1.f : 0.f);
 }
 
 // A small integer as float without an int-to-float conversion (those issue
@@ -215,8 +219,9 @@ __device__ __forceinline__ MixedBond classify_mixed(float sup, const DeviceState
     const float4 limq = S.lim[q];
     const F2 lo = f2_max(F2{limp.x, limp.y}, F2{limq.x, limq.y});
     const F2 hi = f2_max(F2{limp.z, limp.w}, F2{limq.z, limq.w});
-    if (hi.h > 0.f && f2_sign_diff(dd, f2_mul(hi, d0s)) > 0.f) m.live = false;
-    else if (lo.h > 0.f && f2_sign_diff(dd, f2_mul(lo, d0s)) < 0.f) m.live = true;
+    const bool exact_only = lp.w != 0.f || lq.w != 0.f;   // outside the supercell window
+    if (!exact_only && hi.h > 0.f && f2_sign_diff(dd, f2_mul(hi, d0s)) > 0.f) m.live = false;
+    else if (!exact_only && lo.h > 0.f && f2_sign_diff(dd, f2_mul(lo, d0s)) < 0.f) m.live = true;
     else m.live = !(eval_bond(xp, Xp, S.x64[q], S.X64[q]).s > break_threshold(thp, S.st[q]));
     m.ex = ex.h;
     m.ey = ey.h;

@@ -262,3 +262,28 @@ def test_small_block_closed_form(pdgb, scenes, precision):
         assert np.abs(F - f).max() <= 1e-6 * (n - 1) * c
         assert np.abs(y[:, :3] - y_ref).max() <= 2e-5 * np.abs(y_ref).max()
         assert abs(dot - float(np.sum(ws * y_ref))) <= 2e-5 * abs(dot)
+
+
+def test_particles_leaving_the_supercell_window(pdgb, scenes):
+    """Two bonded blocks flying apart at 200 m/s leave the 1024-supercell
+    window around the initial bounding box (supercell 2^-7 m here, so +-4 m)
+    within ~20 steps.  Their cell indices clamp, the two-word positions lose
+    their error bound, and the break test of their bonds falls back to the
+    reference's FP64 expression: bond sets stay the oracle's."""
+    # CG rel. 1e-6: the right-hand side is dominated by the uniform 200 m/s,
+    # and FP32 CG vectors cannot resolve a residual far below 1e-7 of it
+    sc = scenes.two_blocks(n_side=4, spacing=0.002, gap_spacings=3.0, speed=-200.0, dt=1e-3, cg_tol=1e-6,
+                           contact=False, steps=40)
+    sim = scenes.make_simulator(sc)
+    sim.makeReady()
+    ora = make_oracle(sc)
+    for _ in range(4):
+        sim.advance(10)
+        ora.advance(10)
+        assert sim.CGConvergence()
+        assert same_sets(sim.alive_sets(), ora.alive_sets())
+    assert sim.get_current_step() == 40
+    x, xo = sim.get(pdgb.VAR_POSITION)[:, :3], ora.position[:, :3]
+    assert np.abs(xo[:, 0]).max() > 5.0          # beyond the window
+    assert np.abs(x - xo).max() <= 1e-6 * np.abs(xo).max()
+    assert sim.CGConvergence()
