@@ -203,3 +203,30 @@ def test_mesh_fill_golden_pinned_to_reference():
             pos, vel = mg.reference_fill(L, p, bmin, bmax, radius, sf, tr, v0, arr)
             np.testing.assert_array_equal(pos, g[name + "/pos"])
             np.testing.assert_array_equal(vel, g[name + "/vel"])
+
+
+def test_struct_mirrors_match_the_c_layout(pdgb):
+    """The ctypes mirrors are as large as the C structs: the library's default
+    fillers write the whole struct, so a mirror that is too short would let
+    them write past it.  Each call gets a buffer of the mirror's size plus a
+    sentinel tail, which must come back untouched, and the last field of each
+    struct must be written (a mirror that is too long would leave it at the
+    sentinel)."""
+    import ctypes as C
+    lib = pdgb.library()
+    tail = 64
+    cases = [(pdgb.SolverOptions, lib.pd_solver_options_default, "history_size", 0)]
+    for cls, fn, last, expect in cases:
+        size = C.sizeof(cls)
+        buf = (C.c_ubyte * (size + tail))(*([0xA5] * (size + tail)))
+        assert fn(C.cast(buf, C.POINTER(cls))) == 0
+        assert bytes(buf[size:]) == bytes([0xA5] * tail), cls.__name__
+        obj = cls.from_buffer(buf)
+        assert getattr(obj, last) == expect, (cls.__name__, last)
+    # the simulation and running parameters are filled together
+    sim_cls, run_cls = pdgb.SimulationParameters, pdgb.RunningParameters
+    sbuf = (C.c_ubyte * (C.sizeof(sim_cls) + tail))(*([0xA5] * (C.sizeof(sim_cls) + tail)))
+    rbuf = (C.c_ubyte * (C.sizeof(run_cls) + tail))(*([0xA5] * (C.sizeof(run_cls) + tail)))
+    assert lib.pd_params_default(C.cast(sbuf, C.POINTER(sim_cls)), C.cast(rbuf, C.POINTER(run_cls))) == 0
+    assert bytes(sbuf[C.sizeof(sim_cls):]) == bytes([0xA5] * tail)
+    assert bytes(rbuf[C.sizeof(run_cls):]) == bytes([0xA5] * tail)
