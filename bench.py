@@ -23,9 +23,11 @@ build, and per step advance + position download), `roofline` is the SpMV
 kernel's algorithmic bytes per launch over its event-timed mean duration.
 
 --impl reference: the CPU oracle port of the reference step (the reference
-itself needs CUSP and sm_20 and does not build here) on the host cores, on a
-bounded sample: the same scene built at 1/8 of the particle count, steps/s
-scaled by the particle ratio.
+itself needs CUSP and sm_20 and does not build here) on the host cores, on
+the same full-size scene, W warm-up steps then K timed steps, no scaling.
+The scene is built by lattice.py loaded by path, so this arm never maps the
+GPU library.  The GPU arm's cpu_baseline times the first steps of the same
+full-size scene with the same oracle.
 
 Multi-GPU (torchrun): independent replicas, one per GPU ("replicas only"):
 value = total steps of all ranks / max rank time.
@@ -46,8 +48,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 PKG_NAME = "sci-solver_peridynamic_gb300"
 METRIC = "implicit steps/s at 1M particles (CG rel. residual 1e-6)"
-SAMPLE_DIV = 8          # CPU sample: same scene at 1/8 of the particles
 TARGET_N = 1_000_000
+CPU_SAMPLE_STEPS = 2    # the GPU arm's cpu_baseline: the first steps of the same full-size scene
+WORKLOAD_FMT = ("ellipsoid_impact: %d particles, semi-axes 0.5/0.35/0.3 m, spacing %.5f m, horizon 5r, "
+                "s0 0.015, rigid sphere r=0.1 m at 10 m/s (penalty contact), Newmark-beta dt=5e-5 s, CG rel 1e-6")
 
 
 def parse_args(argv=None):
@@ -195,30 +199,42 @@ def ncu_traffic(kernel: str = "k_spmv"):
     return None
 
 
-# ---- the CPU sample ------------------------------------------------------------------
-def cpu_sample_scene(pkg_scenes, n_full):
-    return pkg_scenes.ellipsoid_impact(target_n=max(1000, n_full // SAMPLE_DIV), gap=0.0)
+# ---- the CPU oracle on the same workload ---------------------------------------------------
+def lattice_module():
+    """sci-solver_peridynamic_gb300/lattice.py loaded by path: it builds the
+    scene arrays with numpy alone, so the CPU legs never import the package
+    (which would map the GPU library)."""
+    import importlib.util
+    path = os.path.join(ROOT, PKG_NAME, "lattice.py")
+    spec = importlib.util.spec_from_file_location("pd_lattice_standalone", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
 
 
-def oracle_for(scene):
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from helpers import make_oracle
-    return make_oracle(scene)
-
-
-def cpu_steps_per_s(pkg_scenes, n_full, warmup, steps):
-    """Oracle (FP64 reference restatement) on the 1/8 sample: W untimed steps,
-    then `steps` timed; steps/s scaled to the full particle count."""
+def cpu_oracle_run(n_target, warmup, steps):
+    """The oracle port of the reference step (FP64, OpenMP over particles) on
+    the full workload: the same ellipsoid scene at n_target particles, bonds
+    built, `warmup` untimed steps, then `steps` timed one by one.  Returns a
+    dict: steps_per_s, particles, spacing, timed_s, cg_iterations_per_step,
+    setup_s (scene, bonds and warm-up)."""
     from oracle import oracle as O
     O.build_oracle()
-    sc = cpu_sample_scene(pkg_scenes, n_full)
-    o = oracle_for(sc)
-    o.advance(warmup)
+    body = lattice_module().ellipsoid_impact(target_n=n_target, gap=0.0)
     t0 = time.perf_counter()
-    o.advance(steps)
+    o = O.OracleSim(O.params_from_body(body))
+    o.set_particles(body["pos"], body["vel"], body["act"])
+    o.make_ready()
+    o.advance(warmup)
+    t_setup = time.perf_counter() - t0
+    iters = 0
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.advance(1)
+        iters += o.cg_iters
     dt = time.perf_counter() - t0
-    scale = sc.n / float(n_full)
-    return steps / dt * scale, sc.n, dt
+    return {"steps_per_s": steps / dt, "particles": int(body["pos"].shape[0]), "spacing": body["spacing"],
+            "timed_s": dt, "cg_iterations_per_step": iters / max(steps, 1), "setup_s": t_setup}
 
 
 # ---- GPU arm -------------------------------------------------------------------------------
@@ -296,9 +312,7 @@ def run_gb300(args):
         "dtype": "f32 force/SpMV, f64 stretch test + master state, double-float->f64 dots",
         "data": "synthetic (seeded jittered lattice ellipsoid)",
         "config": {
-            "workload": "ellipsoid_impact: %d particles, semi-axes 0.5/0.35/0.3 m, spacing %.5f m, horizon 5r, "
-                        "s0 0.015, rigid sphere r=0.1 m at 10 m/s (penalty contact), Newmark-beta dt=5e-5 s, "
-                        "CG rel 1e-6" % (n, sc.info["spacing"]),
+            "workload": WORKLOAD_FMT % (n, sc.info["spacing"]),
             "particles": n,
             "bonds_alive": int(bonds),
             "cg_iterations_per_step": round(iters / args.steps, 2),
@@ -385,13 +399,13 @@ def run_gb300(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = os.cpu_count()
         os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-        k = min(args.steps, 3)
-        v, n_s, dt = cpu_steps_per_s(scenes, n, args.warmup, k)
+        k = min(args.steps, CPU_SAMPLE_STEPS)
+        c = cpu_oracle_run(args.n, 0, k)
         result["cpu_baseline"] = {
-            "value": round(v, 6), "unit": "steps/s", "cores": cores, "kind": "port",
-            "sample": "oracle (FP64 restatement of the reference step, OpenMP over particles) on the same scene "
-                      "built with %d particles (1/%d), steps %d..%d timed (%.1f s), steps/s scaled by %d/%d"
-                      % (n_s, SAMPLE_DIV, args.warmup + 1, args.warmup + k, dt, n_s, n),
+            "value": round(c["steps_per_s"], 6), "unit": "steps/s", "cores": cores, "kind": "port",
+            "sample": "oracle (FP64 restatement of the reference step, OpenMP over particles) on the same "
+                      "%d-particle scene, steps 1..%d timed (%.1f s, %.1f CG iterations per step); no scaling"
+                      % (c["particles"], k, c["timed_s"], c["cg_iterations_per_step"]),
         }
     sim.close()
     if rank == 0:
@@ -401,21 +415,28 @@ def run_gb300(args):
 
 
 def run_reference(args):
+    """The reference's step on the host cores: the oracle port (the reference
+    itself needs CUSP and sm_20 and its kernels cannot be built on the GPU
+    box), on the full workload, W warm-up steps then K timed steps, with all
+    host threads.  Rank 0 only; the package is never imported here."""
     world, rank, local = dist_env()
     if rank != 0:
         return
-    scenes = importlib.import_module(PKG_NAME + ".scenes")
     cores = os.cpu_count()
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-    v, n_s, dt = cpu_steps_per_s(scenes, args.n, args.warmup, args.steps)
-    sample = ("oracle port of the reference step (FP64, OpenMP over particles; the reference itself needs CUSP "
-              "and sm_20) on the same scene built with %d particles (1/%d), %d timed steps after %d warm-up "
-              "(%.1f s), steps/s scaled by %d/%d" % (n_s, SAMPLE_DIV, args.steps, args.warmup, dt, n_s, args.n))
+    c = cpu_oracle_run(args.n, args.warmup, args.steps)
+    v, n_s = c["steps_per_s"], c["particles"]
+    sample = ("oracle port of the reference step (FP64, OpenMP over particles on %d threads; the reference itself "
+              "needs CUSP and sm_20) on the full %d-particle scene: %d warm-up steps, then steps %d..%d timed "
+              "(%.1f s, %.1f CG iterations per step, CG started from the previous solution as the reference does); "
+              "set-up and warm-up %.1f s" % (cores, n_s, args.warmup, args.warmup + 1, args.warmup + args.steps,
+                                            c["timed_s"], c["cg_iterations_per_step"], c["setup_s"]))
     result = {
         "metric": METRIC, "value": round(v, 6), "unit": "steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(1e3 / v, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered lattice ellipsoid)",
-        "config": {"workload": "ellipsoid_impact at %d particles (sampled at %d)" % (args.n, n_s)},
+        "config": {"workload": WORKLOAD_FMT % (n_s, c["spacing"]), "particles": n_s,
+                   "cg_iterations_per_step": round(c["cg_iterations_per_step"], 2)},
         "impl": "reference",
         "cpu_baseline": {"value": round(v, 6), "unit": "steps/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": round(v, 6), "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

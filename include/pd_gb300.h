@@ -317,11 +317,18 @@ pd_status pd_apply_operator(pd_handle* h, const void* d_x, void* d_y, double* d_
  * The reduction scratch is a static device array of this library (one FP64
  * partial per block for at most 4096 blocks plus a counter, ~33 KB on every
  * GPU that loads the library, kept until exit); a view asking for more than
- * 4096 blocks is rejected with PD_ERR_INVALID_ARGUMENT.  The first call on a
- * device resolves the array's device address (one-time set-up), so make that
- * first call before any stream capture.  Every call shares the array: calls
- * whose launches overlap on the GPU race.  Calls no cudaMalloc or cudaFree.
- * Returns after enqueueing; errors are read with pd_last_error_message(NULL). */
+ * 4096 blocks is rejected with PD_ERR_INVALID_ARGUMENT.  pd_get_operator_view
+ * fills `blocks` with the handle's own grid, which exceeds 4096 on large
+ * scenes: set view.blocks = 0 (automatic, at most 4096 blocks; every row is
+ * still covered) before passing such a view.  The first call on a device
+ * resolves the array's device address (one-time set-up), so make that first
+ * call before any stream capture.  Call with the device that holds the
+ * view's arrays current (a view on another device is rejected), in the
+ * runtime's primary context; the resolved address is kept for the life of
+ * the process and is not refreshed after cudaDeviceReset.  Every call shares
+ * the array: calls whose launches overlap on the GPU race.  Calls no
+ * cudaMalloc or cudaFree.  Returns after enqueueing; errors are read with
+ * pd_last_error_message(NULL). */
 pd_status pd_apply_operator_noalloc(const pd_operator_view* view, const void* d_x, void* d_y, double* d_dot,
                                     void* stream);
 

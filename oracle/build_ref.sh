@@ -12,10 +12,15 @@
 #   src/core/implicit_euler.cuh:18-179 fillMatrix/fillVectorB/updatePosition (implicit Euler)
 #   src/core/newmark_beta.cuh:18-201   fillMatrix/fillVectorB/updateVelocity/updatePosition (Newmark)
 #   src/core/simulator.cu:802-822      frand, getstretch
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default: $PD_REFERENCE_ROOT; no
+# machine-specific default: without either the script exits 3)
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${PD_REFERENCE_ROOT:-}}"
+if [ -z "$REF" ]; then
+  echo "build_ref.sh: give the reference root as an argument or in PD_REFERENCE_ROOT" >&2
+  exit 3
+fi
 CORE="$REF/src/core"
 if [ ! -f "$CORE/cg_solver.cuh" ]; then
   echo "build_ref.sh: reference source not found under $REF" >&2

@@ -37,9 +37,19 @@ def build_oracle(force: bool = False) -> str:
     return ORACLE_SO
 
 
-def build_ref(reference_root: str = "/root/reference") -> str | None:
-    """Build oracle/_ref/libpdref.so when the reference tree is present."""
-    if not os.path.isdir(os.path.join(reference_root, "src", "core")):
+def reference_root() -> str | None:
+    """The reference project's root, from the PD_REFERENCE_ROOT environment
+    variable (there is no default: the tree exists only where fixtures are
+    made)."""
+    return os.environ.get("PD_REFERENCE_ROOT") or None
+
+
+def build_ref(reference_root: str | None = None) -> str | None:
+    """Build oracle/_ref/libpdref.so when the reference tree is present
+    (argument, else PD_REFERENCE_ROOT); None when it is not."""
+    if reference_root is None:
+        reference_root = globals()["reference_root"]()
+    if not reference_root or not os.path.isdir(os.path.join(reference_root, "src", "core")):
         return None
     subprocess.check_call([os.path.join(HERE, "build_ref.sh"), reference_root],
                           stdout=subprocess.DEVNULL)
@@ -118,6 +128,37 @@ def _ip(a):
 def default_params() -> PdoParams:
     p = PdoParams()
     _load().pdo_default_params(C.byref(p))
+    return p
+
+
+def params_from_body(body: dict) -> PdoParams:
+    """Oracle parameters of a lattice body (the dict of
+    sci-solver_peridynamic_gb300/lattice.py: SI constants, no box, rigid
+    sphere), on top of the reference's defaults (definitions.h).  Used where
+    the GPU library must not be loaded (bench.py's reference arm); a CPU test
+    checks it equals the parameters the package's scene maps to."""
+    p = default_params()
+    p.n = int(body["pos"].shape[0])
+    p.integrator = int(body["integrator"])
+    p.adaptive = 0
+    p.horizon = body["horizon"]
+    p.radius = body["radius"]
+    p.bond_coeff = body["stiffness"]
+    p.mass = body["mass"]
+    p.dt_base = body["dt"] / 128.0
+    p.dt_ticks = 128
+    for k in range(3):
+        p.gravity[k] = body["gravity"][k]
+        p.box_min[k], p.box_max[k] = -1e300, 1e300
+    p.cg_rel_tol = body["cg_tol"]
+    p.cg_max_iter = body["cg_max_iterations"]
+    p.s0 = float(np.float32(body["s0"]))
+    p.sphere_on = 1
+    for k in range(3):
+        p.sphere_c0[k] = body["sphere_center"][k]
+        p.sphere_v[k] = body["sphere_velocity"][k]
+    p.sphere_radius = body["sphere_radius"]
+    p.sphere_k = body["sphere_stiffness"]
     return p
 
 

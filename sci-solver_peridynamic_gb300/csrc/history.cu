@@ -207,10 +207,13 @@ int hist_solve(int m, const double* S_up, const double* G_up, const double* c, d
         used[piv] = true;
         sel[r] = piv;
         const double d = W[piv][piv];
-        double col[kHistMax];
+        // the pivot's column and row are copied first: the update zeroes row
+        // piv, and every row after it must still be downdated by the old row
+        double col[kHistMax], prow[kHistMax];
         for (int a = 0; a < m; ++a) col[a] = W[a][piv] / d;
+        for (int b = 0; b < m; ++b) prow[b] = W[piv][b];
         for (int a = 0; a < m; ++a)
-            for (int b = 0; b < m; ++b) W[a][b] -= col[a] * W[piv][b];
+            for (int b = 0; b < m; ++b) W[a][b] -= col[a] * prow[b];
     }
     if (r == 0) return 0;
     // R: upper Cholesky factor of S restricted to the selected columns

@@ -14,6 +14,11 @@
 // shares it and it keeps the last call's contents; the counter, which must
 // start at zero, is cleared on the call's stream before each launch.  Calls
 // whose launches overlap on the GPU race on the shared scratch.
+//
+// The scratch's device address is resolved once per device ordinal, in the
+// runtime's primary context, and kept: after cudaDeviceReset, or from a
+// context other than the primary one, the kept address is not valid.  The
+// view's arrays must live on the current device (checked per call).
 #include <mutex>
 #include <string>
 
@@ -98,6 +103,15 @@ extern "C" pd_status pd_apply_operator_noalloc(const pd_operator_view* v, const 
         set_handleless_error(std::string("pd_apply_operator_noalloc: scratch set-up: ") + cudaGetErrorString(e));
         cudaGetLastError();
         return PD_ERR_CUDA;
+    }
+    if (v->n > 0) {   // the view's arrays must be on the current device (the scratch is per device)
+        int dev = 0;
+        cudaPointerAttributes attr{};
+        if (cudaGetDevice(&dev) == cudaSuccess && cudaPointerGetAttributes(&attr, v->row_ptr) == cudaSuccess &&
+            attr.type == cudaMemoryTypeDevice && attr.device != dev)
+            return reject("the view's arrays are on device " + std::to_string(attr.device) + ", the current device is " +
+                          std::to_string(dev));
+        cudaGetLastError();
     }
     StepParams P{};
     P.n = v->n;

@@ -27,6 +27,8 @@ import numpy as np
 
 from . import (ACTIVE, CLAMPED, IMPLICIT_EULER, NEWMARK_BETA, PRECISION_MIXED, PRESCRIBED, RunningParameters,
                SimulationParameters, SolverOptions, SystemParameter, default_options)
+from . import lattice as _lat
+from .lattice import si_mass, si_stiffness  # noqa: F401  (re-exported)
 
 
 @dataclasses.dataclass
@@ -46,10 +48,7 @@ class Scene:
         return int(self.pos.shape[0])
 
 
-def _lattice(nx, ny, nz):
-    """Lattice indices in z-major, then y, then x order (as scene.cpp fills)."""
-    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
-    return np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)
+_lattice = _lat.lattice
 
 
 def _si_params(n, spacing, coeff, mass, s0, integrator, final_step):
@@ -70,14 +69,6 @@ def _si_params(n, spacing, coeff, mass, s0, integrator, final_step):
     run.pd_stretch_limit_s0 = s0
     run.final_step = final_step
     return sim, run
-
-
-def si_stiffness(spacing):
-    return 1e6 * (spacing / 0.02) ** 2
-
-
-def si_mass(spacing):
-    return 1e-3 * (spacing / 0.02) ** 3
 
 
 def reference_block(n_side=8, seed=7, integrator=IMPLICIT_EULER, adaptive=0, expansion=300.0, drop=-0.05,
@@ -154,40 +145,28 @@ def ellipsoid_impact(target_n=1_000_000, semi_axes=(0.5, 0.35, 0.3), seed=0, jit
     sphere (penalty contact), Newmark-beta dt = 5e-5, CG rel. tol 1e-6.
     The spacing is chosen so the particle count is ~target_n.  The sphere
     starts `gap` spacings beyond the outermost particle (gap <= 0: in
-    contact from the first step)."""
-    a, b, c = semi_axes
-    if spacing is None:
-        spacing = (4.0 / 3.0 * math.pi * a * b * c / target_n) ** (1.0 / 3.0)
-    nx, ny, nz = (int(math.floor(2 * s / spacing)) + 1 for s in semi_axes)
-    g = _lattice(nx, ny, nz)
-    p0 = g * spacing - np.array([(nx - 1) * spacing / 2, (ny - 1) * spacing / 2, (nz - 1) * spacing / 2])
-    inside = (p0[:, 0] / a) ** 2 + (p0[:, 1] / b) ** 2 + (p0[:, 2] / c) ** 2 <= 1.0
-    p0 = p0[inside]
-    n = p0.shape[0]
-    rng = np.random.default_rng(seed)
-    pos = np.zeros((n, 4))
-    pos[:, :3] = p0 + rng.uniform(-jitter, jitter, (n, 3)) * spacing
-    vel = np.zeros((n, 4))
-    act = np.full(n, ACTIVE, np.int32)
-    cstiff = si_stiffness(spacing)
-    sim, run = _si_params(n, spacing, coeff, si_mass(spacing), s0, NEWMARK_BETA, steps)
+    contact from the first step).  Arrays and constants come from
+    lattice.ellipsoid_impact."""
+    b = _lat.ellipsoid_impact(target_n=target_n, semi_axes=semi_axes, seed=seed, jitter=jitter, coeff=coeff, s0=s0,
+                              dt=dt, cg_tol=cg_tol, sphere_radius=sphere_radius, sphere_speed=sphere_speed,
+                              spacing=spacing, gap=gap)
+    spacing = b["spacing"]
+    n = b["pos"].shape[0]
+    sim, run = _si_params(n, spacing, coeff, b["mass"], s0, NEWMARK_BETA, steps)
     opt = default_options()
     opt.precision = precision
-    opt.cg_relative_tolerance = cg_tol
-    opt.cg_max_iterations = 20000
-    opt.time_step_base = dt / 128.0
-    opt.bond_stiffness = cstiff
-    opt.gravity[:] = (0.0, 0.0, -9.81)
+    opt.cg_relative_tolerance = b["cg_tol"]
+    opt.cg_max_iterations = b["cg_max_iterations"]
+    opt.time_step_base = b["dt"] / 128.0
+    opt.bond_stiffness = b["stiffness"]
+    opt.gravity[:] = b["gravity"]
     opt.box_enabled = 0
     opt.sphere_enabled = 1
-    opt.sphere_radius = sphere_radius
-    opt.sphere_center[:] = (pos[:, 0].max() + sphere_radius + gap * spacing, 0.0, 0.0)
-    opt.sphere_velocity[:] = (-sphere_speed, 0.0, 0.0)
-    # penalty stiffness of the order of one bond's (c / spacing); ten times
-    # stiffer drives the compressed bonds under the impactor into an
-    # indefinite tangent within ~10 steps, where CG (FP64 included) fails
-    opt.sphere_stiffness = cstiff / spacing
-    return Scene("ellipsoid_impact", sim, run, opt, pos, vel, act, steps,
+    opt.sphere_radius = b["sphere_radius"]
+    opt.sphere_center[:] = b["sphere_center"]
+    opt.sphere_velocity[:] = b["sphere_velocity"]
+    opt.sphere_stiffness = b["sphere_stiffness"]
+    return Scene("ellipsoid_impact", sim, run, opt, b["pos"], b["vel"], b["act"], steps,
                  {"spacing": spacing, "seed": seed, "semi_axes": semi_axes})
 
 

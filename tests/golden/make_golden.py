@@ -3,7 +3,7 @@ kernels compiled on the host (oracle/_ref/libpdref.so, built by
 oracle/build_ref.sh from the reference tree).  Run where the reference tree
 is present:
 
-    python tests/golden/make_golden.py [REFERENCE_ROOT]
+    python tests/golden/make_golden.py [REFERENCE_ROOT]   (default: $PD_REFERENCE_ROOT)
 
 Each fixture holds the resolved parameters, the seeded inputs and the
 reference outputs (bond rows, s0, positions/velocities at selected steps,
@@ -76,9 +76,9 @@ def make(name, sc, steps, snap):
 
 
 if __name__ == "__main__":
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else O.reference_root()
     if O.build_ref(ref_root) is None:
-        sys.exit("reference tree not found")
+        sys.exit("reference tree not found: pass its root or set PD_REFERENCE_ROOT")
     make("ref_block_ie", scenes.reference_block(n_side=8, seed=7), 40, [1, 10, 40])
     make("ref_block_nm", scenes.reference_block(n_side=8, seed=11, integrator=1, adaptive=1, expansion=300.0),
          60, [1, 30, 60])

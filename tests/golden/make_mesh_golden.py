@@ -7,7 +7,7 @@ point_inside_mesh, compiled on the host into oracle/_ref/libpdscene.so by
 oracle/build_ref.sh) and stores the OBJ text, the parameters and the
 resulting particles in tests/golden/mesh_fill.npz.
 
-    bash oracle/build_ref.sh && python tests/golden/make_mesh_golden.py
+    PD_REFERENCE_ROOT=<reference root> bash oracle/build_ref.sh && python tests/golden/make_mesh_golden.py
 """
 from __future__ import annotations
 

@@ -66,6 +66,32 @@ def rel_err(x, ref):
     return float(np.abs(x - ref).max() / scale)
 
 
+def rel_disp_err(x, ref, x0):
+    """max |x - ref| / max |ref - x0| over xyz: the error measured against the
+    motion since x0 (the displacement), not against the coordinates."""
+    x = np.asarray(x)[:, :3]
+    ref = np.asarray(ref)[:, :3]
+    x0 = np.asarray(x0)[:, :3]
+    scale = max(np.abs(ref - x0).max(), 1e-300)
+    return float(np.abs(x - ref).max() / scale)
+
+
+# positions: of max |x_ref|; displacements u = x - x0: of max |u_ref|
+POS_TOL = {0: 1e-5, 1: 1e-9}      # mixed, FP64
+DISP_TOL = {0: 1e-3, 1: 1e-7}
+
+
+def assert_positions(x, ref, x0, precision, label=""):
+    """Positions within POS_TOL of max |ref| and displacements from x0 within
+    DISP_TOL of the reference's largest displacement (precision 0 mixed, 1
+    FP64).  Prints both errors (pytest -s shows them)."""
+    e_x, e_u = rel_err(x, ref), rel_disp_err(x, ref, x0)
+    print(f"[parity] {label}: position {e_x:.3e}, displacement {e_u:.3e}")
+    assert e_x < POS_TOL[precision], f"{label}: position error {e_x:.3e}"
+    assert e_u < DISP_TOL[precision], f"{label}: displacement error {e_u:.3e}"
+    return e_x, e_u
+
+
 def apply_on_device(pdgb, sim, x_caller, entry=None):
     """y = A x through the C ABI; x, y in caller order.  Returns (y, <x, A x>)."""
     import torch

@@ -9,7 +9,7 @@ counter must follow the same adaptive history, positions within
 import numpy as np
 import pytest
 
-from helpers import make_oracle, rel_err, same_sets
+from helpers import assert_positions, make_oracle, rel_err, same_sets
 
 pytestmark = pytest.mark.gpu
 
@@ -63,7 +63,7 @@ def test_batch_matches_oracle(pdgb, scenes, precision, tol):
             assert st.time_step_ticks == o.dt_ticks, f"scene {k}: time step differs at step {done}"
             assert same_sets(b.alive_sets(k), o.alive_sets()), f"scene {k}: broken bonds differ at step {done}"
     for k, (sc, o) in enumerate(zip(lst, oras)):
-        assert rel_err(b.get(k, pdgb.VAR_POSITION), o.position) < tol, f"scene {k}"
+        assert_positions(b.get(k, pdgb.VAR_POSITION), o.position, sc.pos, precision, f"batch scene {k}")
         assert b.stats(k).cg_converged == 1
     # the reference-units block broke bonds and went through rollbacks
     st = b.stats(3)

@@ -10,7 +10,7 @@ import math
 import numpy as np
 import pytest
 
-from helpers import make_oracle, rel_err, same_sets
+from helpers import assert_positions, make_oracle, rel_err, same_sets
 
 pytestmark = pytest.mark.gpu
 
@@ -37,7 +37,7 @@ def test_history_guess_matches_oracle(pdgb, scenes, precision, cg_tol, tol):
         ora.advance(5)
         assert same_sets(sim.alive_sets(), ora.alive_sets())
         assert sim.stats().time_step_ticks == ora.dt_ticks
-    assert rel_err(sim.get(pdgb.VAR_POSITION), ora.position) < tol
+    assert_positions(sim.get(pdgb.VAR_POSITION), ora.position, sc.pos, precision, "history 6k impact")
     st = sim.stats()
     assert st.cg_converged
     # every step after the first has a history; the projection is skipped
@@ -78,7 +78,7 @@ def test_history_sizes(pdgb, scenes, history):
     sim.advance(steps)
     ora.advance(steps)
     assert same_sets(sim.alive_sets(), ora.alive_sets())
-    assert rel_err(sim.get(pdgb.VAR_POSITION), ora.position) < 1e-5
+    assert_positions(sim.get(pdgb.VAR_POSITION), ora.position, sc.pos, 0, f"history size {history}")
     assert sim.params()[2].history_size == history
 
 
@@ -105,5 +105,5 @@ def test_history_guess_with_breaking_and_rollbacks(pdgb, scenes, precision, tol)
             assert same_sets(sim.alive_sets(), ora.alive_sets())
     assert len(ticks) > 1   # the time step changed during the run
     assert sim.stats().bonds_alive < sim.stats().bonds_initial
-    assert rel_err(sim.get(pdgb.VAR_POSITION), ora.position) < tol
+    assert_positions(sim.get(pdgb.VAR_POSITION), ora.position, sc.pos, precision, "history breaking")
     assert sim.stats().ws_guesses_kept > 0

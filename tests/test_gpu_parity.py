@@ -8,7 +8,7 @@ velocities within the stated tolerances:
 import numpy as np
 import pytest
 
-from helpers import apply_on_device, make_oracle, rel_err, same_sets
+from helpers import apply_on_device, assert_positions, make_oracle, rel_err, same_sets
 
 pytestmark = pytest.mark.gpu
 
@@ -67,7 +67,7 @@ def test_step_fp64_implicit_euler(pdgb, scenes):
     sc = scenes.reference_block(n_side=8, integrator=pdgb.IMPLICIT_EULER)
     sc.opt.precision = pdgb.PRECISION_FP64
     sim, ora = _run_pair(pdgb, scenes, sc, 40)
-    assert rel_err(sim.get(pdgb.VAR_POSITION), ora.position) < FP64_TOL
+    assert_positions(sim.get(pdgb.VAR_POSITION), ora.position, sc.pos, 1, "fp64 implicit Euler")
     assert rel_err(sim.get(pdgb.VAR_VELOCITY), ora.velocity) < 1e-7
     assert abs(sim.stats().last_cg_iterations - ora.cg_iters) <= 1
 
@@ -78,14 +78,14 @@ def test_step_fp64_newmark_breaking(pdgb, scenes):
     sim, ora = _run_pair(pdgb, scenes, sc, 60)
     st = sim.stats()
     assert st.bonds_alive < st.bonds_initial, "scene should break bonds"
-    assert rel_err(sim.get(pdgb.VAR_POSITION), ora.position) < FP64_TOL
+    assert_positions(sim.get(pdgb.VAR_POSITION), ora.position, sc.pos, 1, "fp64 Newmark breaking")
 
 
 def test_step_mixed_newmark_breaking(pdgb, scenes):
     sc = scenes.reference_block(n_side=8, integrator=pdgb.NEWMARK_BETA, adaptive=1, expansion=300.0,
                                 cg_tol=1e-9)
     sim, ora = _run_pair(pdgb, scenes, sc, 60)
-    assert rel_err(sim.get(pdgb.VAR_POSITION), ora.position) < MIXED_TOL
+    assert_positions(sim.get(pdgb.VAR_POSITION), ora.position, sc.pos, 0, "mixed Newmark breaking")
     # the broken-bond mask export: per row, the bond-list entries it marks are
     # exactly the oracle's initial neighbours that are no longer alive
     rp, bl = sim.get(pdgb.VAR_BOND_ROW_PTR), sim.get(pdgb.VAR_BOND_LIST)
@@ -100,7 +100,7 @@ def test_cube_lattice_mixed_100_steps(pdgb, scenes):
     """The small plain-method workload: 16^3, clamped base, CG rel 1e-6."""
     sc = scenes.cube_lattice()
     sim, ora = _run_pair(pdgb, scenes, sc, 100, check_every=20)
-    assert rel_err(sim.get(pdgb.VAR_POSITION), ora.position) < MIXED_TOL
+    assert_positions(sim.get(pdgb.VAR_POSITION), ora.position, sc.pos, 0, "cube 100 steps")
     # implicit Euler damps the impact out: the block is at rest after 100 steps,
     # so velocity errors are measured against the initial speed (5 m/s)
     v, vo = sim.get(pdgb.VAR_VELOCITY), ora.velocity
@@ -128,7 +128,7 @@ def test_tiny_scenes(pdgb, scenes, n_side):
     sc = scenes.reference_block(n_side=n_side)
     sc.opt.precision = pdgb.PRECISION_FP64
     sim, ora = _run_pair(pdgb, scenes, sc, 5, check_every=5)
-    assert rel_err(sim.get(pdgb.VAR_POSITION), ora.position) < FP64_TOL
+    assert_positions(sim.get(pdgb.VAR_POSITION), ora.position, sc.pos, 1, f"tiny {n_side}")
 
 
 @pytest.mark.parametrize("precision,tol", [(1, FP64_TOL), (0, MIXED_TOL)])
@@ -140,6 +140,7 @@ def test_newmark_dt_halving_and_doubling(pdgb, scenes, precision, tol):
     sc.opt.precision = precision
     sim, ora = _run_pair(pdgb, scenes, sc, 90, check_every=5)
     assert rel_err(sim.get(pdgb.VAR_POSITION), ora.position) < tol
+    assert_positions(sim.get(pdgb.VAR_POSITION), ora.position, sc.pos, precision, "dt halving/doubling")
 
 
 @pytest.mark.parametrize("path", [1, 2])
@@ -152,7 +153,7 @@ def test_spmv_paths_mixed_breaking(pdgb, scenes, path):
     sim, ora = _run_pair(pdgb, scenes, sc, 60)
     assert sim.params()[2].spmv_path == path
     assert sim.stats().bonds_alive < sim.stats().bonds_initial
-    assert rel_err(sim.get(pdgb.VAR_POSITION), ora.position) < MIXED_TOL
+    assert_positions(sim.get(pdgb.VAR_POSITION), ora.position, sc.pos, 0, f"spmv path {path} breaking")
 
 
 @pytest.mark.parametrize("path", [1, 2])
@@ -161,7 +162,7 @@ def test_spmv_paths_cube(pdgb, scenes, path):
     sc.opt.spmv_path = path
     sim, ora = _run_pair(pdgb, scenes, sc, 40, check_every=20)
     assert sim.params()[2].spmv_path == path
-    assert rel_err(sim.get(pdgb.VAR_POSITION), ora.position) < MIXED_TOL
+    assert_positions(sim.get(pdgb.VAR_POSITION), ora.position, sc.pos, 0, f"spmv path {path} cube")
 
 
 def test_spmv_tiled_large_autotuned(pdgb, scenes):
@@ -181,7 +182,7 @@ def test_spmv_tiled_large_autotuned(pdgb, scenes):
     ora.advance(6)
     for path, sim in runs.items():
         assert same_sets(sim.alive_sets(), ora.alive_sets())
-        assert rel_err(sim.get(pdgb.VAR_POSITION), ora.position) < MIXED_TOL, path
+        assert_positions(sim.get(pdgb.VAR_POSITION), ora.position, sc.pos, 0, f"24k ball path {path}")
 
 
 @pytest.mark.parametrize("precision,tol", [(1, FP64_TOL), (0, MIXED_TOL)])
@@ -190,7 +191,7 @@ def test_pd_pd_contact(pdgb, scenes, precision, tol):
     off in the reference build) against the oracle's brute-force pairs."""
     sc = scenes.two_blocks(precision=precision)
     sim, ora = _run_pair(pdgb, scenes, sc, 80, check_every=20)
-    assert rel_err(sim.get(pdgb.VAR_POSITION), ora.position) < tol
+    assert_positions(sim.get(pdgb.VAR_POSITION), ora.position, sc.pos, precision, "pd-pd contact")
     assert rel_err(sim.get(pdgb.VAR_VELOCITY), ora.velocity) < max(tol, 1e-7) * 100
     # the contact changed the motion: without it the blocks pass into each other
     free = scenes.make_simulator(scenes.two_blocks(precision=precision, contact=False))

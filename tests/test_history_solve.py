@@ -69,6 +69,26 @@ def test_galerkin_condition(hist_solve, dependent):
     assert np.linalg.norm(r0) < np.linalg.norm(r1)
 
 
+def test_dependent_column_after_the_first_pivot(hist_solve):
+    """The largest column is chosen first (index 0) and a later column is a
+    combination of it and another one: every row after the pivot must be
+    downdated, so exactly one column is dropped."""
+    rng = np.random.default_rng(5)
+    n = 200
+    B = rng.standard_normal((n, n)) / np.sqrt(n)
+    A = B @ B.T + 2.0 * np.eye(n)
+    h0 = 10.0 * rng.standard_normal(n)
+    h1 = rng.standard_normal(n)
+    h2 = rng.standard_normal(n)
+    H = np.stack([h0, h1, h2, h0 + h1], 1)
+    r1 = rng.standard_normal(n)
+    used, y = hist_solve(4, H.T @ H, H.T @ A @ H, H.T @ r1, 1e-12)
+    assert used == 3
+    assert np.count_nonzero(y) == 3
+    r0 = r1 - A @ (H @ y)
+    assert np.abs(H.T @ r0).max() <= 1e-8 * np.abs(H.T @ r1).max()
+
+
 def test_threshold_drops_noise_columns(hist_solve):
     """A column whose part outside the others' span is below sqrt(rel) of the
     largest norm is dropped."""

@@ -23,8 +23,12 @@ def _vectors(pdgb, sim, seed):
     return v, x.cuda()
 
 
+@pytest.mark.parametrize("blocks", [None, 0, 1])
 @pytest.mark.parametrize("precision", [0, 1])
-def test_noalloc_matches_apply_operator(pdgb, scenes, precision):
+def test_noalloc_matches_apply_operator(pdgb, scenes, precision, blocks):
+    """blocks None: the view's own grid; 0: the automatic grid (rows per
+    block from the lanes, at most 4096 blocks); 1: one block striding over
+    every row."""
     import torch
     sc = scenes.reference_block(n_side=9, integrator=pdgb.NEWMARK_BETA, adaptive=1, expansion=300.0)
     sc.opt.precision = precision
@@ -32,6 +36,8 @@ def test_noalloc_matches_apply_operator(pdgb, scenes, precision):
     sim.makeReady()
     sim.advance(32)
     v, x = _vectors(pdgb, sim, 3)
+    if blocks is not None:
+        v.blocks = blocks
     y_ref = torch.full_like(x, float("nan"))
     dot_ref = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda")
     sim.synchronize()
@@ -63,3 +69,28 @@ def test_noalloc_rejects_more_blocks_than_the_scratch_holds(pdgb, scenes):
     with pytest.raises(pdgb.PdError) as e:
         pdgb.apply_operator_noalloc(v, x.data_ptr(), y.data_ptr(), None, sim.stream_handle())
     assert e.value.status == 1 and "4096" in str(e.value)
+
+
+def test_noalloc_allocates_nothing(pdgb, scenes):
+    """Repeated calls leave the device's free memory unchanged (measured after
+    a first call, which loads the library's module and resolves the scratch)."""
+    import torch
+    sc = scenes.reference_block(n_side=8)
+    sim = scenes.make_simulator(sc)
+    sim.makeReady()
+    v, x = _vectors(pdgb, sim, 5)
+    v.blocks = 0
+    y = torch.zeros_like(x)
+    dot = torch.zeros((1,), dtype=torch.float64, device="cuda")
+    stream = sim.stream_handle()
+    torch.cuda.synchronize()
+    pdgb.apply_operator_noalloc(v, x.data_ptr(), y.data_ptr(), dot.data_ptr(), stream)
+    sim.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    torch_bytes0 = torch.cuda.memory_allocated()
+    for _ in range(20):
+        pdgb.apply_operator_noalloc(v, x.data_ptr(), y.data_ptr(), dot.data_ptr(), stream)
+    sim.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert torch.cuda.memory_allocated() == torch_bytes0
