@@ -63,7 +63,8 @@ def parse_args(argv=None):
     ap.add_argument("--n", type=int, default=TARGET_N, help="target particle count")
     ap.add_argument("--lanes", type=int, default=0, help="lanes per particle row (0 = automatic)")
     ap.add_argument("--unroll", type=int, default=0, help="SpMV gather unroll 1/2/4 (0 = automatic)")
-    ap.add_argument("--spmv-path", type=int, default=0, help="1 shared-memory tiles, 2 per-bond gathers, 0 automatic")
+    ap.add_argument("--spmv-path", type=int, default=0,
+                    help="1 shared-memory tiles, 2 per-bond gathers, 3 lattice stencil, 0 automatic")
     ap.add_argument("--workload", choices=("ellipsoid", "batched", "learned", "beam"), default="ellipsoid",
                     help="ellipsoid: the 1M-particle headline; batched: 64 scenes in one batch; learned: "
                          "learned vs plain CG warm start on the 16^3 cube; beam: FP32 vs FP64 notched beam")
@@ -237,6 +238,15 @@ def cpu_oracle_run(n_target, warmup, steps):
             "timed_s": dt, "cg_iterations_per_step": iters / max(steps, 1), "setup_s": t_setup}
 
 
+def spmv_variant(opt, args):
+    """The product in use, as pd_get_options reports it."""
+    how = "fixed" if args.spmv_path else "autotuned"
+    if opt.spmv_path == 3:
+        return "lattice stencil (brick halos in shared memory, 1/d0 table per stencil entry) (%s)" % how
+    return "%s, %d lanes x %d unroll (%s)" % ("shared-memory tiles" if opt.spmv_path == 1 else "per-bond gathers",
+                                             opt.lanes_per_particle, opt.spmv_unroll, how)
+
+
 # ---- GPU arm -------------------------------------------------------------------------------
 def run_gb300(args):
     world, rank, local = dist_env()
@@ -291,7 +301,8 @@ def run_gb300(args):
     achieved = spmv_bytes / spmv_s / 1e9 if spmv_launches else None
     peak, peak_kind = measured_peak_hbm()
     traffic = None
-    tr = ncu_traffic("k_spmv")
+    kernel_name = "k_spmv_lattice" if sim.params()[2].spmv_path == 3 else "k_spmv"
+    tr = ncu_traffic(kernel_name)
     if tr is not None:
         bytes_ref, n_ref, b_ref = tr
         traffic = bytes_ref * (4.0 * bonds + 64.0 * n) / (4.0 * b_ref + 64.0 * n_ref)
@@ -319,17 +330,14 @@ def run_gb300(args):
             "cg_initial_guess": ("previous solution (the reference's)" if args.warm_start == 0 else
                                  "history projection: previous solution + Galerkin correction in the span of "
                                  "the last %d solutions" % (sim.params()[2].history_size or 8)),
-            "spmv_variant": "%s, %d lanes x %d unroll (%s)" % (
-                "shared-memory tiles" if sim.params()[2].spmv_path == 1 else "per-bond gathers",
-                sim.params()[2].lanes_per_particle, sim.params()[2].spmv_unroll,
-                "fixed" if args.lanes and args.unroll and args.spmv_path else "autotuned"),
+            "spmv_variant": spmv_variant(sim.params()[2], args),
             "parallelism": "replicas x%d" % world,
             "l2": "inputs larger than L2 (bond columns + 1/d0 %.0f MB + particle state > 129 MB L2)" % (8 * bonds / 1e6),
         },
         "gpu_launches": int(launches),
         "kernel_time_share": shares,
         "roofline": {
-            "kernel": "k_spmv (matrix-free A*p)",
+            "kernel": "%s (matrix-free A*p)" % kernel_name,
             "bound": "hbm",
             "achieved": round(achieved, 1) if achieved else None,
             "peak": peak,

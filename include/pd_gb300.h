@@ -136,11 +136,17 @@ typedef struct pd_solver_options {
      * the span of the last history_size solutions (history projection, either
      * precision).  The CG still runs to the same tolerance. */
     int warm_start;
-    /* mixed-precision SpMV path: 0 or 2 = per-bond gathers from global
-     * memory; 1 = shared-memory tiles of 256 consecutive rows and their halos
-     * (measured slower than the gathers at 1M particles; kept as an option).
-     * Either way lanes x unroll is measured at make_ready when n >= 20000;
-     * pd_get_options reports the path in use (1 or 2). */
+    /* mixed-precision SpMV path: 2 = per-bond gathers from global memory;
+     * 1 = shared-memory tiles of 256 consecutive rows and their halos
+     * (measured slower than the gathers at 1M particles; kept as an option);
+     * 3 = lattice stencil: for bodies whose particles each lie within 0.3
+     * spacings (2 r) of a distinct site of a simple-cubic lattice -- as the
+     * reference's Scene fills them -- the slots are renumbered brick by
+     * brick and the product walks each row's stencil of lattice offsets over
+     * the brick's halo staged in shared memory (other bodies fall back to
+     * 2); 0 = automatic: from 20000 particles, 3 when the body is a lattice
+     * fill, timed against the lanes x unroll shapes of 2 at make_ready.
+     * pd_get_options reports the path in use (1, 2 or 3). */
     int spmv_path;
     /* PD-PD contact (collectPDParticles / collidePDParticles,
      * src/core/simulator.cuh:606-768, compiled out in the reference): every

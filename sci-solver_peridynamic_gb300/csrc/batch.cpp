@@ -424,6 +424,7 @@ pd_status Batch::make_ready()
     free_device();
     for (size_t s = 0; s < eng_.size(); ++s) {
         Engine& e = *eng_[s];
+        e.batch_member_ = true;   // the batch kernels walk the builder's CSR rows
         pd_status st = e.make_ready();
         if (st == PD_OK) st = e.synchronize();
         if (st != PD_OK) {

@@ -385,6 +385,38 @@ cudaError_t scan_exclusive_u32(const unsigned* in, unsigned* out, long long n, c
     return exclusive_scan(in, out, n, st);
 }
 
+cudaError_t sort_pairs_u32(unsigned* keys, int* vals, int n, int key_bits, cudaStream_t st)
+{
+    if (n <= 1) return cudaSuccess;
+    const int tiles = (n + kSortTile - 1) / kSortTile;
+    unsigned *k1 = nullptr, *hist = nullptr;
+    int* v1 = nullptr;
+    PD_TRY(cudaMalloc(&k1, sizeof(unsigned) * n));
+    PD_TRY(cudaMalloc(&v1, sizeof(int) * n));
+    PD_TRY(cudaMalloc(&hist, sizeof(unsigned) * 256 * (size_t)tiles));
+    unsigned *ka = keys, *kb = k1;
+    int *va = vals, *vb = v1;
+    cudaError_t e = cudaSuccess;
+    for (int shift = 0; shift < key_bits && e == cudaSuccess; shift += 8) {
+        k_radix_hist<<<tiles, kSortThreads, 0, st>>>(ka, n, shift, tiles, hist);
+        e = exclusive_scan(hist, hist, 256LL * tiles, st);
+        if (e != cudaSuccess) break;
+        k_radix_scatter<<<tiles, kSortThreads, 0, st>>>(ka, va, n, shift, tiles, hist, kb, vb);
+        std::swap(ka, kb);
+        std::swap(va, vb);
+    }
+    if (e == cudaSuccess && ka != keys) {   // an odd number of passes: copy back
+        e = cudaMemcpyAsync(keys, ka, sizeof(unsigned) * n, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(vals, va, sizeof(int) * n, cudaMemcpyDeviceToDevice, st);
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    cudaError_t e2 = cudaStreamSynchronize(st);
+    cudaFree(k1);
+    cudaFree(v1);
+    cudaFree(hist);
+    return e != cudaSuccess ? e : e2;
+}
+
 void gather_double4(const dbl4* in, const int* perm, dbl4* out, int n, cudaStream_t st)
 {
     if (n > 0) k_gather_d4<<<grid_for(n), kBlock, 0, st>>>(in, perm, out, n);

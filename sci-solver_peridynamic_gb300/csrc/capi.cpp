@@ -77,11 +77,11 @@ pd_status pd_create(const pd_sim_params* sim, const pd_run_params* run, const pd
         g_create_error = "contact distance and volume must be positive";
         return PD_ERR_INVALID_ARGUMENT;
     }
-    if (o.spmv_path < 0 || o.spmv_path > 2 ||
+    if (o.spmv_path < 0 || o.spmv_path > 3 ||
         (o.lanes_per_particle != 0 && o.lanes_per_particle != 4 && o.lanes_per_particle != 8 &&
          o.lanes_per_particle != 16 && o.lanes_per_particle != 32) ||
         (o.spmv_unroll != 0 && o.spmv_unroll != 1 && o.spmv_unroll != 2 && o.spmv_unroll != 4)) {
-        g_create_error = "SpMV options: spmv_path 0..2, lanes 0/4/8/16/32, unroll 0/1/2/4";
+        g_create_error = "SpMV options: spmv_path 0..3, lanes 0/4/8/16/32, unroll 0/1/2/4";
         return PD_ERR_INVALID_ARGUMENT;
     }
     pd_handle* h = new (std::nothrow) pd_handle{nullptr};

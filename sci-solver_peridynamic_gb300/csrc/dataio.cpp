@@ -423,6 +423,9 @@ pd_status Engine::dataio_load_state(size_t timestep)
         return PD_ERR_FILE;
     }
     CK(cudaMemcpy(d_perm_, perm.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice), "upload perm");
+    // the lattice product's tables follow this handle's slot order: a state
+    // saved in another order continues on the gather product
+    const bool same_order = std::equal(perm.begin(), perm.end(), perm_.begin());
     perm_.assign(perm.begin(), perm.end());
     cnt_init_.assign(cinit.begin(), cinit.end());
     for (size_t i = 0; i < N; ++i) inv_[(size_t)perm_[i]] = (int)i;
@@ -452,6 +455,20 @@ pd_status Engine::dataio_load_state(size_t timestep)
             S_.halo_cap = std::min(max_halo, kMaxHaloCap);
         }
     }
+    if (lat_ok_ && !same_order) {
+        lattice_free(&latb_);
+        lat_ = LatticeParams{};
+        lat_ok_ = false;
+        if (L_.lattice) {
+            L_.lattice = 0;
+            L_.lat = nullptr;
+            L_.lanes = 8;
+            L_.unroll = 1;
+            L_.grid_bonds = grid_for_rows(8, row_kernel_blocks_per_sm(fp64_, 8, 1));
+            lay_g_ = lay_u_ = 1;
+        }
+    }
+    lattice_resync(true);
     last_params_ = P;
     CK(cudaStreamSynchronize(stream_), "state sync");
     return PD_OK;

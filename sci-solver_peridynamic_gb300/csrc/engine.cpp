@@ -140,6 +140,11 @@ void Engine::free_all()
     for (void* p : ptrs)
         if (p) cudaFree(p);
     free_tiles(S_);
+    lattice_free(&latb_);
+    lat_ = LatticeParams{};
+    lat_ok_ = false;
+    L_.lattice = 0;
+    L_.lat = nullptr;
     cudaFree(contact_.counts);
     cudaFree(contact_.start);
     cudaFree(contact_.cursor);
@@ -239,6 +244,18 @@ pd_status Engine::make_ready()
     total_slots_ = out.total;
     bonds_initial_ = out.bonds;
     sim_.pd_max_num_bonds = out.max_bonds;
+    // lattice-filled bodies: slots renumbered brick by brick for the stencil
+    // product (mixed mode; automatic above kLatticeMinRows particles, or asked
+    // for with spmv_path 3).  Bodies that are not a lattice fill keep the
+    // builder's order and the gather product.
+    if (!fp64_ && n > 0 && !batch_member_ &&
+        (opt_.spmv_path == 3 || (opt_.spmv_path == 0 && n >= kLatticeMinRows))) {
+        int ok = 0;
+        CK(lattice_build(n, 2.0 * sim_.pd_particle_radius, S_.x64, S_.X32, d_perm_, S_.row_ptr, S_.cnt, &S_.col,
+                         total_slots_, &lat_, &latb_, &ok, stream_),
+           "lattice build");
+        lat_ok_ = ok != 0;
+    }
     if (n > 0) {
         CK(cudaMemcpyAsync(S_.X64, S_.x64, sizeof(dbl4) * N, cudaMemcpyDeviceToDevice, stream_), "copy X");
         CK(cudaMemcpyAsync(d_tmp4, h_vel_.data(), sizeof(dbl4) * N, cudaMemcpyHostToDevice, stream_), "upload v");
@@ -278,6 +295,10 @@ pd_status Engine::make_ready()
             const int g = (int)std::min<long long>(std::max<long long>(((long long)n + kBlock - 1) / kBlock, 1), kMaxPartials);
             launch_bond_geometry(S_, g, stream_);
             ++launches_;
+            if (lat_ok_) {
+                launch_lattice_ell(S_, lat_, 1, g, stream_);
+                ++launches_;
+            }
         }
         const double h = sim_.pd_horizon > 0 ? sim_.pd_horizon : 1.0;
         sup_ = std::ldexp(1.0, (int)std::ceil(std::log2(h)));
@@ -367,7 +388,7 @@ int Engine::grid_for_rows(int lanes, int blocks_per_sm) const
 pd_status Engine::tune_spmv()
 {
     struct Cand {
-        int tiled, g, u;
+        int tiled, g, u, lattice = 0;
     };
     std::vector<Cand> cand;
     const int fixed_lanes = opt_.lanes_per_particle;
@@ -393,8 +414,21 @@ pd_status Engine::tune_spmv()
             }
         }
     }
+    if (lat_ok_) {
+        if (opt_.spmv_path == 3) cand.clear();   // asked for: the only candidate
+        cand.push_back({0, 1, 1, 1});
+    }
     if (cand.empty()) cand.push_back({0, fixed_lanes ? fixed_lanes : 8, fixed_unroll ? fixed_unroll : 1});
     auto apply = [&](const Cand& c) {
+        L_.lattice = c.lattice;
+        L_.lat = c.lattice ? &lat_ : nullptr;
+        if (c.lattice) {
+            L_.tiled = 0;
+            L_.lanes = 1;
+            L_.unroll = 1;
+            L_.grid_bonds = lat_.grid;
+            return;
+        }
         if (c.tiled) relayout_bonds(1, 1);
         else relayout_bonds(c.g, c.u);
         L_.tiled = c.tiled;
@@ -411,6 +445,7 @@ pd_status Engine::tune_spmv()
         // small problems: launch overhead dominates, keep the default (the
         // tiled path when it was asked for)
         Cand c = cand.size() == 1 ? cand[0] : Cand{0, 8, fp64_ ? 1 : 2};
+        if (lat_ok_ && opt_.spmv_path == 3) c = Cand{0, 1, 1, 1};
         if (opt_.spmv_path == 1 && can_tile && cand.size() > 1) c = Cand{1, fixed_lanes ? fixed_lanes : 8, fixed_unroll ? fixed_unroll : 2};
         apply(c);
         return PD_OK;
@@ -449,6 +484,20 @@ pd_status Engine::tune_spmv()
     apply(best_c);
     tuned_ms_ = best;
     return PD_OK;
+}
+
+void Engine::apply_op(const StepParams& P, const void* in, void* out, ReduceSlot slot, double* dot_out)
+{
+    if (L_.lattice) launch_spmv_lattice(dot_out != nullptr, P, S_, lat_, in, out, slot, nullptr, dot_out, stream_);
+    else launch_operator_u(fp64_, P, S_, L_.lanes, L_.unroll, L_.grid_bonds, in, out, slot, dot_out, stream_);
+}
+
+void Engine::lattice_resync(bool force)
+{
+    if (!lat_ok_ || n_ == 0) return;
+    const int g = (int)std::min<long long>(((long long)n_ + kBlock - 1) / kBlock, (long long)sm_count_ * 8);
+    launch_lattice_ell(S_, lat_, force ? 1 : 0, std::max(g, 1), stream_);
+    ++launches_;
 }
 
 void Engine::relayout_bonds(int g, int u)
@@ -711,8 +760,10 @@ pd_status Engine::operator_view(pd_operator_view* v) const
     const StepParams& P = last_params_;
     v->n = n_;
     v->precision = fp64_ ? PD_PRECISION_FP64 : PD_PRECISION_MIXED;
-    v->lanes_per_particle = L_.lanes;
-    v->blocks = L_.grid_bonds;
+    // the view describes the CSR rows; with the lattice product in use it
+    // carries a CSR launch shape of its own
+    v->lanes_per_particle = L_.lattice ? 8 : L_.lanes;
+    v->blocks = L_.lattice ? grid_for_rows(8, row_kernel_blocks_per_sm(fp64_, 8, 1)) : L_.grid_bonds;
     v->activity = S_.act;
     v->row_ptr = S_.row_ptr;
     v->bond_count = S_.cnt;
@@ -743,7 +794,7 @@ pd_status Engine::apply_operator(const void* d_x, void* d_y, double* d_dot)
     CK(cudaSetDevice(device_), "cudaSetDevice");
     // counter 4 of the handle's reduction scratch is reserved for this call
     ReduceSlot slot{S_.partials, S_.counters + 4};
-    launch_operator_u(fp64_, last_params_, S_, L_.lanes, L_.unroll, L_.grid_bonds, d_x, d_y, slot, d_dot, stream_);
+    apply_op(last_params_, d_x, d_y, slot, d_dot);
     ++launches_;
     CK(cudaGetLastError(), "apply_operator launch");
     return PD_OK;
@@ -788,6 +839,7 @@ pd_status Engine::integrate(bool* advanced)
     launch_force(fp64_, Pf, S_, L_, stream_);
     mark_end();
     launches_ += fp64_ ? 1 : 2;   // mixed: the supercell words, then the pass
+    lattice_resync(false);        // only where the pass broke a bond (read on the device)
     const bool adaptive = run_.integrator == PD_NEWMARK_BETA || run_.adaptive_integration != 0;
     if (adaptive) {
         CK(cudaMemcpyAsync(h_flags_, S_.flags, sizeof(int) * 2, cudaMemcpyDeviceToHost, stream_), "read flag");
@@ -802,6 +854,7 @@ pd_status Engine::integrate(bool* advanced)
             CK(cudaMemcpyAsync(S_.v64, S_.v64_bk, sizeof(dbl4) * N, cudaMemcpyDeviceToDevice, stream_), "restore v");
             launch_refresh(fp64_, Pf, S_, L_, stream_);
             ++launches_;
+            lattice_resync(true);   // the restored live sets
             return PD_OK;
         }
         CK(cudaMemcpyAsync(S_.cnt_bk, S_.cnt, sizeof(int) * N, cudaMemcpyDeviceToDevice, stream_), "backup cnt");
@@ -956,9 +1009,7 @@ pd_status Engine::hist_project(const StepParams& P)
     mark_begin(PD_KC_GUESS, -1);
     // products with this step's operator (counter 4 of the reduction scratch is unused without a dot)
     const ReduceSlot slot{S_.partials, S_.counters + 4};
-    for (int j = 0; j < m; ++j)
-        launch_operator_u(fp64_, P, S_, L_.lanes, L_.unroll, L_.grid_bonds, H.v[j], (void*)W.v[j], slot, nullptr,
-                          stream_);
+    for (int j = 0; j < m; ++j) apply_op(P, H.v[j], (void*)W.v[j], slot, nullptr);
     const int na = hist_dots_count(0);
     launch_hist_dots(fp64_, 0, n_, m, H, W, S_.r, d_hpart_, hist_blocks_, d_hdots_, stream_);
     launch_hist_dots(fp64_, 1, n_, m, H, W, nullptr, d_hpart_, hist_blocks_, d_hdots_ + na, stream_);
@@ -1274,7 +1325,7 @@ void Engine::params(pd_sim_params* s, pd_run_params* r, pd_solver_options* o) co
         if (ready_) {   // report the launch shape in use (autotuned when left at 0)
             o->lanes_per_particle = L_.lanes;
             o->spmv_unroll = L_.unroll;
-            o->spmv_path = L_.tiled ? 1 : 2;
+            o->spmv_path = L_.lattice ? 3 : (L_.tiled ? 1 : 2);
         }
     }
 }

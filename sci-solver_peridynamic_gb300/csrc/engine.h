@@ -63,6 +63,9 @@ private:
     StepParams step_params() const;
     int grid_for_rows(int lanes, int blocks_per_sm) const;
     pd_status tune_spmv();
+    // y = A in with this handle's product (lattice stencil or CSR rows)
+    void apply_op(const StepParams& P, const void* in, void* out, ReduceSlot slot, double* dot_out);
+    void lattice_resync(bool force);   // the lattice product's 1/d0 table from the live CSR bonds
     // mixed mode: reorders every row's live bonds for the (g, u) SpMV shape
     void relayout_bonds(int g, int u);
     // allocates the warm-start state on first use; without the network
@@ -174,6 +177,11 @@ private:
     long long kc_samples_[PD_KC_COUNT] = {};   // sampled CG iterations
     double kc_sample_ms_[PD_KC_COUNT] = {};
     long long launches_ = 0;
+    // lattice-stencil product (mixed mode, lattice-filled bodies)
+    LatticeParams lat_{};
+    LatticeBuffers latb_{};
+    bool lat_ok_ = false;
+    bool batch_member_ = false;        // set by Batch: its scenes keep the builder's slot order
     ContactBuffers contact_{};         // PD-PD contact hash (when enabled)
     size_t saved_frame_ = 0;           // DataIO::savedFrame
     bool wrote_sim_info_ = false;      // DataIO::writtenSimulationParameter

@@ -1,0 +1,523 @@
+// lattice.cu -- the system product A w for bodies filled on a lattice
+// (mixed precision).
+//
+// The reference fills every body on a simple-cubic lattice of spacing 2 r
+// (src/examples/scene.cpp:33-135) and bonds each particle to the others within
+// the horizon (src/core/kdtree.h:304-353); its product computeAx
+// (src/core/cg_solver.cuh:343-383) then gathers one 3x3 block and one vector
+// entry per bond.  Here, when every particle sits within 0.3 spacings of a
+// distinct lattice site, each bond joins two sites whose offset lies in a
+// small stencil (80 offsets for a horizon of 2.5 spacings).  The slots are
+// renumbered brick by brick (bricks of 32 x 4 x bz sites, x fastest), and the
+// product runs one brick per block iteration: the block stages the halo of
+// the brick's sites (the neighbours' supercell positions and their entries of
+// w) in shared memory, then each thread walks its row's stencil.  Rows of a
+// warp are x-consecutive sites, so the neighbours at one stencil entry are
+// x-consecutive shared-memory words (no bank conflicts), and the only per-bond
+// stream is 1/d0 per (row, stencil entry), 0 where there is no live bond.
+//
+// The per-bond arithmetic is the gather product's (step_rows.cuh,
+// mixed_bond_chunk): the bond vector is rebuilt from the same supercell words,
+// the Jacobian applied to w_p - w_q is
+//   c [ (1/d0 - 1/d) (w_p - w_q) + (xi . (w_p - w_q)) xi / d^3 ],
+// and only the order of the per-row sum differs.
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <vector>
+
+#include "step_rows.cuh"
+
+namespace pdgb {
+
+namespace {
+
+#define LT_TRY(x)                              \
+    do {                                       \
+        cudaError_t e_ = (x);                  \
+        if (e_ != cudaSuccess) return e_;      \
+    } while (0)
+
+constexpr int kLatBX = 32;
+constexpr int kLatBY = 4;
+constexpr float kLatEmpty = 1.0e4f;   // supercell offset of an empty site (any far, finite position)
+// the largest halo: R = 3, bricks of 32 x 4 x 2 sites -> 38 x 10 x 8 sites of 36 bytes
+constexpr int kLatSmemMax = 38 * 10 * 8 * 36;
+
+int blocks_for(long long n) { return (int)std::max<long long>(1, std::min<long long>((n + kBlock - 1) / kBlock, 8192)); }
+
+// ---- detection ------------------------------------------------------------------------
+// site = rint((X - anchor) / h) per axis; ext[0..2] = min, ext[3..5] = max,
+// ext[6] != 0 when some coordinate lies more than 0.3 h from its site
+__global__ void __launch_bounds__(kBlock) k_lat_sites(const dbl4* __restrict__ x, int n, double ax, double ay,
+                                                      double az, double inv_h, int4* __restrict__ site,
+                                                      int* __restrict__ ext)
+{
+    int mn[3] = {INT_MAX, INT_MAX, INT_MAX}, mx[3] = {INT_MIN, INT_MIN, INT_MIN};
+    int fail = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const dbl4 p = x[i];
+        const double f[3] = {(p.x - ax) * inv_h, (p.y - ay) * inv_h, (p.z - az) * inv_h};
+        int s[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const double r = rint(f[k]);
+            if (!(fabs(f[k] - r) <= 0.3) || !(fabs(r) < 1.0e8)) {
+                fail = 1;
+                s[k] = 0;
+            } else {
+                s[k] = (int)r;
+            }
+            mn[k] = min(mn[k], s[k]);
+            mx[k] = max(mx[k], s[k]);
+        }
+        site[i] = make_int4(s[0], s[1], s[2], 0);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        mn[k] = __reduce_min_sync(0xffffffffu, mn[k]);
+        mx[k] = __reduce_max_sync(0xffffffffu, mx[k]);
+    }
+    fail = __reduce_or_sync(0xffffffffu, fail);
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            atomicMin(&ext[k], mn[k]);
+            atomicMax(&ext[3 + k], mx[k]);
+        }
+        if (fail) atomicOr(&ext[6], 1);
+    }
+}
+
+// every live bond's site offset marked in the kLatTab^3 table (fail[0] set
+// when an offset exceeds kLatRmax on some axis)
+__global__ void __launch_bounds__(kBlock) k_lat_offsets(int n, const int4* __restrict__ site,
+                                                        const int* __restrict__ row_ptr, const int* __restrict__ cnt,
+                                                        const int* __restrict__ col, int* __restrict__ tab,
+                                                        int* __restrict__ fail)
+{
+    __shared__ int stab[kLatTab * kLatTab * kLatTab];
+    for (int i = threadIdx.x; i < kLatTab * kLatTab * kLatTab; i += blockDim.x) stab[i] = 0;
+    __syncthreads();
+    int bad = 0;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const int4 sp = site[p];
+        const int rs = row_ptr[p], cn = cnt[p];
+        for (int j = 0; j < cn; ++j) {
+            const int4 sq = site[col[rs + j]];
+            const int dx = sq.x - sp.x, dy = sq.y - sp.y, dz = sq.z - sp.z;
+            if (abs(dx) > kLatRmax || abs(dy) > kLatRmax || abs(dz) > kLatRmax) {
+                bad = 1;
+                continue;
+            }
+            stab[((dz + kLatRmax) * kLatTab + (dy + kLatRmax)) * kLatTab + (dx + kLatRmax)] = 1;
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kLatTab * kLatTab * kLatTab; i += blockDim.x)
+        if (stab[i]) atomicOr(&tab[i], 1);
+    if (bad) atomicOr(fail, 1);
+}
+
+// shifted sites and the brick-major sort key of every slot
+__global__ void __launch_bounds__(kBlock) k_lat_keys(int n, int4* __restrict__ site, int3 lo, int bz, int3 nb,
+                                                     unsigned* __restrict__ key, int* __restrict__ val)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int4 s = site[i];
+        s.x -= lo.x;
+        s.y -= lo.y;
+        s.z -= lo.z;
+        site[i] = s;
+        const unsigned brick = ((unsigned)(s.z / bz) * (unsigned)nb.y + (unsigned)(s.y / kLatBY)) * (unsigned)nb.x +
+                               (unsigned)(s.x / kLatBX);
+        const unsigned local = ((unsigned)(s.z % bz) * kLatBY + (unsigned)(s.y % kLatBY)) * kLatBX +
+                               (unsigned)(s.x % kLatBX);
+        key[i] = brick * (unsigned)(kLatBX * kLatBY * bz) + local;
+        val[i] = i;
+    }
+}
+
+__global__ void k_lat_dups(const unsigned* __restrict__ key, int n, int* __restrict__ fail)
+{
+    for (int i = 1 + blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        if (key[i] == key[i - 1]) atomicOr(fail, 1);
+}
+
+// ---- renumbering (new slot i holds old slot n2o[i]) -------------------------------------
+template <typename T>
+__global__ void k_lat_gather(const T* __restrict__ in, const int* __restrict__ n2o, T* __restrict__ out, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = in[n2o[i]];
+}
+
+__global__ void k_lat_inverse(const int* __restrict__ n2o, int* __restrict__ o2n, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) o2n[n2o[i]] = i;
+}
+
+__global__ void k_lat_lengths(const int* __restrict__ row_ptr, const int* __restrict__ n2o, unsigned* __restrict__ len,
+                              int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int o = n2o[i];
+        len[i] = (unsigned)(row_ptr[o + 1] - row_ptr[o]);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) len[n] = 0u;
+}
+
+__global__ void k_lat_remap_col(const int* __restrict__ row_ptr_old, const int* __restrict__ col_old,
+                                const unsigned* __restrict__ row_ptr_new, const int* __restrict__ n2o,
+                                const int* __restrict__ o2n, int* __restrict__ col_new, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int o = n2o[i];
+        const int a = row_ptr_old[o], len = row_ptr_old[o + 1] - a;
+        const int b = (int)row_ptr_new[i];
+        for (int j = 0; j < len; ++j) col_new[b + j] = o2n[col_old[a + j]];
+    }
+}
+
+__global__ void k_lat_map(const int4* __restrict__ site, int n, int R, int mx, int my, int* __restrict__ map)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int4 s = site[i];
+        map[((long long)(s.z + R) * my + (s.y + R)) * mx + (s.x + R)] = i;
+    }
+}
+
+// ---- 1/d0 table ------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_lat_ell(DeviceState S, LatticeParams lp, int force)
+{
+    if (!force && ((volatile int*)S.flags)[1] == 0) return;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < S.n; p += gridDim.x * blockDim.x) {
+        const int b = lp.row_brick[p];
+        const int start = lp.brick_start[b];
+        const int rows = lp.brick_start[b + 1] - start;
+        float* e = lp.ell + (size_t)lp.K * start + (p - start);
+        for (int k = 0; k < lp.K; ++k) e[(size_t)k * rows] = 0.f;
+        const int4 sp = lp.site[p];
+        const int rs = S.row_ptr[p], cn = S.cnt[p];
+        for (int j = 0; j < cn; ++j) {
+            const int4 sq = lp.site[S.col[rs + j]];
+            const int t = ((sq.z - sp.z + kLatRmax) * kLatTab + (sq.y - sp.y + kLatRmax)) * kLatTab +
+                          (sq.x - sp.x + kLatRmax);
+            e[(size_t)lp.offk[t] * rows] = S.inv_d0[rs + j];
+        }
+    }
+}
+
+// ---- the product -----------------------------------------------------------------------
+// Shared memory per halo site: A = (supercell offset x, y, z, sup * i),
+// B = (sup * j, sup * k, w.x, w.y), W = w.z (36 bytes).
+template <bool DOT>
+__global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, DeviceState S, LatticeParams lp,
+                                                           const float4* __restrict__ in, float4* __restrict__ out,
+                                                           ReduceSlot slot, CgScalars* cg, double* dot_out)
+{
+    if (DOT && cg && ((volatile CgScalars*)cg)->done) return;
+    extern __shared__ float4 lat_smem[];
+    const int H = lp.hx * lp.hy * lp.hz;
+    float4* sA = lat_smem;
+    float4* sB = sA + H;
+    float* sW = (float*)(sB + H);
+    const float sup = (float)P.sup;
+    const int hx = lp.hx, hxy = lp.hx * lp.hy;
+    const int mx = lp.map_dim[0], mxy = lp.map_dim[0] * lp.map_dim[1];
+    const int K = lp.K;
+    DotAcc32 acc;
+    for (int b = blockIdx.x; b < lp.n_bricks; b += gridDim.x) {
+        const int corner = lp.brick_corner[b];
+        const int start = lp.brick_start[b];
+        const int rows = lp.brick_start[b + 1] - start;
+        __syncthreads();   // the previous brick's rows are done with the halo
+        for (int h = threadIdx.x; h < H; h += blockDim.x) {
+            const int iz = h / hxy;
+            const int r2 = h - iz * hxy;
+            const int iy = r2 / hx;
+            const int ix = r2 - iy * hx;
+            const int q = __ldg(lp.map + corner + iz * mxy + iy * mx + ix);
+            float4 a = make_float4(kLatEmpty, kLatEmpty, kLatEmpty, 0.f), bb = make_float4(0.f, 0.f, 0.f, 0.f);
+            float wz = 0.f;
+            if (q >= 0) {
+                const float4 x = __ldg(S.xs4 + q);
+                const float4 w = __ldg(in + q);
+                const int wq = __float_as_int(x.w);
+                a = make_float4(x.x, x.y, x.z, sup * small_int_to_float(wq & 1023));
+                bb = make_float4(sup * small_int_to_float((wq >> 10) & 1023), sup * small_int_to_float((wq >> 20) & 1023),
+                                 w.x, w.y);
+                wz = w.z;
+            }
+            sA[h] = a;
+            sB[h] = bb;
+            sW[h] = wz;
+        }
+        __syncthreads();
+        for (int l = threadIdx.x; l < rows; l += blockDim.x) {
+            const int p = start + l;
+            const uint8_t ab = S.act[p];
+            if (is_dirichlet(ab & kActMask)) {
+                out[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+                continue;
+            }
+            const int c = lp.row_local[p];
+            const float4 pa = sA[c], pb = sB[c];
+            const float4 w = make_float4(pb.z, pb.w, sW[c], 0.f);
+            const float* __restrict__ e = lp.ell + (size_t)K * start + l;
+            float ax = 0.f, ay = 0.f, az = 0.f;
+#pragma unroll 4
+            for (int k = 0; k < K; ++k) {
+                const float s = __ldcs(e + (size_t)k * rows);
+                const int q = c + lp.off[k];
+                const float4 qa = sA[q], qb = sB[q];
+                const float qwz = sW[q];
+                // (X_q - X_p) + sup (ijk_q - ijk_p): the gather product's bond vector
+                const float xs = (qa.x - pa.x) + (qa.w - pa.w);
+                const float ys = (qa.y - pa.y) + (qb.x - pb.x);
+                const float zs = (qa.z - pa.z) + (qb.y - pb.y);
+                const float wx = w.x - qb.z, wy = w.y - qb.w, wz = w.z - qwz;
+                float inv_d = rsqrtf(fmaf(xs, xs, fmaf(ys, ys, zs * zs)));
+                inv_d = s > 0.f ? inv_d : 0.f;   // no live bond: the term vanishes
+                const float a1 = s - inv_d;
+                const float g = fmaf(xs, wx, fmaf(ys, wy, zs * wz)) * (inv_d * inv_d * inv_d);
+                ax = fmaf(a1, wx, fmaf(g, xs, ax));
+                ay = fmaf(a1, wy, fmaf(g, ys, ay));
+                az = fmaf(a1, wz, fmaf(g, zs, az));
+            }
+            spmv_finish_mixed<1, DOT>(P, S, p, ab, w, ax, ay, az, 0, 0xffffffffu, out, acc);
+        }
+    }
+    if (DOT) {
+        block_reduce_finish(acc, slot, [cg, dot_out](double pAp) {
+            if (cg) cg_fin_alpha(cg, pAp);
+            if (dot_out) *dot_out = pAp;
+        });
+    }
+}
+
+}  // namespace
+
+size_t lattice_smem_bytes(const LatticeParams& lp)
+{
+    return (size_t)lp.hx * lp.hy * lp.hz * (2 * sizeof(float4) + sizeof(float));
+}
+
+int lattice_spmv_blocks_per_sm(const LatticeParams& lp)
+{
+    const size_t smem = lattice_smem_bytes(lp);
+    int a = 0, b = 0;
+    // the attribute is per kernel and process: set to the largest halo any
+    // handle can need, so that every handle's launch fits
+    cudaFuncSetAttribute(k_spmv_lattice<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kLatSmemMax);
+    cudaFuncSetAttribute(k_spmv_lattice<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kLatSmemMax);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_spmv_lattice<true>, kBlock, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_spmv_lattice<false>, kBlock, smem);
+    const int m = std::min(a, b);
+    return m > 0 ? m : 1;
+}
+
+void launch_spmv_lattice(bool dot, const StepParams& P, const DeviceState& S, const LatticeParams& lp,
+                         const void* in, void* out, ReduceSlot slot, CgScalars* cg, double* dot_out, cudaStream_t st)
+{
+    const size_t smem = lattice_smem_bytes(lp);
+    const int grid = std::max(1, std::min(lp.grid, std::max(lp.n_bricks, 1)));
+    if (dot)
+        k_spmv_lattice<true><<<grid, kBlock, smem, st>>>(P, S, lp, (const float4*)in, (float4*)out, slot, cg, dot_out);
+    else
+        k_spmv_lattice<false><<<grid, kBlock, smem, st>>>(P, S, lp, (const float4*)in, (float4*)out, slot, nullptr,
+                                                           nullptr);
+}
+
+void launch_lattice_ell(const DeviceState& S, const LatticeParams& lp, int force, int grid, cudaStream_t st)
+{
+    k_lat_ell<<<grid, kBlock, 0, st>>>(S, lp, force);
+}
+
+void lattice_free(LatticeBuffers* lb)
+{
+    cudaFree(lb->brick_start);
+    cudaFree(lb->brick_corner);
+    cudaFree(lb->row_local);
+    cudaFree(lb->row_brick);
+    cudaFree(lb->site);
+    cudaFree(lb->map);
+    cudaFree(lb->offk);
+    cudaFree(lb->ell);
+    *lb = LatticeBuffers{};
+}
+
+cudaError_t lattice_build(int n, double spacing, dbl4* x64, float4* X32, int* perm, int* row_ptr, int* cnt, int** col,
+                          long long total_slots, LatticeParams* lp, LatticeBuffers* lb, int* ok, cudaStream_t st)
+{
+    *ok = 0;
+    if (n < 1 || !(spacing > 0.0) || total_slots >= (1LL << 31) - 64) return cudaSuccess;
+    // every temporary in one owner, freed on every return path
+    struct Tmp {
+        int* ext = nullptr;
+        int* tab = nullptr;
+        unsigned* key = nullptr;
+        int* n2o = nullptr;
+        int* o2n = nullptr;
+        unsigned* len = nullptr;
+        void* buf = nullptr;
+        int* col_new = nullptr;
+        LatticeBuffers lb{};
+        ~Tmp()
+        {
+            cudaFree(ext); cudaFree(tab); cudaFree(key); cudaFree(n2o); cudaFree(o2n); cudaFree(len); cudaFree(buf);
+            cudaFree(col_new);
+            lattice_free(&lb);
+        }
+    } t;
+    const int G = blocks_for(n);
+    LT_TRY(cudaMalloc(&t.lb.site, sizeof(int4) * (size_t)n));
+    LT_TRY(cudaMalloc(&t.ext, sizeof(int) * 8));
+    LT_TRY(cudaMalloc(&t.tab, sizeof(int) * kLatTab * kLatTab * kLatTab));
+    int ext_init[8] = {INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN, 0, 0};
+    LT_TRY(cudaMemcpyAsync(t.ext, ext_init, sizeof(ext_init), cudaMemcpyHostToDevice, st));
+    LT_TRY(cudaMemsetAsync(t.tab, 0, sizeof(int) * kLatTab * kLatTab * kLatTab, st));
+    // the lattice anchor: slot 0's position
+    dbl4 anchor;
+    LT_TRY(cudaMemcpyAsync(&anchor, x64, sizeof(dbl4), cudaMemcpyDeviceToHost, st));
+    LT_TRY(cudaStreamSynchronize(st));
+    k_lat_sites<<<G, kBlock, 0, st>>>(x64, n, anchor.x, anchor.y, anchor.z, 1.0 / spacing, t.lb.site, t.ext);
+    LT_TRY(cudaGetLastError());
+    int ext[8];
+    LT_TRY(cudaMemcpyAsync(ext, t.ext, sizeof(ext), cudaMemcpyDeviceToHost, st));
+    LT_TRY(cudaStreamSynchronize(st));
+    if (ext[6]) return cudaSuccess;   // not a lattice fill
+    k_lat_offsets<<<G, kBlock, 0, st>>>(n, t.lb.site, row_ptr, cnt, *col, t.tab, t.ext + 7);
+    LT_TRY(cudaGetLastError());
+    std::vector<int> tab(kLatTab * kLatTab * kLatTab);
+    LT_TRY(cudaMemcpyAsync(tab.data(), t.tab, sizeof(int) * tab.size(), cudaMemcpyDeviceToHost, st));
+    LT_TRY(cudaMemcpyAsync(ext, t.ext, sizeof(ext), cudaMemcpyDeviceToHost, st));
+    LT_TRY(cudaStreamSynchronize(st));
+    if (ext[7]) return cudaSuccess;   // a bond longer than the stencil reach
+    // the stencil: offsets in (dz, dy, dx) order
+    LatticeParams L{};
+    int R = 1;
+    std::vector<int> offk(tab.size(), -1);
+    std::vector<int3> sten;
+    for (int dz = -kLatRmax; dz <= kLatRmax; ++dz)
+        for (int dy = -kLatRmax; dy <= kLatRmax; ++dy)
+            for (int dx = -kLatRmax; dx <= kLatRmax; ++dx) {
+                const int i = ((dz + kLatRmax) * kLatTab + (dy + kLatRmax)) * kLatTab + (dx + kLatRmax);
+                if (!tab[i]) continue;
+                if ((int)sten.size() >= kLatMaxK) return cudaSuccess;
+                offk[i] = (int)sten.size();
+                sten.push_back(make_int3(dx, dy, dz));
+                R = std::max(R, std::max(std::abs(dx), std::max(std::abs(dy), std::abs(dz))));
+            }
+    L.K = (int)sten.size();
+    L.R = R;
+    L.bx = kLatBX;
+    L.by = kLatBY;
+    L.bz = R <= 2 ? 4 : 2;
+    L.hx = L.bx + 2 * R;
+    L.hy = L.by + 2 * R;
+    L.hz = L.bz + 2 * R;
+    for (int k = 0; k < L.K; ++k) L.off[k] = (sten[k].z * L.hy + sten[k].y) * L.hx + sten[k].x;
+    const long long D[3] = {(long long)ext[3] - ext[0] + 1, (long long)ext[4] - ext[1] + 1,
+                            (long long)ext[5] - ext[2] + 1};
+    const long long NB[3] = {(D[0] + L.bx - 1) / L.bx, (D[1] + L.by - 1) / L.by, (D[2] + L.bz - 1) / L.bz};
+    const long long M[3] = {NB[0] * L.bx + 2 * R, NB[1] * L.by + 2 * R, NB[2] * L.bz + 2 * R};
+    const long long map_size = M[0] * M[1] * M[2];
+    const long long bricks_total = NB[0] * NB[1] * NB[2];
+    // a dense site map of modest size (the body fills a good part of its box)
+    if (map_size > std::max<long long>(16LL * n, 1LL << 22) || map_size >= (1LL << 31) ||
+        bricks_total * L.bx * L.by * L.bz >= (1LL << 32))
+        return cudaSuccess;
+    for (int k = 0; k < 3; ++k) L.map_dim[k] = (int)M[k];
+    // brick-major keys, sorted; two particles on one site: not a lattice fill
+    LT_TRY(cudaMalloc(&t.key, sizeof(unsigned) * (size_t)n));
+    LT_TRY(cudaMalloc(&t.n2o, sizeof(int) * (size_t)n));
+    k_lat_keys<<<G, kBlock, 0, st>>>(n, t.lb.site, make_int3(ext[0], ext[1], ext[2]), L.bz,
+                                     make_int3((int)NB[0], (int)NB[1], (int)NB[2]), t.key, t.n2o);
+    LT_TRY(cudaGetLastError());
+    int key_bits = 0;
+    while (key_bits < 32 && (1ULL << key_bits) < (unsigned long long)(bricks_total * L.bx * L.by * L.bz)) ++key_bits;
+    key_bits = (key_bits + 7) / 8 * 8;
+    LT_TRY(sort_pairs_u32(t.key, t.n2o, n, std::max(key_bits, 8), st));
+    LT_TRY(cudaMemsetAsync(t.ext + 7, 0, sizeof(int), st));
+    k_lat_dups<<<G, kBlock, 0, st>>>(t.key, n, t.ext + 7);
+    LT_TRY(cudaMemcpyAsync(ext + 7, t.ext + 7, sizeof(int), cudaMemcpyDeviceToHost, st));
+    std::vector<unsigned> keys(n);
+    LT_TRY(cudaMemcpyAsync(keys.data(), t.key, sizeof(unsigned) * (size_t)n, cudaMemcpyDeviceToHost, st));
+    LT_TRY(cudaStreamSynchronize(st));
+    if (ext[7]) return cudaSuccess;
+    // ---- from here on the particles are renumbered: no more early returns ----
+    LT_TRY(cudaMalloc(&t.o2n, sizeof(int) * (size_t)n));
+    LT_TRY(cudaMalloc(&t.len, sizeof(unsigned) * ((size_t)n + 1)));
+    LT_TRY(cudaMalloc(&t.buf, sizeof(dbl4) * (size_t)n));
+    k_lat_inverse<<<G, kBlock, 0, st>>>(t.n2o, t.o2n, n);
+    k_lat_gather<dbl4><<<G, kBlock, 0, st>>>(x64, t.n2o, (dbl4*)t.buf, n);
+    LT_TRY(cudaMemcpyAsync(x64, t.buf, sizeof(dbl4) * (size_t)n, cudaMemcpyDeviceToDevice, st));
+    k_lat_gather<float4><<<G, kBlock, 0, st>>>(X32, t.n2o, (float4*)t.buf, n);
+    LT_TRY(cudaMemcpyAsync(X32, t.buf, sizeof(float4) * (size_t)n, cudaMemcpyDeviceToDevice, st));
+    k_lat_gather<int4><<<G, kBlock, 0, st>>>(t.lb.site, t.n2o, (int4*)t.buf, n);
+    LT_TRY(cudaMemcpyAsync(t.lb.site, t.buf, sizeof(int4) * (size_t)n, cudaMemcpyDeviceToDevice, st));
+    k_lat_gather<int><<<G, kBlock, 0, st>>>(perm, t.n2o, (int*)t.buf, n);
+    LT_TRY(cudaMemcpyAsync(perm, t.buf, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, st));
+    k_lat_gather<int><<<G, kBlock, 0, st>>>(cnt, t.n2o, (int*)t.buf, n);
+    LT_TRY(cudaMemcpyAsync(cnt, t.buf, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, st));
+    // CSR: rows keep their padded lengths and bond order; columns renamed
+    k_lat_lengths<<<G, kBlock, 0, st>>>(row_ptr, t.n2o, t.len, n);
+    LT_TRY(scan_exclusive_u32(t.len, t.len, (long long)n + 1, st));
+    LT_TRY(cudaMalloc(&t.col_new, sizeof(int) * ((size_t)total_slots + 8)));
+    LT_TRY(cudaMemsetAsync(t.col_new, 0, sizeof(int) * ((size_t)total_slots + 8), st));
+    k_lat_remap_col<<<G, kBlock, 0, st>>>(row_ptr, *col, t.len, t.n2o, t.o2n, t.col_new, n);
+    LT_TRY(cudaMemcpyAsync(row_ptr, t.len, sizeof(int) * ((size_t)n + 1), cudaMemcpyDeviceToDevice, st));
+    LT_TRY(cudaGetLastError());
+    std::swap(*col, t.col_new);   // the old column array is freed with the temporaries
+    // bricks, each row's halo index, the site map and the stencil lookup
+    const unsigned bsz = (unsigned)(L.bx * L.by * L.bz);
+    std::vector<int> bstart, bcorner, rlocal(n), rbrick(n);
+    for (int i = 0; i < n; ++i) {
+        const unsigned brick = keys[i] / bsz, local = keys[i] % bsz;
+        if (i == 0 || brick != keys[i - 1] / bsz) {
+            bstart.push_back(i);
+            const long long bxi = brick % NB[0], byi = (brick / NB[0]) % NB[1], bzi = brick / (NB[0] * NB[1]);
+            bcorner.push_back((int)(((bzi * L.bz) * M[1] + byi * L.by) * M[0] + bxi * L.bx));
+        }
+        const int lx = (int)(local % L.bx), ly = (int)((local / L.bx) % L.by), lz = (int)(local / (L.bx * L.by));
+        rlocal[i] = ((lz + R) * L.hy + (ly + R)) * L.hx + (lx + R);
+        rbrick[i] = (int)bstart.size() - 1;
+    }
+    L.n_bricks = (int)bstart.size();
+    bstart.push_back(n);
+    LT_TRY(cudaMalloc(&t.lb.brick_start, sizeof(int) * bstart.size()));
+    LT_TRY(cudaMalloc(&t.lb.brick_corner, sizeof(int) * bcorner.size()));
+    LT_TRY(cudaMalloc(&t.lb.row_local, sizeof(int) * (size_t)n));
+    LT_TRY(cudaMalloc(&t.lb.row_brick, sizeof(int) * (size_t)n));
+    LT_TRY(cudaMalloc(&t.lb.map, sizeof(int) * (size_t)map_size));
+    LT_TRY(cudaMalloc(&t.lb.offk, sizeof(int) * offk.size()));
+    LT_TRY(cudaMalloc(&t.lb.ell, sizeof(float) * (size_t)L.K * (size_t)n));
+    LT_TRY(cudaMemcpyAsync(t.lb.brick_start, bstart.data(), sizeof(int) * bstart.size(), cudaMemcpyHostToDevice, st));
+    LT_TRY(cudaMemcpyAsync(t.lb.brick_corner, bcorner.data(), sizeof(int) * bcorner.size(), cudaMemcpyHostToDevice, st));
+    LT_TRY(cudaMemcpyAsync(t.lb.row_local, rlocal.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, st));
+    LT_TRY(cudaMemcpyAsync(t.lb.row_brick, rbrick.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, st));
+    LT_TRY(cudaMemcpyAsync(t.lb.offk, offk.data(), sizeof(int) * offk.size(), cudaMemcpyHostToDevice, st));
+    LT_TRY(cudaMemsetAsync(t.lb.map, 0xff, sizeof(int) * (size_t)map_size, st));
+    k_lat_map<<<G, kBlock, 0, st>>>(t.lb.site, n, R, (int)M[0], (int)M[1], t.lb.map);
+    LT_TRY(cudaGetLastError());
+    LT_TRY(cudaStreamSynchronize(st));   // the host vectors above are read by the copies
+    L.brick_start = t.lb.brick_start;
+    L.brick_corner = t.lb.brick_corner;
+    L.row_local = t.lb.row_local;
+    L.row_brick = t.lb.row_brick;
+    L.site = t.lb.site;
+    L.map = t.lb.map;
+    L.offk = t.lb.offk;
+    L.ell = t.lb.ell;
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    L.grid = std::max(1, std::min(L.n_bricks, lattice_spmv_blocks_per_sm(L) * sms));
+    *lp = L;
+    *lb = t.lb;
+    t.lb = LatticeBuffers{};
+    *ok = 1;
+    return cudaGetLastError();
+}
+
+}  // namespace pdgb

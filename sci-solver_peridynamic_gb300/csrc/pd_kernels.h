@@ -135,6 +135,51 @@ struct DeviceState {
     int* flags;              // [0] has_broken, [1] broken bonds this pass, [2] overflow
 };
 
+// ---- lattice-stencil SpMV (lattice.cu) ---------------------------------------
+// Bodies filled on a simple-cubic lattice (the reference's Scene fills every
+// body that way, src/examples/scene.cpp:33-135) keep each particle within a
+// fraction of a spacing of its lattice site, and every bond joins two sites
+// whose offset lies in a small stencil.  For such bodies the slots are
+// renumbered brick by brick (bricks of bx x by x bz sites, x fastest), and the
+// product runs brick-wise with the brick's halo of sites staged in shared
+// memory: a row's neighbour at stencil entry k sits at a fixed shared-memory
+// offset, and 1/d0 per (row, stencil entry) streams from a table in which 0
+// marks "no live bond" (no particle there, beyond the horizon, or broken).
+constexpr int kLatMaxK = 160;        // stencil entries at most
+constexpr int kLatticeMinRows = 20000;   // automatic choice: smaller bodies keep the gather product
+constexpr int kLatRmax = 3;          // largest offset per axis (sites)
+constexpr int kLatTab = 2 * kLatRmax + 1;
+
+struct LatticeParams {
+    int K;                    // stencil entries
+    int R;                    // halo width (sites)
+    int bx, by, bz;           // brick extent (sites)
+    int hx, hy, hz;           // halo extent = brick + 2R
+    int n_bricks;
+    int grid;                 // blocks of the product
+    int map_dim[3];           // site map extent (bricks + R on each side)
+    const int* brick_start;   // n_bricks + 1: slot range of each brick
+    const int* brick_corner;  // n_bricks: map index of the halo's first site
+    const int* row_local;     // n: halo index of the row's own site
+    const int* row_brick;     // n: brick of each slot
+    const int4* site;         // n: site coordinates (x, y, z) of each slot, from the map's first site
+    const int* map;           // site map: slot or -1
+    const int* offk;          // kLatTab^3: stencil entry of an offset, or -1
+    float* ell;               // K per row, brick-major: [K * start_b + k * rows_b + l]
+    int off[kLatMaxK];        // halo index offset of each stencil entry
+};
+
+struct LatticeBuffers {       // device allocations owned by the engine
+    int* brick_start = nullptr;
+    int* brick_corner = nullptr;
+    int* row_local = nullptr;
+    int* row_brick = nullptr;
+    int4* site = nullptr;
+    int* map = nullptr;
+    int* offk = nullptr;
+    float* ell = nullptr;
+};
+
 // ---- step kernels (step.cu) --------------------------------------------------
 struct LaunchCfg {
     int lanes;          // SpMV lanes per particle row (4, 8, 16, 32)
@@ -145,7 +190,26 @@ struct LaunchCfg {
     int force_lanes;    // force-pass lanes per particle row
     int grid_force;     // force-pass blocks
     int grid_vec;       // blocks for per-particle vector kernels
+    int lattice;        // 1: lattice-stencil SpMV (mixed mode, lat set)
+    const LatticeParams* lat;
 };
+
+// Lattice detection and slot renumbering, after build_bonds (the arrays are
+// the builder's, in its slot order, and are permuted in place): returns
+// cudaSuccess with *ok = 0 when the particles are not a lattice fill whose
+// bonds fit the stencil (nothing is changed then).  spacing: the lattice
+// spacing (2 r).  On success fills *lp (without `ell`) and *lb.
+cudaError_t lattice_build(int n, double spacing, dbl4* x64, float4* X32, int* perm, int* row_ptr, int* cnt, int** col,
+                          long long total_slots, LatticeParams* lp, LatticeBuffers* lb, int* ok, cudaStream_t st);
+// 1/d0 table from the live CSR bonds (force = 0: only when the force pass
+// reported a broken bond, read from S.flags[1] on the device)
+void launch_lattice_ell(const DeviceState& S, const LatticeParams& lp, int force, int grid, cudaStream_t st);
+// y = A(in) by the lattice stencil; dot as launch_operator (cg: CG iteration)
+void launch_spmv_lattice(bool dot, const StepParams& P, const DeviceState& S, const LatticeParams& lp,
+                         const void* in, void* out, ReduceSlot slot, CgScalars* cg, double* dot_out, cudaStream_t st);
+int lattice_spmv_blocks_per_sm(const LatticeParams& lp);
+size_t lattice_smem_bytes(const LatticeParams& lp);
+void lattice_free(LatticeBuffers* lb);
 
 void launch_force(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
 void launch_cg_init(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
@@ -176,6 +240,8 @@ void free_tiles(DeviceState& S);
 int tile_spmv_blocks_per_sm(int lanes, int unroll, int halo_cap);
 void launch_spmv_tiled(bool dot, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
 cudaError_t scan_exclusive_u32(const unsigned* in, unsigned* out, long long n, cudaStream_t st);
+// Stable LSD radix sort of (key, value) pairs on the low key_bits bits, in place.
+cudaError_t sort_pairs_u32(unsigned* keys, int* vals, int n, int key_bits, cudaStream_t st);
 
 // PD-PD contact (contact.cu)
 struct ContactParams {

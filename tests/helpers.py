@@ -76,19 +76,22 @@ def rel_disp_err(x, ref, x0):
     return float(np.abs(x - ref).max() / scale)
 
 
-# positions: of max |x_ref|; displacements u = x - x0: of max |u_ref|
+# positions: of max |x_ref|; displacements u = x - x0: of max |u_ref|.
+# Largest errors measured over the parity tests on a GB300: mixed 4.8e-6 of
+# the displacement (PD-PD contact 6.3e-5, see its test), FP64 8.3e-9.
 POS_TOL = {0: 1e-5, 1: 1e-9}      # mixed, FP64
-DISP_TOL = {0: 1e-3, 1: 1e-7}
+DISP_TOL = {0: 2e-5, 1: 5e-8}
 
 
-def assert_positions(x, ref, x0, precision, label=""):
+def assert_positions(x, ref, x0, precision, label="", disp_tol=None):
     """Positions within POS_TOL of max |ref| and displacements from x0 within
-    DISP_TOL of the reference's largest displacement (precision 0 mixed, 1
-    FP64).  Prints both errors (pytest -s shows them)."""
+    DISP_TOL (or disp_tol) of the reference's largest displacement (precision
+    0 mixed, 1 FP64).  Prints both errors (pytest -s shows them)."""
     e_x, e_u = rel_err(x, ref), rel_disp_err(x, ref, x0)
     print(f"[parity] {label}: position {e_x:.3e}, displacement {e_u:.3e}")
     assert e_x < POS_TOL[precision], f"{label}: position error {e_x:.3e}"
-    assert e_u < DISP_TOL[precision], f"{label}: displacement error {e_u:.3e}"
+    tol_u = DISP_TOL[precision] if disp_tol is None else disp_tol
+    assert e_u < tol_u, f"{label}: displacement error {e_u:.3e}"
     return e_x, e_u
 
 

@@ -130,7 +130,7 @@ def test_no_gpu_fails_loudly(pdgb, scenes):
     assert e.value.status == 5
 
 
-@pytest.mark.parametrize("field,value", [("spmv_path", 3), ("lanes_per_particle", 6), ("spmv_unroll", 3)])
+@pytest.mark.parametrize("field,value", [("spmv_path", 4), ("spmv_path", -1), ("lanes_per_particle", 6), ("spmv_unroll", 3)])
 def test_invalid_spmv_options_rejected(pdgb, scenes, field, value):
     """Option checks run before any device call: an unsupported SpMV shape is
     an invalid argument (status 1), not a silent default."""
