@@ -42,7 +42,9 @@ constexpr int kLatBX = 32;
 constexpr int kLatBY = 4;
 constexpr float kLatEmpty = 1.0e4f;   // supercell offset of an empty site (any far, finite position)
 // the largest halo: R = 3, bricks of 32 x 4 x 2 sites -> 38 x 10 x 8 sites of 36 bytes
-constexpr int kLatSmemMax = 38 * 10 * 8 * 36;
+constexpr int kLatHaloMax = 38 * 10 * 8;
+constexpr int kLatSmemMax = kLatHaloMax * 36;
+constexpr int kLatHaloPerThread = (kLatHaloMax + kBlock - 1) / kBlock;
 
 int blocks_for(long long n) { return (int)std::max<long long>(1, std::min<long long>((n + kBlock - 1) / kBlock, 8192)); }
 
@@ -194,15 +196,18 @@ __global__ void __launch_bounds__(kBlock) k_lat_ell(DeviceState S, LatticeParams
         const int b = lp.row_brick[p];
         const int start = lp.brick_start[b];
         const int rows = lp.brick_start[b + 1] - start;
-        float* e = lp.ell + (size_t)lp.K * start + (p - start);
-        for (int k = 0; k < lp.K; ++k) e[(size_t)k * rows] = 0.f;
+        const int l = p - start;
+        float* e = lp.ell + (size_t)lp.K * start;
+        for (int k4 = 0; k4 < lp.K / 4; ++k4)
+            ((float4*)e)[(size_t)k4 * rows + l] = make_float4(0.f, 0.f, 0.f, 0.f);
         const int4 sp = lp.site[p];
         const int rs = S.row_ptr[p], cn = S.cnt[p];
         for (int j = 0; j < cn; ++j) {
             const int4 sq = lp.site[S.col[rs + j]];
             const int t = ((sq.z - sp.z + kLatRmax) * kLatTab + (sq.y - sp.y + kLatRmax)) * kLatTab +
                           (sq.x - sp.x + kLatRmax);
-            e[(size_t)lp.offk[t] * rows] = S.inv_d0[rs + j];
+            const int k = lp.offk[t];
+            e[((size_t)(k >> 2) * rows + l) * 4 + (k & 3)] = S.inv_d0[rs + j];
         }
     }
 }
@@ -231,12 +236,26 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
         const int start = lp.brick_start[b];
         const int rows = lp.brick_start[b + 1] - start;
         __syncthreads();   // the previous brick's rows are done with the halo
-        for (int h = threadIdx.x; h < H; h += blockDim.x) {
-            const int iz = h / hxy;
-            const int r2 = h - iz * hxy;
-            const int iy = r2 / hx;
-            const int ix = r2 - iy * hx;
-            const int q = __ldg(lp.map + corner + iz * mxy + iy * mx + ix);
+        // the map entries of this thread's halo sites first (independent
+        // loads), then their positions and w entries
+        int qs[kLatHaloPerThread];
+#pragma unroll
+        for (int t = 0; t < kLatHaloPerThread; ++t) {
+            const int h = threadIdx.x + t * kBlock;
+            qs[t] = -1;
+            if (h < H) {
+                const int iz = h / hxy;
+                const int r2 = h - iz * hxy;
+                const int iy = r2 / hx;
+                const int ix = r2 - iy * hx;
+                qs[t] = __ldg(lp.map + corner + iz * mxy + iy * mx + ix);
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < kLatHaloPerThread; ++t) {
+            const int h = threadIdx.x + t * kBlock;
+            if (h >= H) continue;
+            const int q = qs[t];
             float4 a = make_float4(kLatEmpty, kLatEmpty, kLatEmpty, 0.f), bb = make_float4(0.f, 0.f, 0.f, 0.f);
             float wz = 0.f;
             if (q >= 0) {
@@ -263,11 +282,10 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
             const int c = lp.row_local[p];
             const float4 pa = sA[c], pb = sB[c];
             const float4 w = make_float4(pb.z, pb.w, sW[c], 0.f);
-            const float* __restrict__ e = lp.ell + (size_t)K * start + l;
+            // this row's 1/d0 stream: 16 bytes (4 stencil entries) per load
+            const float4* __restrict__ e4 = (const float4*)(lp.ell + (size_t)K * start) + l;
             float ax = 0.f, ay = 0.f, az = 0.f;
-#pragma unroll 4
-            for (int k = 0; k < K; ++k) {
-                const float s = __ldcs(e + (size_t)k * rows);
+            const auto bond = [&](int k, float s) {
                 const int q = c + lp.off[k];
                 const float4 qa = sA[q], qb = sB[q];
                 const float qwz = sW[q];
@@ -283,6 +301,14 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
                 ax = fmaf(a1, wx, fmaf(g, xs, ax));
                 ay = fmaf(a1, wy, fmaf(g, ys, ay));
                 az = fmaf(a1, wz, fmaf(g, zs, az));
+            };
+#pragma unroll 4
+            for (int k4 = 0; k4 < K / 4; ++k4) {
+                const float4 s4 = __ldcs(e4 + (size_t)k4 * rows);
+                bond(4 * k4, s4.x);
+                bond(4 * k4 + 1, s4.y);
+                bond(4 * k4 + 2, s4.z);
+                bond(4 * k4 + 3, s4.w);
             }
             spmv_finish_mixed<1, DOT>(P, S, p, ab, w, ax, ay, az, 0, 0xffffffffu, out, acc);
         }
@@ -403,12 +429,12 @@ cudaError_t lattice_build(int n, double spacing, dbl4* x64, float4* X32, int* pe
             for (int dx = -kLatRmax; dx <= kLatRmax; ++dx) {
                 const int i = ((dz + kLatRmax) * kLatTab + (dy + kLatRmax)) * kLatTab + (dx + kLatRmax);
                 if (!tab[i]) continue;
-                if ((int)sten.size() >= kLatMaxK) return cudaSuccess;
+                if ((int)sten.size() >= kLatMaxK) return cudaSuccess;   // (kLatMaxK is a multiple of 4)
                 offk[i] = (int)sten.size();
                 sten.push_back(make_int3(dx, dy, dz));
                 R = std::max(R, std::max(std::abs(dx), std::max(std::abs(dy), std::abs(dz))));
             }
-    L.K = (int)sten.size();
+    L.K = ((int)sten.size() + 3) / 4 * 4;   // padding entries: offset 0 (the row's own site), 1/d0 = 0
     L.R = R;
     L.bx = kLatBX;
     L.by = kLatBY;
@@ -416,7 +442,8 @@ cudaError_t lattice_build(int n, double spacing, dbl4* x64, float4* X32, int* pe
     L.hx = L.bx + 2 * R;
     L.hy = L.by + 2 * R;
     L.hz = L.bz + 2 * R;
-    for (int k = 0; k < L.K; ++k) L.off[k] = (sten[k].z * L.hy + sten[k].y) * L.hx + sten[k].x;
+    for (int k = 0; k < L.K; ++k)
+        L.off[k] = k < (int)sten.size() ? (sten[k].z * L.hy + sten[k].y) * L.hx + sten[k].x : 0;
     const long long D[3] = {(long long)ext[3] - ext[0] + 1, (long long)ext[4] - ext[1] + 1,
                             (long long)ext[5] - ext[2] + 1};
     const long long NB[3] = {(D[0] + L.bx - 1) / L.bx, (D[1] + L.by - 1) / L.by, (D[2] + L.bz - 1) / L.bz};

@@ -151,7 +151,7 @@ constexpr int kLatRmax = 3;          // largest offset per axis (sites)
 constexpr int kLatTab = 2 * kLatRmax + 1;
 
 struct LatticeParams {
-    int K;                    // stencil entries
+    int K;                    // stencil entries, padded to a multiple of 4 (padding: offset 0, 1/d0 = 0)
     int R;                    // halo width (sites)
     int bx, by, bz;           // brick extent (sites)
     int hx, hy, hz;           // halo extent = brick + 2R
@@ -165,7 +165,8 @@ struct LatticeParams {
     const int4* site;         // n: site coordinates (x, y, z) of each slot, from the map's first site
     const int* map;           // site map: slot or -1
     const int* offk;          // kLatTab^3: stencil entry of an offset, or -1
-    float* ell;               // K per row, brick-major: [K * start_b + k * rows_b + l]
+    float* ell;               // K per row, brick-major, in chunks of 4 entries:
+                              // [K * start_b + (k / 4) * 4 rows_b + 4 l + k % 4]
     int off[kLatMaxK];        // halo index offset of each stencil entry
 };
 
