@@ -46,6 +46,55 @@ constexpr int kLatHaloMax = 38 * 10 * 8;
 constexpr int kLatSmemMax = kLatHaloMax * 36;
 constexpr int kLatHaloPerThread = (kLatHaloMax + kBlock - 1) / kBlock;
 
+// The stencil of a horizon of 2.5 spacings (the benchmark's 5 r): every lattice
+// offset with |v|^2 <= 6 (80 offsets, reach 2 per axis), in (dz, dy, dx)
+// order.  Bodies whose bonds all fall in it use a product specialised for it:
+// bricks of 32 x 4 x 4 sites, a 36 x 8 x 8 halo, and shared-memory offsets
+// known at compile time.
+constexpr int kS80 = 80;
+constexpr int kS80Hx = kLatBX + 4, kS80Hy = kLatBY + 4, kS80Hz = 4 + 4;
+struct Stencil80 {
+    int off[kS80];
+};
+__host__ __device__ constexpr bool in_s80(int dx, int dy, int dz)
+{
+    return (dx || dy || dz) && dx * dx + dy * dy + dz * dz <= 6 && dx >= -2 && dx <= 2 && dy >= -2 && dy <= 2 &&
+           dz >= -2 && dz <= 2;
+}
+__host__ __device__ constexpr Stencil80 make_stencil80()
+{
+    Stencil80 t{};
+    int k = 0;
+    for (int dz = -2; dz <= 2; ++dz)
+        for (int dy = -2; dy <= 2; ++dy)
+            for (int dx = -2; dx <= 2; ++dx)
+                if (in_s80(dx, dy, dz)) t.off[k++] = (dz * kS80Hy + dy) * kS80Hx + dx;
+    return t;
+}
+__host__ __device__ constexpr int count_s80()
+{
+    int k = 0;
+    for (int dz = -2; dz <= 2; ++dz)
+        for (int dy = -2; dy <= 2; ++dy)
+            for (int dx = -2; dx <= 2; ++dx)
+                if (in_s80(dx, dy, dz)) ++k;
+    return k;
+}
+static_assert(count_s80() == kS80, "the |v|^2 <= 6 stencil has 80 offsets");
+
+// L2 prefetch of [p, p + bytes) (16-byte aligned, bytes a multiple of 16) in
+// pieces of at most 16 KB, one per thread of the first threads of the block
+__device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes)
+{
+    constexpr unsigned kPiece = 16384;
+    const unsigned pieces = (bytes + kPiece - 1) / kPiece;
+    if (threadIdx.x < pieces) {
+        const unsigned off = threadIdx.x * kPiece;
+        const unsigned len = bytes - off < kPiece ? bytes - off : kPiece;
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"((const char*)p + off), "r"(len) : "memory");
+    }
+}
+
 int blocks_for(long long n) { return (int)std::max<long long>(1, std::min<long long>((n + kBlock - 1) / kBlock, 8192)); }
 
 // ---- detection ------------------------------------------------------------------------
@@ -215,27 +264,31 @@ __global__ void __launch_bounds__(kBlock) k_lat_ell(DeviceState S, LatticeParams
 // ---- the product -----------------------------------------------------------------------
 // Shared memory per halo site: A = (supercell offset x, y, z, sup * i),
 // B = (sup * j, sup * k, w.x, w.y), W = w.z (36 bytes).
-template <bool DOT>
+// FIXED: the 80-entry stencil with its compile-time halo (lp.K == 80, halo 36 x 8 x 8).
+template <bool DOT, bool FIXED>
 __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, DeviceState S, LatticeParams lp,
                                                            const float4* __restrict__ in, float4* __restrict__ out,
                                                            ReduceSlot slot, CgScalars* cg, double* dot_out)
 {
     if (DOT && cg && ((volatile CgScalars*)cg)->done) return;
     extern __shared__ float4 lat_smem[];
-    const int H = lp.hx * lp.hy * lp.hz;
+    const int H = FIXED ? kS80Hx * kS80Hy * kS80Hz : lp.hx * lp.hy * lp.hz;
     float4* sA = lat_smem;
     float4* sB = sA + H;
     float* sW = (float*)(sB + H);
     const float sup = (float)P.sup;
-    const int hx = lp.hx, hxy = lp.hx * lp.hy;
+    const int hx = FIXED ? kS80Hx : lp.hx, hxy = FIXED ? kS80Hx * kS80Hy : lp.hx * lp.hy;
     const int mx = lp.map_dim[0], mxy = lp.map_dim[0] * lp.map_dim[1];
-    const int K = lp.K;
+    const int K = FIXED ? kS80 : lp.K;
     DotAcc32 acc;
     for (int b = blockIdx.x; b < lp.n_bricks; b += gridDim.x) {
         const int corner = lp.brick_corner[b];
         const int start = lp.brick_start[b];
         const int rows = lp.brick_start[b + 1] - start;
         __syncthreads();   // the previous brick's rows are done with the halo
+        // the brick's 1/d0 block (K * rows floats, contiguous) on its way to
+        // L2 while the halo is staged
+        prefetch_l2(lp.ell + (size_t)K * start, (unsigned)(sizeof(float) * K * rows));
         // the map entries of this thread's halo sites first (independent
         // loads), then their positions and w entries
         int qs[kLatHaloPerThread];
@@ -285,8 +338,9 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
             // this row's 1/d0 stream: 16 bytes (4 stencil entries) per load
             const float4* __restrict__ e4 = (const float4*)(lp.ell + (size_t)K * start) + l;
             float ax = 0.f, ay = 0.f, az = 0.f;
+            constexpr Stencil80 s80 = make_stencil80();
             const auto bond = [&](int k, float s) {
-                const int q = c + lp.off[k];
+                const int q = c + (FIXED ? s80.off[k] : lp.off[k]);
                 const float4 qa = sA[q], qb = sB[q];
                 const float qwz = sW[q];
                 // (X_q - X_p) + sup (ijk_q - ijk_p): the gather product's bond vector
@@ -302,13 +356,24 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
                 ay = fmaf(a1, wy, fmaf(g, ys, ay));
                 az = fmaf(a1, wz, fmaf(g, zs, az));
             };
+            if constexpr (FIXED) {
+#pragma unroll
+                for (int k4 = 0; k4 < kS80 / 4; ++k4) {
+                    const float4 s4 = __ldcs(e4 + (size_t)k4 * rows);
+                    bond(4 * k4, s4.x);
+                    bond(4 * k4 + 1, s4.y);
+                    bond(4 * k4 + 2, s4.z);
+                    bond(4 * k4 + 3, s4.w);
+                }
+            } else {
 #pragma unroll 4
-            for (int k4 = 0; k4 < K / 4; ++k4) {
-                const float4 s4 = __ldcs(e4 + (size_t)k4 * rows);
-                bond(4 * k4, s4.x);
-                bond(4 * k4 + 1, s4.y);
-                bond(4 * k4 + 2, s4.z);
-                bond(4 * k4 + 3, s4.w);
+                for (int k4 = 0; k4 < K / 4; ++k4) {
+                    const float4 s4 = __ldcs(e4 + (size_t)k4 * rows);
+                    bond(4 * k4, s4.x);
+                    bond(4 * k4 + 1, s4.y);
+                    bond(4 * k4 + 2, s4.z);
+                    bond(4 * k4 + 3, s4.w);
+                }
             }
             spmv_finish_mixed<1, DOT>(P, S, p, ab, w, ax, ay, az, 0, 0xffffffffu, out, acc);
         }
@@ -334,10 +399,13 @@ int lattice_spmv_blocks_per_sm(const LatticeParams& lp)
     int a = 0, b = 0;
     // the attribute is per kernel and process: set to the largest halo any
     // handle can need, so that every handle's launch fits
-    cudaFuncSetAttribute(k_spmv_lattice<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kLatSmemMax);
-    cudaFuncSetAttribute(k_spmv_lattice<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kLatSmemMax);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_spmv_lattice<true>, kBlock, smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_spmv_lattice<false>, kBlock, smem);
+    const bool fixed = lp.fixed != 0;
+    const void* kd = fixed ? (const void*)k_spmv_lattice<true, true> : (const void*)k_spmv_lattice<true, false>;
+    const void* kn = fixed ? (const void*)k_spmv_lattice<false, true> : (const void*)k_spmv_lattice<false, false>;
+    cudaFuncSetAttribute(kd, cudaFuncAttributeMaxDynamicSharedMemorySize, kLatSmemMax);
+    cudaFuncSetAttribute(kn, cudaFuncAttributeMaxDynamicSharedMemorySize, kLatSmemMax);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, kd, kBlock, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kn, kBlock, smem);
     const int m = std::min(a, b);
     return m > 0 ? m : 1;
 }
@@ -347,11 +415,15 @@ void launch_spmv_lattice(bool dot, const StepParams& P, const DeviceState& S, co
 {
     const size_t smem = lattice_smem_bytes(lp);
     const int grid = std::max(1, std::min(lp.grid, std::max(lp.n_bricks, 1)));
-    if (dot)
-        k_spmv_lattice<true><<<grid, kBlock, smem, st>>>(P, S, lp, (const float4*)in, (float4*)out, slot, cg, dot_out);
-    else
-        k_spmv_lattice<false><<<grid, kBlock, smem, st>>>(P, S, lp, (const float4*)in, (float4*)out, slot, nullptr,
-                                                           nullptr);
+    const float4* x = (const float4*)in;
+    float4* y = (float4*)out;
+    if (lp.fixed) {
+        if (dot) k_spmv_lattice<true, true><<<grid, kBlock, smem, st>>>(P, S, lp, x, y, slot, cg, dot_out);
+        else k_spmv_lattice<false, true><<<grid, kBlock, smem, st>>>(P, S, lp, x, y, slot, nullptr, nullptr);
+    } else {
+        if (dot) k_spmv_lattice<true, false><<<grid, kBlock, smem, st>>>(P, S, lp, x, y, slot, cg, dot_out);
+        else k_spmv_lattice<false, false><<<grid, kBlock, smem, st>>>(P, S, lp, x, y, slot, nullptr, nullptr);
+    }
 }
 
 void launch_lattice_ell(const DeviceState& S, const LatticeParams& lp, int force, int grid, cudaStream_t st)
@@ -424,18 +496,28 @@ cudaError_t lattice_build(int n, double spacing, dbl4* x64, float4* X32, int* pe
     int R = 1;
     std::vector<int> offk(tab.size(), -1);
     std::vector<int3> sten;
+    // every offset inside the 80-entry stencil: take that stencil whole (absent
+    // offsets get 1/d0 = 0) so that the specialised product applies
+    bool in80 = true;
+    for (int dz = -kLatRmax; dz <= kLatRmax; ++dz)
+        for (int dy = -kLatRmax; dy <= kLatRmax; ++dy)
+            for (int dx = -kLatRmax; dx <= kLatRmax; ++dx)
+                if (tab[((dz + kLatRmax) * kLatTab + (dy + kLatRmax)) * kLatTab + (dx + kLatRmax)] && !in_s80(dx, dy, dz))
+                    in80 = false;
     for (int dz = -kLatRmax; dz <= kLatRmax; ++dz)
         for (int dy = -kLatRmax; dy <= kLatRmax; ++dy)
             for (int dx = -kLatRmax; dx <= kLatRmax; ++dx) {
                 const int i = ((dz + kLatRmax) * kLatTab + (dy + kLatRmax)) * kLatTab + (dx + kLatRmax);
-                if (!tab[i]) continue;
+                if (in80 ? !in_s80(dx, dy, dz) : !tab[i]) continue;
                 if ((int)sten.size() >= kLatMaxK) return cudaSuccess;   // (kLatMaxK is a multiple of 4)
                 offk[i] = (int)sten.size();
                 sten.push_back(make_int3(dx, dy, dz));
                 R = std::max(R, std::max(std::abs(dx), std::max(std::abs(dy), std::abs(dz))));
             }
     L.K = ((int)sten.size() + 3) / 4 * 4;   // padding entries: offset 0 (the row's own site), 1/d0 = 0
+    if (in80) R = 2;
     L.R = R;
+    L.fixed = in80 ? 1 : 0;
     L.bx = kLatBX;
     L.by = kLatBY;
     L.bz = R <= 2 ? 4 : 2;

@@ -157,6 +157,7 @@ struct LatticeParams {
     int hx, hy, hz;           // halo extent = brick + 2R
     int n_bricks;
     int grid;                 // blocks of the product
+    int fixed;                // 1: the 80-entry stencil of a 2.5-spacing horizon (compile-time offsets)
     int map_dim[3];           // site map extent (bricks + R on each side)
     const int* brick_start;   // n_bricks + 1: slot range of each brick
     const int* brick_corner;  // n_bricks: map index of the halo's first site
