@@ -143,6 +143,8 @@ void Engine::free_all()
     lattice_free(&latb_);
     lat_ = LatticeParams{};
     lat_ok_ = false;
+    if (d_p2_) cudaFree(d_p2_);
+    d_p2_ = nullptr;
     L_.lattice = 0;
     L_.lat = nullptr;
     cudaFree(contact_.counts);
@@ -255,6 +257,7 @@ pd_status Engine::make_ready()
                          total_slots_, &lat_, &latb_, &ok, stream_),
            "lattice build");
         lat_ok_ = ok != 0;
+        if (lat_ok_) CK(cudaMalloc(&d_p2_, sizeof(float4) * N), "alloc second direction buffer");
     }
     if (n > 0) {
         CK(cudaMemcpyAsync(S_.X64, S_.x64, sizeof(dbl4) * N, cudaMemcpyDeviceToDevice, stream_), "copy X");
@@ -488,7 +491,8 @@ pd_status Engine::tune_spmv()
 
 void Engine::apply_op(const StepParams& P, const void* in, void* out, ReduceSlot slot, double* dot_out)
 {
-    if (L_.lattice) launch_spmv_lattice(dot_out != nullptr, P, S_, lat_, in, out, slot, nullptr, dot_out, stream_);
+    if (L_.lattice)
+        launch_spmv_lattice(dot_out != nullptr, P, S_, lat_, in, out, slot, nullptr, dot_out, nullptr, nullptr, stream_);
     else launch_operator_u(fp64_, P, S_, L_.lanes, L_.unroll, L_.grid_bonds, in, out, slot, dot_out, stream_);
 }
 
@@ -909,16 +913,34 @@ pd_status Engine::solve(const StepParams& P)
             // event records barely perturb the solve they measure; the mean
             // sampled duration is scaled to the exact launch count
             const bool sample = (launched % kMarkStride) == 0;
-            if (sample) mark_begin(PD_KC_SPMV, launched);
-            launch_spmv(fp64_, true, P, S_, L_, stream_);
-            if (sample) mark_end();
-            if (sample) mark_begin(PD_KC_CG_VECTOR, launched);
-            launch_cg_axpy(fp64_, P, S_, L_, stream_);
-            launch_cg_xpby(fp64_, P, S_, L_, stream_);
-            if (sample) mark_end();
+            if (L_.lattice && d_p2_) {
+                // the direction update p = r + beta p is fused into the
+                // product, which reads the previous direction from one buffer
+                // and writes the new one to the other (buffer 0 = S_.p, set to r
+                // by the residual kernel)
+                void* p_prev = (launched & 1) ? d_p2_ : S_.p;
+                void* p_new = (launched & 1) ? S_.p : d_p2_;
+                if (sample) mark_begin(PD_KC_SPMV, launched);
+                launch_spmv_lattice(true, P, S_, lat_, p_prev, S_.y, ReduceSlot{S_.partials, S_.counters + 1}, S_.sc,
+                                    nullptr, S_.r, p_new, stream_);
+                if (sample) mark_end();
+                DeviceState Sj = S_;
+                Sj.p = p_new;
+                if (sample) mark_begin(PD_KC_CG_VECTOR, launched);
+                launch_cg_axpy(fp64_, P, Sj, L_, stream_);
+                if (sample) mark_end();
+            } else {
+                if (sample) mark_begin(PD_KC_SPMV, launched);
+                launch_spmv(fp64_, true, P, S_, L_, stream_);
+                if (sample) mark_end();
+                if (sample) mark_begin(PD_KC_CG_VECTOR, launched);
+                launch_cg_axpy(fp64_, P, S_, L_, stream_);
+                launch_cg_xpby(fp64_, P, S_, L_, stream_);
+                if (sample) mark_end();
+            }
             ++launched;
         }
-        launches_ += 3LL * batch;
+        launches_ += (L_.lattice && d_p2_ ? 2LL : 3LL) * batch;
         CK(cudaGetLastError(), "cg launch");
         CK(cudaMemcpyAsync(h_sc_, S_.sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, stream_), "read cg scalars");
         CK(cudaStreamSynchronize(stream_), "cg sync");
@@ -945,7 +967,7 @@ pd_status Engine::solve(const StepParams& P)
     }
     if (profiling_) {
         kc_launches_[PD_KC_SPMV] += last_iters_;
-        kc_launches_[PD_KC_CG_VECTOR] += 2LL * last_iters_;
+        kc_launches_[PD_KC_CG_VECTOR] += (L_.lattice && d_p2_ ? 1LL : 2LL) * last_iters_;
     }
     if (!h_sc_->converged) cg_converged_ = false;
     if (ws_features_needed()) return ws_after_cg(P);

@@ -181,6 +181,7 @@ private:
     LatticeParams lat_{};
     LatticeBuffers latb_{};
     bool lat_ok_ = false;
+    void* d_p2_ = nullptr;             // second CG direction buffer of the lattice product's fused update
     bool batch_member_ = false;        // set by Batch: its scenes keep the builder's slot order
     ContactBuffers contact_{};         // PD-PD contact hash (when enabled)
     size_t saved_frame_ = 0;           // DataIO::savedFrame

@@ -83,13 +83,11 @@ __host__ __device__ constexpr int count_s80()
 static_assert(count_s80() == kS80, "the |v|^2 <= 6 stencil has 80 offsets");
 
 // L2 prefetch of [p, p + bytes) (16-byte aligned, bytes a multiple of 16) in
-// pieces of at most 16 KB, one per thread of the first threads of the block
+// pieces of at most 16 KB, all issued by the calling thread
 __device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes)
 {
     constexpr unsigned kPiece = 16384;
-    const unsigned pieces = (bytes + kPiece - 1) / kPiece;
-    if (threadIdx.x < pieces) {
-        const unsigned off = threadIdx.x * kPiece;
+    for (unsigned off = 0; off < bytes; off += kPiece) {
         const unsigned len = bytes - off < kPiece ? bytes - off : kPiece;
         asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"((const char*)p + off), "r"(len) : "memory");
     }
@@ -264,14 +262,27 @@ __global__ void __launch_bounds__(kBlock) k_lat_ell(DeviceState S, LatticeParams
 // ---- the product -----------------------------------------------------------------------
 // Shared memory per halo site: A = (supercell offset x, y, z, sup * i),
 // B = (sup * j, sup * k, w.x, w.y), W = w.z (36 bytes).
-// FIXED: the 80-entry stencil with its compile-time halo (lp.K == 80, halo 36 x 8 x 8).
-template <bool DOT, bool FIXED>
+//
+// Blocks take bricks from a counter (lp.sched[0]) in brick order, so that
+// bricks of uneven fill balance over the blocks; the last block to finish
+// resets the counter for the next launch.  The next brick's 1/d0 block is
+// prefetched to L2 while the current one is computed.
+//
+// FIXED: the 80-entry stencil with its compile-time halo (lp.K == 80, halo
+// 36 x 8 x 8).  FUSE (a CG iteration): the direction is updated on the way
+// in, w = r + beta p_prev for every halo site (beta = 0 on the first
+// iteration, which cg_fin_residual sets), and each brick writes its rows' new
+// direction to p_out (p_prev and p_out are different buffers, so blocks that
+// still stage halos read the old direction).
+template <bool DOT, bool FIXED, bool FUSE>
 __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, DeviceState S, LatticeParams lp,
                                                            const float4* __restrict__ in, float4* __restrict__ out,
-                                                           ReduceSlot slot, CgScalars* cg, double* dot_out)
+                                                           ReduceSlot slot, CgScalars* cg, double* dot_out,
+                                                           const float4* __restrict__ r_in, float4* __restrict__ p_out)
 {
     if (DOT && cg && ((volatile CgScalars*)cg)->done) return;
     extern __shared__ float4 lat_smem[];
+    __shared__ int s_next;
     const int H = FIXED ? kS80Hx * kS80Hy * kS80Hz : lp.hx * lp.hy * lp.hz;
     float4* sA = lat_smem;
     float4* sB = sA + H;
@@ -280,15 +291,21 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
     const int hx = FIXED ? kS80Hx : lp.hx, hxy = FIXED ? kS80Hx * kS80Hy : lp.hx * lp.hy;
     const int mx = lp.map_dim[0], mxy = lp.map_dim[0] * lp.map_dim[1];
     const int K = FIXED ? kS80 : lp.K;
+    const float beta = FUSE ? (float)((volatile CgScalars*)cg)->beta : 0.f;
     DotAcc32 acc;
-    for (int b = blockIdx.x; b < lp.n_bricks; b += gridDim.x) {
+    if (threadIdx.x == 0) {
+        s_next = (int)atomicAdd(&lp.sched[0], 1u);
+        if (s_next < lp.n_bricks) {
+            const int s0 = lp.brick_start[s_next], s1 = lp.brick_start[s_next + 1];
+            prefetch_l2(lp.ell + (size_t)K * s0, (unsigned)(sizeof(float) * K * (s1 - s0)));
+        }
+    }
+    __syncthreads();
+    int b = s_next;
+    while (b < lp.n_bricks) {
         const int corner = lp.brick_corner[b];
         const int start = lp.brick_start[b];
         const int rows = lp.brick_start[b + 1] - start;
-        __syncthreads();   // the previous brick's rows are done with the halo
-        // the brick's 1/d0 block (K * rows floats, contiguous) on its way to
-        // L2 while the halo is staged
-        prefetch_l2(lp.ell + (size_t)K * start, (unsigned)(sizeof(float) * K * rows));
         // the map entries of this thread's halo sites first (independent
         // loads), then their positions and w entries
         int qs[kLatHaloPerThread];
@@ -313,7 +330,13 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
             float wz = 0.f;
             if (q >= 0) {
                 const float4 x = __ldg(S.xs4 + q);
-                const float4 w = __ldg(in + q);
+                float4 w = __ldg(in + q);
+                if (FUSE) {   // xpby_elem: p = r + beta p
+                    const float4 r = __ldg(r_in + q);
+                    w.x = r.x + beta * w.x;
+                    w.y = r.y + beta * w.y;
+                    w.z = r.z + beta * w.z;
+                }
                 const int wq = __float_as_int(x.w);
                 a = make_float4(x.x, x.y, x.z, sup * small_int_to_float(wq & 1023));
                 bb = make_float4(sup * small_int_to_float((wq >> 10) & 1023), sup * small_int_to_float((wq >> 20) & 1023),
@@ -324,17 +347,25 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
             sB[h] = bb;
             sW[h] = wz;
         }
-        __syncthreads();
+        __syncthreads();   // halo staged; every thread has read s_next
+        if (threadIdx.x == 0) {
+            s_next = (int)atomicAdd(&lp.sched[0], 1u);
+            if (s_next < lp.n_bricks) {
+                const int s0 = lp.brick_start[s_next], s1 = lp.brick_start[s_next + 1];
+                prefetch_l2(lp.ell + (size_t)K * s0, (unsigned)(sizeof(float) * K * (s1 - s0)));
+            }
+        }
         for (int l = threadIdx.x; l < rows; l += blockDim.x) {
             const int p = start + l;
             const uint8_t ab = S.act[p];
+            const int c = lp.row_local[p];
+            const float4 pa = sA[c], pb = sB[c];
+            const float4 w = make_float4(pb.z, pb.w, sW[c], 0.f);
+            if (FUSE) p_out[p] = w;
             if (is_dirichlet(ab & kActMask)) {
                 out[p] = make_float4(0.f, 0.f, 0.f, 0.f);
                 continue;
             }
-            const int c = lp.row_local[p];
-            const float4 pa = sA[c], pb = sB[c];
-            const float4 w = make_float4(pb.z, pb.w, sW[c], 0.f);
             // this row's 1/d0 stream: 16 bytes (4 stencil entries) per load
             const float4* __restrict__ e4 = (const float4*)(lp.ell + (size_t)K * start) + l;
             float ax = 0.f, ay = 0.f, az = 0.f;
@@ -377,6 +408,16 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
             }
             spmv_finish_mixed<1, DOT>(P, S, p, ab, w, ax, ay, az, 0, 0xffffffffu, out, acc);
         }
+        __syncthreads();   // the rows are done with the halo; s_next is visible
+        b = s_next;
+    }
+    // every block has taken its last brick index: the last to arrive resets the counter
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&lp.sched[1], 1u) == gridDim.x - 1) {
+            lp.sched[0] = 0u;
+            lp.sched[1] = 0u;
+        }
     }
     if (DOT) {
         block_reduce_finish(acc, slot, [cg, dot_out](double pAp) {
@@ -393,37 +434,55 @@ size_t lattice_smem_bytes(const LatticeParams& lp)
     return (size_t)lp.hx * lp.hy * lp.hz * (2 * sizeof(float4) + sizeof(float));
 }
 
-int lattice_spmv_blocks_per_sm(const LatticeParams& lp)
+template <bool FIXED>
+int lattice_blocks(size_t smem)
 {
-    const size_t smem = lattice_smem_bytes(lp);
-    int a = 0, b = 0;
-    // the attribute is per kernel and process: set to the largest halo any
-    // handle can need, so that every handle's launch fits
-    const bool fixed = lp.fixed != 0;
-    const void* kd = fixed ? (const void*)k_spmv_lattice<true, true> : (const void*)k_spmv_lattice<true, false>;
-    const void* kn = fixed ? (const void*)k_spmv_lattice<false, true> : (const void*)k_spmv_lattice<false, false>;
-    cudaFuncSetAttribute(kd, cudaFuncAttributeMaxDynamicSharedMemorySize, kLatSmemMax);
-    cudaFuncSetAttribute(kn, cudaFuncAttributeMaxDynamicSharedMemorySize, kLatSmemMax);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, kd, kBlock, smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kn, kBlock, smem);
-    const int m = std::min(a, b);
+    const void* ks[3] = {(const void*)k_spmv_lattice<false, FIXED, false>, (const void*)k_spmv_lattice<true, FIXED, false>,
+                         (const void*)k_spmv_lattice<true, FIXED, true>};
+    int m = 1 << 30;
+    for (const void* k : ks) {
+        // the attribute is per kernel and process: set to the largest halo any
+        // handle can need, so that every handle's launch fits
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kLatSmemMax);
+        int a = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k, kBlock, smem);
+        m = std::min(m, a);
+    }
     return m > 0 ? m : 1;
 }
 
+int lattice_spmv_blocks_per_sm(const LatticeParams& lp)
+{
+    const size_t smem = lattice_smem_bytes(lp);
+    return lp.fixed ? lattice_blocks<true>(smem) : lattice_blocks<false>(smem);
+}
+
+template <bool FIXED>
+void launch_lattice_t(bool dot, const StepParams& P, const DeviceState& S, const LatticeParams& lp, const void* in,
+                      void* out, ReduceSlot slot, CgScalars* cg, double* dot_out, const void* r_in, void* p_out,
+                      int grid, size_t smem, cudaStream_t st)
+{
+    const float4* x = (const float4*)in;
+    float4* y = (float4*)out;
+    if (r_in)
+        k_spmv_lattice<true, FIXED, true><<<grid, kBlock, smem, st>>>(P, S, lp, x, y, slot, cg, dot_out,
+                                                                      (const float4*)r_in, (float4*)p_out);
+    else if (dot)
+        k_spmv_lattice<true, FIXED, false><<<grid, kBlock, smem, st>>>(P, S, lp, x, y, slot, cg, dot_out, nullptr,
+                                                                       nullptr);
+    else
+        k_spmv_lattice<false, FIXED, false><<<grid, kBlock, smem, st>>>(P, S, lp, x, y, slot, nullptr, nullptr,
+                                                                        nullptr, nullptr);
+}
+
 void launch_spmv_lattice(bool dot, const StepParams& P, const DeviceState& S, const LatticeParams& lp,
-                         const void* in, void* out, ReduceSlot slot, CgScalars* cg, double* dot_out, cudaStream_t st)
+                         const void* in, void* out, ReduceSlot slot, CgScalars* cg, double* dot_out,
+                         const void* r_in, void* p_out, cudaStream_t st)
 {
     const size_t smem = lattice_smem_bytes(lp);
     const int grid = std::max(1, std::min(lp.grid, std::max(lp.n_bricks, 1)));
-    const float4* x = (const float4*)in;
-    float4* y = (float4*)out;
-    if (lp.fixed) {
-        if (dot) k_spmv_lattice<true, true><<<grid, kBlock, smem, st>>>(P, S, lp, x, y, slot, cg, dot_out);
-        else k_spmv_lattice<false, true><<<grid, kBlock, smem, st>>>(P, S, lp, x, y, slot, nullptr, nullptr);
-    } else {
-        if (dot) k_spmv_lattice<true, false><<<grid, kBlock, smem, st>>>(P, S, lp, x, y, slot, cg, dot_out);
-        else k_spmv_lattice<false, false><<<grid, kBlock, smem, st>>>(P, S, lp, x, y, slot, nullptr, nullptr);
-    }
+    if (lp.fixed) launch_lattice_t<true>(dot, P, S, lp, in, out, slot, cg, dot_out, r_in, p_out, grid, smem, st);
+    else launch_lattice_t<false>(dot, P, S, lp, in, out, slot, cg, dot_out, r_in, p_out, grid, smem, st);
 }
 
 void launch_lattice_ell(const DeviceState& S, const LatticeParams& lp, int force, int grid, cudaStream_t st)
@@ -441,6 +500,7 @@ void lattice_free(LatticeBuffers* lb)
     cudaFree(lb->map);
     cudaFree(lb->offk);
     cudaFree(lb->ell);
+    cudaFree(lb->sched);
     *lb = LatticeBuffers{};
 }
 
@@ -601,6 +661,8 @@ cudaError_t lattice_build(int n, double spacing, dbl4* x64, float4* X32, int* pe
     LT_TRY(cudaMalloc(&t.lb.map, sizeof(int) * (size_t)map_size));
     LT_TRY(cudaMalloc(&t.lb.offk, sizeof(int) * offk.size()));
     LT_TRY(cudaMalloc(&t.lb.ell, sizeof(float) * (size_t)L.K * (size_t)n));
+    LT_TRY(cudaMalloc(&t.lb.sched, sizeof(unsigned) * 2));
+    LT_TRY(cudaMemsetAsync(t.lb.sched, 0, sizeof(unsigned) * 2, st));
     LT_TRY(cudaMemcpyAsync(t.lb.brick_start, bstart.data(), sizeof(int) * bstart.size(), cudaMemcpyHostToDevice, st));
     LT_TRY(cudaMemcpyAsync(t.lb.brick_corner, bcorner.data(), sizeof(int) * bcorner.size(), cudaMemcpyHostToDevice, st));
     LT_TRY(cudaMemcpyAsync(t.lb.row_local, rlocal.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, st));
@@ -618,6 +680,7 @@ cudaError_t lattice_build(int n, double spacing, dbl4* x64, float4* X32, int* pe
     L.map = t.lb.map;
     L.offk = t.lb.offk;
     L.ell = t.lb.ell;
+    L.sched = t.lb.sched;
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

@@ -166,6 +166,7 @@ struct LatticeParams {
     const int4* site;         // n: site coordinates (x, y, z) of each slot, from the map's first site
     const int* map;           // site map: slot or -1
     const int* offk;          // kLatTab^3: stencil entry of an offset, or -1
+    unsigned* sched;          // [0] next brick, [1] blocks finished (zero between launches)
     float* ell;               // K per row, brick-major, in chunks of 4 entries:
                               // [K * start_b + (k / 4) * 4 rows_b + 4 l + k % 4]
     int off[kLatMaxK];        // halo index offset of each stencil entry
@@ -180,6 +181,7 @@ struct LatticeBuffers {       // device allocations owned by the engine
     int* map = nullptr;
     int* offk = nullptr;
     float* ell = nullptr;
+    unsigned* sched = nullptr;
 };
 
 // ---- step kernels (step.cu) --------------------------------------------------
@@ -206,9 +208,12 @@ cudaError_t lattice_build(int n, double spacing, dbl4* x64, float4* X32, int* pe
 // 1/d0 table from the live CSR bonds (force = 0: only when the force pass
 // reported a broken bond, read from S.flags[1] on the device)
 void launch_lattice_ell(const DeviceState& S, const LatticeParams& lp, int force, int grid, cudaStream_t st);
-// y = A(in) by the lattice stencil; dot as launch_operator (cg: CG iteration)
+// y = A(in) by the lattice stencil; dot as launch_operator (cg: CG iteration).
+// r_in set (a CG iteration): the direction p = r_in + beta in is formed on the
+// way in (beta from cg) and written to p_out (a buffer other than in); y = A p.
 void launch_spmv_lattice(bool dot, const StepParams& P, const DeviceState& S, const LatticeParams& lp,
-                         const void* in, void* out, ReduceSlot slot, CgScalars* cg, double* dot_out, cudaStream_t st);
+                         const void* in, void* out, ReduceSlot slot, CgScalars* cg, double* dot_out,
+                         const void* r_in, void* p_out, cudaStream_t st);
 int lattice_spmv_blocks_per_sm(const LatticeParams& lp);
 size_t lattice_smem_bytes(const LatticeParams& lp);
 void lattice_free(LatticeBuffers* lb);

@@ -288,8 +288,8 @@ static void spmv_d(bool fp64, const StepParams& P, const DeviceState& S, int lan
 void launch_spmv(bool fp64, bool dot, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st)
 {
     if (!fp64 && L.lattice && L.lat) {
-        if (dot) launch_spmv_lattice(true, P, S, *L.lat, S.p, S.y, slot_of(S, 1), S.sc, nullptr, st);
-        else launch_spmv_lattice(false, P, S, *L.lat, S.sol, S.y, slot_of(S, 1), nullptr, nullptr, st);
+        if (dot) launch_spmv_lattice(true, P, S, *L.lat, S.p, S.y, slot_of(S, 1), S.sc, nullptr, nullptr, nullptr, st);
+        else launch_spmv_lattice(false, P, S, *L.lat, S.sol, S.y, slot_of(S, 1), nullptr, nullptr, nullptr, nullptr, st);
         return;
     }
     if (!fp64 && L.tiled) {

@@ -802,6 +802,7 @@ __device__ __forceinline__ void cg_fin_init(CgScalars* sc, double bb)
 __device__ __forceinline__ void cg_fin_residual(CgScalars* sc, double rr)
 {
     sc->rz = rr;
+    sc->beta = 0.0;   // p = r: a direction update fused into the next product keeps p as it is
     sc->rnorm = sqrt(rr);
     if (sc->rnorm <= sc->tol) {
         sc->done = 1;
