@@ -28,10 +28,8 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["step.cu", "bonds.cu", "noalloc.cu", "mlp.cu", "mlp_tc.cu", "warmstart.cu", "batch.cu", "tiles.cu", "mesh_fill.cu", "contact.cu", "history.cu", "lattice.cu"]
-# lattice.cu: FP32 denormals flush to zero (its bond terms, CG entries and
-# positions are far above the FP32 denormal range), so rsqrtf needs no
-# denormal path in the per-bond loop
-CU_EXTRA = {"lattice.cu": ["-ftz=true"]}
+# per-file nvcc flags (none at present)
+CU_EXTRA = {}
 CPP_SOURCES = ["engine.cpp", "capi.cpp", "params.cpp", "batch.cpp", "dataio.cpp", "scene.cpp"]
 
 

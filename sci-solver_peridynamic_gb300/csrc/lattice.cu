@@ -82,6 +82,18 @@ __host__ __device__ constexpr int count_s80()
 }
 static_assert(count_s80() == kS80, "the |v|^2 <= 6 stencil has 80 offsets");
 
+// 1/sqrt(x) by the hardware approximation without a denormal path: a live
+// bond's d^2 is far above the FP32 denormal range, and an empty or padding
+// entry (d^2 = 0 -> +inf) is masked to 0 by its caller.  The file is built
+// without flush-to-zero: the CG dot products of small right-hand sides
+// (1e-20 entries, products near 1e-40) must keep their denormal terms.
+__device__ __forceinline__ float rsqrt_ftz(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // L2 prefetch of [p, p + bytes) (16-byte aligned, bytes a multiple of 16) in
 // pieces of at most 16 KB, all issued by the calling thread
 __device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes)
@@ -379,7 +391,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
                 const float ys = (qa.y - pa.y) + (qb.x - pb.x);
                 const float zs = (qa.z - pa.z) + (qb.y - pb.y);
                 const float wx = w.x - qb.z, wy = w.y - qb.w, wz = w.z - qwz;
-                float inv_d = rsqrtf(fmaf(xs, xs, fmaf(ys, ys, zs * zs)));
+                float inv_d = rsqrt_ftz(fmaf(xs, xs, fmaf(ys, ys, zs * zs)));
                 inv_d = s > 0.f ? inv_d : 0.f;   // no live bond: the term vanishes
                 const float a1 = s - inv_d;
                 const float g = fmaf(xs, wx, fmaf(ys, wy, zs * wz)) * (inv_d * inv_d * inv_d);
