@@ -459,6 +459,7 @@ pd_status Engine::dataio_load_state(size_t timestep)
         lattice_free(&latb_);
         lat_ = LatticeParams{};
         lat_ok_ = false;
+        lat_fixed_built_ = false;
         if (d_p2_) cudaFree(d_p2_);
         d_p2_ = nullptr;
         if (L_.lattice) {

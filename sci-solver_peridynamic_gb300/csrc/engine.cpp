@@ -143,6 +143,7 @@ void Engine::free_all()
     lattice_free(&latb_);
     lat_ = LatticeParams{};
     lat_ok_ = false;
+    lat_fixed_built_ = false;
     if (d_p2_) cudaFree(d_p2_);
     d_p2_ = nullptr;
     L_.lattice = 0;
@@ -257,6 +258,7 @@ pd_status Engine::make_ready()
                          total_slots_, &lat_, &latb_, &ok, stream_),
            "lattice build");
         lat_ok_ = ok != 0;
+        lat_fixed_built_ = lat_ok_ && lat_.fixed != 0;
         if (lat_ok_) CK(cudaMalloc(&d_p2_, sizeof(float4) * N), "alloc second direction buffer");
     }
     if (n > 0) {
@@ -420,12 +422,16 @@ pd_status Engine::tune_spmv()
     if (lat_ok_) {
         if (opt_.spmv_path == 3) cand.clear();   // asked for: the only candidate
         cand.push_back({0, 1, 1, 1});
+        // the 80-entry stencil also runs on the general kernel (offsets from
+        // the launch parameters instead of compile-time constants)
+        if (lat_fixed_built_ && n_ >= 20000) cand.push_back({0, 1, 1, 2});
     }
     if (cand.empty()) cand.push_back({0, fixed_lanes ? fixed_lanes : 8, fixed_unroll ? fixed_unroll : 1});
     auto apply = [&](const Cand& c) {
-        L_.lattice = c.lattice;
+        L_.lattice = c.lattice ? 1 : 0;
         L_.lat = c.lattice ? &lat_ : nullptr;
         if (c.lattice) {
+            lat_.fixed = (c.lattice == 1 && lat_fixed_built_) ? 1 : 0;
             L_.tiled = 0;
             L_.lanes = 1;
             L_.unroll = 1;

@@ -181,6 +181,7 @@ private:
     LatticeParams lat_{};
     LatticeBuffers latb_{};
     bool lat_ok_ = false;
+    bool lat_fixed_built_ = false;     // the stencil is the 80-entry one (compile-time kernel available)
     void* d_p2_ = nullptr;             // second CG direction buffer of the lattice product's fused update
     bool batch_member_ = false;        // set by Batch: its scenes keep the builder's slot order
     ContactBuffers contact_{};         // PD-PD contact hash (when enabled)

@@ -94,6 +94,15 @@ __device__ __forceinline__ float rsqrt_ftz(float x)
     return y;
 }
 
+// 16-byte asynchronous global -> shared copy (both addresses 16-byte aligned)
+// and the wait for all of this thread's copies
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // L2 prefetch of [p, p + bytes) (16-byte aligned, bytes a multiple of 16) in
 // pieces of at most 16 KB, all issued by the calling thread
 __device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes)
@@ -319,7 +328,10 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
         const int start = lp.brick_start[b];
         const int rows = lp.brick_start[b + 1] - start;
         // the map entries of this thread's halo sites first (independent
-        // loads), then their positions and w entries
+        // loads); then the neighbours' supercell words and w entries go
+        // straight to shared memory by asynchronous copies (all in flight at
+        // once, no registers held; the fused update's r entries in
+        // registers); last, each thread converts its own sites in place
         int qs[kLatHaloPerThread];
 #pragma unroll
         for (int t = 0; t < kLatHaloPerThread; ++t) {
@@ -333,6 +345,18 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
                 qs[t] = __ldg(lp.map + corner + iz * mxy + iy * mx + ix);
             }
         }
+        float4 rr[FUSE ? kLatHaloPerThread : 1];
+#pragma unroll
+        for (int t = 0; t < kLatHaloPerThread; ++t) {
+            const int h = threadIdx.x + t * kBlock;
+            const int q = qs[t];
+            if (h < H && q >= 0) {
+                cp_async16(&sA[h], S.xs4 + q);
+                cp_async16(&sB[h], in + q);
+                if (FUSE) rr[t] = __ldg(r_in + q);
+            }
+        }
+        cp_async_wait_all();
 #pragma unroll
         for (int t = 0; t < kLatHaloPerThread; ++t) {
             const int h = threadIdx.x + t * kBlock;
@@ -341,13 +365,12 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
             float4 a = make_float4(kLatEmpty, kLatEmpty, kLatEmpty, 0.f), bb = make_float4(0.f, 0.f, 0.f, 0.f);
             float wz = 0.f;
             if (q >= 0) {
-                const float4 x = __ldg(S.xs4 + q);
-                float4 w = __ldg(in + q);
+                const float4 x = sA[h];
+                float4 w = sB[h];
                 if (FUSE) {   // xpby_elem: p = r + beta p
-                    const float4 r = __ldg(r_in + q);
-                    w.x = r.x + beta * w.x;
-                    w.y = r.y + beta * w.y;
-                    w.z = r.z + beta * w.z;
+                    w.x = rr[t].x + beta * w.x;
+                    w.y = rr[t].y + beta * w.y;
+                    w.z = rr[t].z + beta * w.z;
                 }
                 const int wq = __float_as_int(x.w);
                 a = make_float4(x.x, x.y, x.z, sup * small_int_to_float(wq & 1023));
