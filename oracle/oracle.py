@@ -38,15 +38,19 @@ def build_oracle(force: bool = False) -> str:
 
 
 def reference_root() -> str | None:
-    """The reference project's root, from the PD_REFERENCE_ROOT environment
-    variable (there is no default: the tree exists only where fixtures are
-    made)."""
-    return os.environ.get("PD_REFERENCE_ROOT") or None
+    """The reference project's root: the PD_REFERENCE_ROOT environment
+    variable, else a checkout named `reference` beside this repository's
+    directory, else None (the tree exists only where fixtures are made)."""
+    env = os.environ.get("PD_REFERENCE_ROOT")
+    if env:
+        return env
+    beside = os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+    return beside if os.path.isdir(os.path.join(beside, "src", "core")) else None
 
 
 def build_ref(reference_root: str | None = None) -> str | None:
     """Build oracle/_ref/libpdref.so when the reference tree is present
-    (argument, else PD_REFERENCE_ROOT); None when it is not."""
+    (argument, else reference_root()); None when it is not."""
     if reference_root is None:
         reference_root = globals()["reference_root"]()
     if not reference_root or not os.path.isdir(os.path.join(reference_root, "src", "core")):

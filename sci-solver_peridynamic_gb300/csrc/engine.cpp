@@ -472,10 +472,12 @@ pd_status Engine::tune_spmv()
         apply(c);
         launch_spmv(fp64_, true, P, S_, L_, stream_);
         ++launches_;
+        if (cudaGetLastError() != cudaSuccess) continue;   // a shape that cannot launch is not a candidate
         float ms_c = 1e30f;
         for (int rep = 0; rep < 3; ++rep) {
             CK(cudaEventRecord(e0, stream_), "event");
             for (int k = 0; k < 2; ++k) launch_spmv(fp64_, true, P, S_, L_, stream_);
+            CK(cudaGetLastError(), "tune launch");
             CK(cudaEventRecord(e1, stream_), "event");
             CK(cudaEventSynchronize(e1), "tune sync");
             float ms = 0.f;

@@ -488,8 +488,11 @@ int lattice_blocks(size_t smem)
 
 int lattice_spmv_blocks_per_sm(const LatticeParams& lp)
 {
+    // both variants get the shared-memory attribute: the autotuner may run
+    // the general kernel on a stencil the compile-time one also covers
     const size_t smem = lattice_smem_bytes(lp);
-    return lp.fixed ? lattice_blocks<true>(smem) : lattice_blocks<false>(smem);
+    const int general = lattice_blocks<false>(smem);
+    return lp.fixed ? std::min(general, lattice_blocks<true>(smem)) : general;
 }
 
 template <bool FIXED>
