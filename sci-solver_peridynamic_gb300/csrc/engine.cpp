@@ -466,17 +466,26 @@ pd_status Engine::tune_spmv()
     float best = 1e30f;
     Cand best_c = cand[0];
     // each candidate: one warm-up launch, then the best of three timed pairs
-    // of the CG iteration's product (y = A p with <p, y>; the scalars it
-    // writes are reset by the first solve)
+    // of the CG iteration's product as the CG loop launches it (y = A p with
+    // <p, y>; the lattice product with the direction update fused in; the
+    // scalars and the second direction buffer it writes are reset by the
+    // first solve)
+    const auto cg_product = [&]() {
+        if (L_.lattice && d_p2_)
+            launch_spmv_lattice(true, P, S_, lat_, S_.p, S_.y, ReduceSlot{S_.partials, S_.counters + 1}, S_.sc,
+                                nullptr, S_.r, d_p2_, stream_);
+        else
+            launch_spmv(fp64_, true, P, S_, L_, stream_);
+    };
     for (const auto& c : cand) {
         apply(c);
-        launch_spmv(fp64_, true, P, S_, L_, stream_);
+        cg_product();
         ++launches_;
         if (cudaGetLastError() != cudaSuccess) continue;   // a shape that cannot launch is not a candidate
         float ms_c = 1e30f;
         for (int rep = 0; rep < 3; ++rep) {
             CK(cudaEventRecord(e0, stream_), "event");
-            for (int k = 0; k < 2; ++k) launch_spmv(fp64_, true, P, S_, L_, stream_);
+            for (int k = 0; k < 2; ++k) cg_product();
             CK(cudaGetLastError(), "tune launch");
             CK(cudaEventRecord(e1, stream_), "event");
             CK(cudaEventSynchronize(e1), "tune sync");
