@@ -14,7 +14,8 @@
 // w) in shared memory, then each thread walks its row's stencil.  Rows of a
 // warp are x-consecutive sites, so the neighbours at one stencil entry are
 // x-consecutive shared-memory words (no bank conflicts), and the only per-bond
-// stream is 1/d0 per (row, stencil entry), 0 where there is no live bond.
+// stream is 1/d0 per (row, stencil entry), 0 where there is no live bond
+// (stored scaled by 2^100, see kLatScale).
 //
 // The per-bond arithmetic is the gather product's (step_rows.cuh,
 // mixed_bond_chunk): the bond vector is rebuilt from the same supercell words,
@@ -41,6 +42,11 @@ namespace {
 constexpr int kLatBX = 32;
 constexpr int kLatBY = 4;
 constexpr float kLatEmpty = 1.0e4f;   // supercell offset of an empty site (any far, finite position)
+// The table holds 2^100 / d0: then min(1/d, entry) is 1/d for a live bond (its
+// entry is near 1e31 or more) and 0 for "no bond" (entry 0), one instruction,
+// and 1/d0 - 1/d = fma(entry, 2^-100, -1/d) is exact scaling by a power of two.
+constexpr float kLatScale = 1.2676506002282294e30f;     // 2^100
+constexpr float kLatUnscale = 7.888609052210118e-31f;   // 2^-100
 // the largest halo: R = 3, bricks of 32 x 4 x 2 sites -> 38 x 10 x 8 sites of 36 bytes
 constexpr int kLatHaloMax = 38 * 10 * 8;
 constexpr int kLatSmemMax = kLatHaloMax * 36;
@@ -93,15 +99,6 @@ __device__ __forceinline__ float rsqrt_ftz(float x)
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
 }
-
-// 16-byte asynchronous global -> shared copy (both addresses 16-byte aligned)
-// and the wait for all of this thread's copies
-__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src)
-{
-    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gmem_src) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // L2 prefetch of [p, p + bytes) (16-byte aligned, bytes a multiple of 16) in
 // pieces of at most 16 KB, all issued by the calling thread
@@ -275,7 +272,7 @@ __global__ void __launch_bounds__(kBlock) k_lat_ell(DeviceState S, LatticeParams
             const int t = ((sq.z - sp.z + kLatRmax) * kLatTab + (sq.y - sp.y + kLatRmax)) * kLatTab +
                           (sq.x - sp.x + kLatRmax);
             const int k = lp.offk[t];
-            e[((size_t)(k >> 2) * rows + l) * 4 + (k & 3)] = S.inv_d0[rs + j];
+            e[((size_t)(k >> 2) * rows + l) * 4 + (k & 3)] = S.inv_d0[rs + j] * kLatScale;
         }
     }
 }
@@ -328,10 +325,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
         const int start = lp.brick_start[b];
         const int rows = lp.brick_start[b + 1] - start;
         // the map entries of this thread's halo sites first (independent
-        // loads); then the neighbours' supercell words and w entries go
-        // straight to shared memory by asynchronous copies (all in flight at
-        // once, no registers held; the fused update's r entries in
-        // registers); last, each thread converts its own sites in place
+        // loads), then their positions and w entries
         int qs[kLatHaloPerThread];
 #pragma unroll
         for (int t = 0; t < kLatHaloPerThread; ++t) {
@@ -345,18 +339,6 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
                 qs[t] = __ldg(lp.map + corner + iz * mxy + iy * mx + ix);
             }
         }
-        float4 rr[FUSE ? kLatHaloPerThread : 1];
-#pragma unroll
-        for (int t = 0; t < kLatHaloPerThread; ++t) {
-            const int h = threadIdx.x + t * kBlock;
-            const int q = qs[t];
-            if (h < H && q >= 0) {
-                cp_async16(&sA[h], S.xs4 + q);
-                cp_async16(&sB[h], in + q);
-                if (FUSE) rr[t] = __ldg(r_in + q);
-            }
-        }
-        cp_async_wait_all();
 #pragma unroll
         for (int t = 0; t < kLatHaloPerThread; ++t) {
             const int h = threadIdx.x + t * kBlock;
@@ -365,12 +347,13 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
             float4 a = make_float4(kLatEmpty, kLatEmpty, kLatEmpty, 0.f), bb = make_float4(0.f, 0.f, 0.f, 0.f);
             float wz = 0.f;
             if (q >= 0) {
-                const float4 x = sA[h];
-                float4 w = sB[h];
+                const float4 x = __ldg(S.xs4 + q);
+                float4 w = __ldg(in + q);
                 if (FUSE) {   // xpby_elem: p = r + beta p
-                    w.x = rr[t].x + beta * w.x;
-                    w.y = rr[t].y + beta * w.y;
-                    w.z = rr[t].z + beta * w.z;
+                    const float4 r = __ldg(r_in + q);
+                    w.x = r.x + beta * w.x;
+                    w.y = r.y + beta * w.y;
+                    w.z = r.z + beta * w.z;
                 }
                 const int wq = __float_as_int(x.w);
                 a = make_float4(x.x, x.y, x.z, sup * small_int_to_float(wq & 1023));
@@ -415,8 +398,8 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
                 const float zs = (qa.z - pa.z) + (qb.y - pb.y);
                 const float wx = w.x - qb.z, wy = w.y - qb.w, wz = w.z - qwz;
                 float inv_d = rsqrt_ftz(fmaf(xs, xs, fmaf(ys, ys, zs * zs)));
-                inv_d = s > 0.f ? inv_d : 0.f;   // no live bond: the term vanishes
-                const float a1 = s - inv_d;
+                inv_d = fminf(inv_d, s);   // no live bond (s = 0): the term vanishes
+                const float a1 = fmaf(s, kLatUnscale, -inv_d);
                 const float g = fmaf(xs, wx, fmaf(ys, wy, zs * wz)) * (inv_d * inv_d * inv_d);
                 ax = fmaf(a1, wx, fmaf(g, xs, ax));
                 ay = fmaf(a1, wy, fmaf(g, ys, ay));
@@ -546,7 +529,8 @@ cudaError_t lattice_build(int n, double spacing, dbl4* x64, float4* X32, int* pe
                           long long total_slots, LatticeParams* lp, LatticeBuffers* lb, int* ok, cudaStream_t st)
 {
     *ok = 0;
-    if (n < 1 || !(spacing > 0.0) || total_slots >= (1LL << 31) - 64) return cudaSuccess;
+    // (spacings below 1e-6 would take 2^100 / d0 out of the FP32 range)
+    if (n < 1 || !(spacing > 1e-6) || total_slots >= (1LL << 31) - 64) return cudaSuccess;
     // every temporary in one owner, freed on every return path
     struct Tmp {
         int* ext = nullptr;
