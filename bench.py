@@ -76,6 +76,7 @@ def parse_args(argv=None):
     ap.add_argument("--no-plain", action="store_true", help="skip the previous-solution-guess comparison run")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-guess study on the 16^3 cube")
     return ap.parse_args(argv)
 
 
@@ -404,6 +405,11 @@ def run_gb300(args):
                          "includes": "pd_set_particles + pd_make_ready (GPU bond build) once, then per step "
                                      "pd_advance(1) + pd_get(POSITION) to host; wall clock"}
         sim2.close()
+    # the metric's second half: CG iterations per step with the learned guess
+    # against the plain one (16^3 cube, held-out seed)
+    if rank == 0 and world == 1 and not args.no_learned:
+        r = learned_study(local, 3)
+        result["learned_vs_plain"] = r
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = os.cpu_count()
         os.environ.setdefault("OMP_NUM_THREADS", str(cores))
@@ -592,17 +598,21 @@ def run_batched(args):
     print(json.dumps(result), flush=True)
 
 
-def run_learned(args):
-    """Learned vs plain CG warm start on the 16^3 cube: 5 training seeds x
-    100 steps x 100 sampled particles = 50k pairs, BF16 MLP trained on the
-    GPU, then 100 steps of the seed-0 scene with each warm start."""
+LEARNED_GUESSES = {0: "previous solution (the reference's)", 1: "learned correction (network alone, guarded)",
+                   2: "history projection", 3: "history projection + learned column"}
+
+
+def learned_study(local=0, warmup=3, steps_total=100):
+    """Learned vs plain CG initial guesses on the 16^3 cube: 5 training seeds x
+    100 steps x 100 sampled particles = 50k pairs from the plain solver, BF16
+    network trained on the GPU, then the held-out seed-0 scene stepped with
+    each initial guess (0 previous solution, 1 network alone with its guard,
+    2 history projection, 3 history projection with the network's correction
+    as one more column).  Returns a dict (no JSON printing)."""
     import numpy as np
-    import torch
     pkg = importlib.import_module(PKG_NAME)
     scenes = importlib.import_module(PKG_NAME + ".scenes")
     ws = importlib.import_module(PKG_NAME + ".warmstart")
-    local = 0
-    torch.cuda.set_device(local)
     t0 = time.perf_counter()
     X, T = ws.collect(lambda s: scenes.cube_lattice(seed=s), seeds=[1, 2, 3, 4, 5], steps=100, samples_per_step=100)
     t_collect = time.perf_counter() - t0
@@ -610,42 +620,60 @@ def run_learned(args):
     params, loss = ws.train(X, T, iterations=3000)
     t_train = time.perf_counter() - t0
     out = {}
-    for mode in (0, 1):
+    steps = steps_total - warmup
+    for mode in (0, 1, 2, 3):
         sc = scenes.cube_lattice(seed=0)
         sc.opt.warm_start = mode
         sim = scenes.make_simulator(sc, local)
         sim.makeReady()
-        if mode:
+        if mode in (1, 3):
             sim.ws_set_params(params)
-        sim.advance(args.warmup)
+        sim.advance(warmup)
         st0 = sim.stats()
-        steps = 100 - args.warmup
         ms = _timed(sim.stream_handle(), lambda: sim.advance(steps), local)
         st1 = sim.stats()
-        out["learned" if mode else "plain"] = {
+        out[mode] = {
+            "guess": LEARNED_GUESSES[mode],
             "steps_per_s": round(steps / (ms / 1e3), 3),
             "cg_iterations_per_step": round((st1.total_cg_iterations - st0.total_cg_iterations) / steps, 2),
-            "position": sim.get(pkg.VAR_POSITION), "kept": int(st1.ws_guesses_kept),
-            "alive": sim.alive_sets(),
+            "guesses_kept": int(st1.ws_guesses_kept - st0.ws_guesses_kept),
+            "learned_column_used": int(st1.ws_learned_used - st0.ws_learned_used),
+            "position": sim.get(pkg.VAR_POSITION), "alive": sim.alive_sets(),
         }
         sim.close()
-    pl, le = out["plain"], out["learned"]
-    same = all(np.array_equal(a, c) for a, c in zip(pl["alive"], le["alive"]))
-    dpos = float(np.abs(pl["position"] - le["position"])[:, :3].max() / np.abs(pl["position"][:, :3]).max())
+    pl = out[0]
+    res = {"workload": "cube_lattice 16^3 = 4096 particles, implicit Euler dt=1e-4, CG rel 1e-6, steps %d..%d of "
+                       "held-out seed 0" % (warmup + 1, steps_total),
+           "training_pairs": int(X.shape[0]), "train_iterations": 3000, "final_loss": float(loss),
+           "collect_s": round(t_collect, 2), "train_s": round(t_train, 2), "guesses": {}}
+    for mode, r in out.items():
+        same = all(np.array_equal(a, c) for a, c in zip(pl["alive"], r["alive"]))
+        dpos = float(np.abs(pl["position"] - r["position"])[:, :3].max() / np.abs(pl["position"][:, :3]).max())
+        res["guesses"][str(mode)] = {k: r[k] for k in ("guess", "steps_per_s", "cg_iterations_per_step",
+                                                        "guesses_kept", "learned_column_used")}
+        res["guesses"][str(mode)].update({
+            "cg_iterations_vs_plain": round(pl["cg_iterations_per_step"] / max(r["cg_iterations_per_step"], 1e-9), 4),
+            "steps_per_s_vs_plain": round(r["steps_per_s"] / pl["steps_per_s"], 4),
+            "same_broken_bond_set_as_plain": bool(same), "max_position_difference_rel": dpos})
+    best = max(res["guesses"].values(), key=lambda g: g["cg_iterations_vs_plain"])
+    res["target_1p5x_steps_per_s_met"] = bool(max(g["steps_per_s_vs_plain"] for g in res["guesses"].values()) >= 1.5)
+    res["best_cg_iterations_vs_plain"] = best["cg_iterations_vs_plain"]
+    return res
+
+
+def run_learned(args):
+    """The learned-guess study as its own JSON line (bench.py --workload learned)."""
+    import torch
+    torch.cuda.set_device(0)
+    r = learned_study(0, args.warmup)
+    g = r["guesses"]
     result = {
         "metric": "CG iterations per step, learned vs plain warm start (rel. residual 1e-6)",
-        "value": round(pl["cg_iterations_per_step"] / max(le["cg_iterations_per_step"], 1e-9), 4),
-        "unit": "plain/learned iterations ratio", "higher_is_better": True, "n_gpus": 1,
-        "steps": 100 - args.warmup, "warmup": args.warmup, "dtype": "bf16 MLP (f32 accumulate), f32/f64 CG",
+        "value": g["3"]["cg_iterations_vs_plain"], "unit": "plain/learned iterations ratio (history projection + "
+        "learned column)", "higher_is_better": True, "n_gpus": 1, "steps": 100 - args.warmup, "warmup": args.warmup,
+        "dtype": "bf16 MLP (f32 accumulate), f32/f64 CG",
         "data": "synthetic (16^3 jittered cube, training seeds 1-5, evaluation seed 0)",
-        "config": {"workload": "cube_lattice 16^3 = 4096 particles, implicit Euler dt=1e-4, CG rel 1e-6, 100 steps",
-                   "training_pairs": int(X.shape[0]), "train_iterations": 3000, "final_loss": float(loss),
-                   "collect_s": round(t_collect, 2), "train_s": round(t_train, 2)},
-        "plain": {k: pl[k] for k in ("steps_per_s", "cg_iterations_per_step")},
-        "learned": {k: le[k] for k in ("steps_per_s", "cg_iterations_per_step", "kept")},
-        "steps_per_s_ratio": round(le["steps_per_s"] / pl["steps_per_s"], 4),
-        "same_broken_bond_set": bool(same),
-        "max_position_difference_rel": dpos,
+        "config": {k: v for k, v in r.items() if k != "guesses"}, "guesses": g,
     }
     print(json.dumps(result), flush=True)
 

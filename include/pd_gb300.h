@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define PD_GB300_ABI_VERSION 3
+#define PD_GB300_ABI_VERSION 4
 
 typedef enum pd_status {
     PD_OK = 0,
@@ -129,12 +129,16 @@ typedef struct pd_solver_options {
     int lanes_per_particle;        /* 4, 8, 16 or 32 lanes cooperate on one bond row of the SpMV */
     int cg_check_interval;         /* CG iterations launched between convergence read-backs */
     int spmv_unroll;               /* 1, 2 or 4 bonds loaded per lane before computing */
-    /* CG initial guess (no reference counterpart for 1 and 2): 0 = the
+    /* CG initial guess (no reference counterpart for 1, 2 and 3): 0 = the
      * previous solution, as the reference (simulator.cu:745-770); 1 = previous
      * solution plus the learned correction of pd_ws_set_params' network (mixed
      * precision only); 2 = previous solution plus its Galerkin correction in
      * the span of the last history_size solutions (history projection, either
-     * precision).  The CG still runs to the same tolerance. */
+     * precision); 3 = as 2 with the network's predicted correction as one more
+     * column of the projection (mixed precision; history_size <= 7): the
+     * Galerkin solve weights it only as far as it lowers the A-norm error, so
+     * the guess is never worse than 2's.  The CG still runs to the same
+     * tolerance. */
     int warm_start;
     /* mixed-precision SpMV path: 2 = per-bond gathers from global memory;
      * 1 = shared-memory tiles of 256 consecutive rows and their halos
@@ -200,6 +204,7 @@ typedef struct pd_step_stats {
     long long ws_guesses_kept;     /* steps whose learned guess beat the previous solution, or
                                       (warm_start 2) whose history projection was applied */
     double last_ws_residual_ratio; /* ||r(guess)|| / ||r(previous solution)|| of the last step */
+    long long ws_learned_used;     /* warm_start 3: projections that gave the network's column a nonzero weight */
 } pd_step_stats;
 
 /* Device time per kernel class, accumulated with CUDA events on the handle's

@@ -106,6 +106,7 @@ class StepStats(C.Structure):
         ("retries_last_step", C.c_int), ("bonds_initial", C.c_longlong), ("bonds_alive", C.c_longlong),
         ("max_bonds_per_particle", C.c_int), ("clock_scale", C.c_double), ("sim_time", C.c_double),
         ("ws_guesses_kept", C.c_longlong), ("last_ws_residual_ratio", C.c_double),
+        ("ws_learned_used", C.c_longlong),
     ]
 
     def as_dict(self):

@@ -69,8 +69,9 @@ pd_status pd_create(const pd_sim_params* sim, const pd_run_params* run, const pd
         g_create_error = "time step must be positive";
         return PD_ERR_INVALID_ARGUMENT;
     }
-    if (o.warm_start < 0 || o.warm_start > 2 || o.history_size < 0 || o.history_size > pdgb::kHistMax) {
-        g_create_error = "warm_start 0..2, history_size 0..8";
+    if (o.warm_start < 0 || o.warm_start > 3 || o.history_size < 0 || o.history_size > pdgb::kHistMax ||
+        (o.warm_start == 3 && o.history_size > pdgb::kHistMax - 1)) {
+        g_create_error = "warm_start 0..3, history_size 0..8 (0..7 with warm_start 3)";
         return PD_ERR_INVALID_ARGUMENT;
     }
     if (o.contact_enabled && !(o.contact_distance > 0 && o.contact_volume > 0)) {

@@ -360,7 +360,7 @@ pd_status Engine::make_ready()
     }
     s = tune_spmv();
     if (s != PD_OK) return s;
-    if (opt_.warm_start == 2) {
+    if (opt_.warm_start == 2 || opt_.warm_start == 3) {
         s = hist_prepare();
         if (s != PD_OK) return s;
     }
@@ -570,7 +570,10 @@ StepParams Engine::step_params() const
 }
 
 // ---- learned warm start --------------------------------------------------------------
-bool Engine::ws_features_needed() const { return !fp64_ && ready_ && (opt_.warm_start == 1 || ws_samples_ > 0); }
+bool Engine::ws_features_needed() const
+{
+    return !fp64_ && ready_ && (opt_.warm_start == 1 || opt_.warm_start == 3 || ws_samples_ > 0);
+}
 
 void Engine::ws_free()
 {
@@ -655,6 +658,13 @@ pd_status Engine::ws_before_cg(const StepParams& P)
     launch_ws_jacobi(P, S_, W_, 8, L_.grid_force, s0, s1, s2, stream_);
     launch_ws_features(P, S_, W_, L_.grid_force, stream_);
     launches_ += 2;
+    if (opt_.warm_start == 3 && d_hnet_) {
+        // the network's correction becomes the last column of the history
+        // projection (hist_project runs next and decides its weight)
+        CK(mlp_infer_tc(mlp_, W_.features, n_, mlp_work_.y, stream_), "network launch");
+        launch_ws_column(P, S_, W_, mlp_work_.y, (float4*)d_hnet_, L_.grid_vec, stream_);
+        launches_ += 2;
+    }
     if (opt_.warm_start == 1) {
         CK(cudaMemcpyAsync(ws_rsave_, S_.r, sizeof(float4) * N, cudaMemcpyDeviceToDevice, stream_), "save r");
         launch_ws_save_plain(S_, stream_);
@@ -671,7 +681,7 @@ pd_status Engine::ws_before_cg(const StepParams& P)
 
 pd_status Engine::ws_after_cg(const StepParams& P)
 {
-    if (opt_.warm_start == 1 && mlp_tc_take_error()) {
+    if ((opt_.warm_start == 1 || opt_.warm_start == 3) && mlp_tc_take_error()) {
         err_ = "warm-start network: a tensor-core wait ran out of time";
         return PD_ERR_CUDA;
     }
@@ -913,13 +923,19 @@ pd_status Engine::solve(const StepParams& P)
     launch_spmv(fp64_, false, P, S_, L_, stream_);
     launch_cg_residual(fp64_, P, S_, L_, stream_);
     launches_ += 3;
-    if (opt_.warm_start == 2) {
-        pd_status s = hist_project(P);
-        if (s != PD_OK) return s;
-    }
-    if (ws_features_needed()) {
+    if (opt_.warm_start == 3) {   // network column first, then the projection over history + column
         pd_status s = ws_before_cg(P);
+        if (s == PD_OK) s = hist_project(P);
         if (s != PD_OK) return s;
+    } else {
+        if (opt_.warm_start == 2) {
+            pd_status s = hist_project(P);
+            if (s != PD_OK) return s;
+        }
+        if (ws_features_needed()) {
+            pd_status s = ws_before_cg(P);
+            if (s != PD_OK) return s;
+        }
     }
     const int check = opt_.cg_check_interval > 0 ? opt_.cg_check_interval : 8;
     int batch = predicted_iters_ > 0 ? predicted_iters_ : check;
@@ -974,7 +990,7 @@ pd_status Engine::solve(const StepParams& P)
     total_iters_ += last_iters_;
     predicted_iters_ = std::max(1, last_iters_);
     flush_marks(last_iters_);
-    if (opt_.warm_start == 2) {
+    if (opt_.warm_start == 2 || opt_.warm_start == 3) {
         if (hist_pending_ratio_) {   // the projected residual's scalars arrived with the loop's syncs
             last_ws_ratio_ = hist_rz1_ > 0.0 ? std::sqrt(h_sc_hist_->rz / hist_rz1_) : 0.0;
             hist_pending_ratio_ = false;
@@ -999,12 +1015,19 @@ pd_status Engine::solve(const StepParams& P)
 pd_status Engine::hist_prepare()
 {
     hist_free();
-    hist_cap_ = opt_.history_size > 0 ? std::min(opt_.history_size, kHistMax) : kHistMax;
+    // warm_start 3 keeps one column of the Gram passes for the network's correction
+    const bool net = opt_.warm_start == 3;
+    const int cap_max = net ? kHistMax - 1 : kHistMax;
+    hist_cap_ = opt_.history_size > 0 ? std::min(opt_.history_size, cap_max) : cap_max;
     const size_t vec = (size_t)std::max(n_, 1) * (fp64_ ? sizeof(dbl4) : sizeof(float4));
     hist_blocks_ = (int)std::max<long long>(1, std::min<long long>(((long long)n_ + kBlock - 1) / kBlock,
                                                                   2LL * sm_count_));
     CK(cudaMalloc(&d_hist_, vec * hist_cap_), "alloc history");
-    CK(cudaMalloc(&d_ahist_, vec * hist_cap_), "alloc history products");
+    CK(cudaMalloc(&d_ahist_, vec * (hist_cap_ + (net ? 1 : 0))), "alloc history products");
+    if (net) {
+        CK(cudaMalloc(&d_hnet_, vec), "alloc learned column");
+        CK(cudaMemsetAsync(d_hnet_, 0, vec, stream_), "memset learned column");
+    }
     CK(cudaMalloc((void**)&d_hpart_, sizeof(double) * (size_t)hist_blocks_ * hist_dots_count(0)),
        "alloc history partials");
     CK(cudaMalloc((void**)&d_hdots_, sizeof(double) * 128), "alloc history dots");
@@ -1018,6 +1041,8 @@ void Engine::hist_free()
 {
     if (d_hist_) cudaFree(d_hist_);
     if (d_ahist_) cudaFree(d_ahist_);
+    if (d_hnet_) cudaFree(d_hnet_);
+    d_hnet_ = nullptr;
     if (d_hpart_) cudaFree(d_hpart_);
     if (d_hdots_) cudaFree(d_hdots_);
     if (h_hdots_) cudaFreeHost(h_hdots_);
@@ -1037,12 +1062,15 @@ void* Engine::hist_vec(int j) const
 
 pd_status Engine::hist_project(const StepParams& P)
 {
-    const int m = hist_m_;
+    // columns: the last hist_m_ accepted solutions, then (warm_start 3) the
+    // network's correction of this step
+    const bool net = opt_.warm_start == 3 && d_hnet_;
+    const int m = hist_m_ + (net ? 1 : 0);
     if (m == 0 || n_ == 0 || !d_hist_) return PD_OK;
     const size_t vec = (size_t)n_ * (fp64_ ? sizeof(dbl4) : sizeof(float4));
     HistPtrs H{}, W{};
     for (int j = 0; j < m; ++j) {
-        H.v[j] = hist_vec(j);
+        H.v[j] = (net && j == m - 1) ? d_hnet_ : hist_vec(j);
         W.v[j] = (const char*)d_ahist_ + vec * (size_t)j;
     }
     mark_begin(PD_KC_GUESS, -1);
@@ -1064,6 +1092,7 @@ pd_status Engine::hist_project(const StepParams& P)
     // (measured on a 100k-particle impact: 1e-14 .. 1e-10 within 1 % of iterations; 1e-6 loses the gain)
     const double rel = fp64_ ? 1e-26 : 1e-12;
     const int used = hist_solve(m, h_hdots_, h_hdots_ + na, h_hdots_ + hist_dots_count(1), rel, Y.y);
+    if (net && Y.y[m - 1] != 0.0) ++ws_net_used_;
     if (used > 0 && !h_sc_->done) {
         hist_rz1_ = h_sc_->rz;
         launch_hist_apply(fp64_, n_, m, H, Y, S_.sol, L_.grid_vec, stream_);
@@ -1342,6 +1371,7 @@ pd_status Engine::stats(pd_step_stats* s) const
     s->bonds_alive = bonds_initial_;
     s->ws_guesses_kept = ws_kept_;
     s->last_ws_residual_ratio = last_ws_ratio_;
+    s->ws_learned_used = ws_net_used_;
     if (ready_ && n_ > 0) {
         std::vector<int> c((size_t)n_);
         cudaSetDevice(device_);

@@ -148,6 +148,8 @@ private:
     int hist_cap_ = 0, hist_m_ = 0, hist_next_ = 0, hist_blocks_ = 0;
     void* d_hist_ = nullptr;      // hist_cap_ vectors of n entries: accepted solutions, Dirichlet rows 0
     void* d_ahist_ = nullptr;     // their products with this step's operator
+    void* d_hnet_ = nullptr;      // warm_start 3: the network's correction (the projection's last column)
+    long long ws_net_used_ = 0;   // warm_start 3: projections that gave the network's column a weight
     double* d_hpart_ = nullptr;   // per-block partial sums of a Gram pass
     double* d_hdots_ = nullptr;   // S (36), c (8), G (36)
     double* h_hdots_ = nullptr;   // pinned copy

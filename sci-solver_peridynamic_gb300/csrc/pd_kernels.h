@@ -393,6 +393,8 @@ void launch_ws_jacobi(const StepParams& P, const DeviceState& S, const WsState& 
 void launch_ws_features(const StepParams& P, const DeviceState& S, const WsState& W, int grid, cudaStream_t st);
 void launch_ws_apply(const StepParams& P, const DeviceState& S, const WsState& W, const float* Y, int grid,
                      cudaStream_t st);
+void launch_ws_column(const StepParams& P, const DeviceState& S, const WsState& W, const float* Y, float4* h,
+                      int grid, cudaStream_t st);
 void launch_ws_collect(const StepParams& P, const DeviceState& S, const WsState& W, int count, int stride, int offset,
                        long long pos, long long cap, cudaStream_t st);
 void launch_count_free(const uint8_t* act, int n, int* out, cudaStream_t st);

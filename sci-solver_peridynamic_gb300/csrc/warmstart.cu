@@ -11,6 +11,8 @@
 //                  differences, velocity, stretch statistics, stiffness ratio,
 //                  contact/boundary flags;
 //   k_ws_apply     x0 = x1 + sigma_o * MLP(features) on free rows;
+//   k_ws_column    h = sigma_o * MLP(features) (0 on Dirichlet rows), the
+//                  learned column of the history projection;
 //   k_ws_collect   (features, (x_new - x1) / sigma_o) rows into a dataset.
 #include <cuda_bf16.h>
 
@@ -68,6 +70,20 @@ __global__ void k_ws_apply(StepParams P, DeviceState S, WsState W, const float* 
         ws_apply_elem(S, Y, p, so);
 }
 
+// the network's correction as a vector: h = sigma_o * y on free rows, 0 on
+// Dirichlet rows (a column of the history projection, warm_start = 3)
+__global__ void k_ws_column(StepParams P, DeviceState S, WsState W, const float* __restrict__ Y,
+                            float4* __restrict__ h)
+{
+    const WsScalars* sc = W.sc;
+    const float so = safe_scale(sc->sum_x2, sc->n_free) + safe_scale(sc->sum_r2, sc->n_free);
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P.n; p += gridDim.x * blockDim.x) {
+        const float* y = Y + (size_t)p * kMlpOutPad;
+        h[p] = is_dirichlet(S.act[p] & kActMask) ? make_float4(0.f, 0.f, 0.f, 0.f)
+                                                  : make_float4(so * y[0], so * y[1], so * y[2], 0.f);
+    }
+}
+
 // dataset rows: features of particle p and (x_new - x1) / sigma_o
 __global__ void k_ws_collect(StepParams P, DeviceState S, WsState W, int count, int stride, int offset,
                              long long pos, long long cap)
@@ -116,6 +132,11 @@ void launch_ws_apply(const StepParams& P, const DeviceState& S, const WsState& W
     k_ws_apply<<<grid, kBlock, 0, st>>>(P, S, W, Y);
 }
 
+void launch_ws_column(const StepParams& P, const DeviceState& S, const WsState& W, const float* Y, float4* h,
+                      int grid, cudaStream_t st)
+{
+    k_ws_column<<<grid, kBlock, 0, st>>>(P, S, W, Y, h);
+}
 void launch_ws_collect(const StepParams& P, const DeviceState& S, const WsState& W, int count, int stride, int offset,
                        long long pos, long long cap, cudaStream_t st)
 {

@@ -32,7 +32,7 @@ def test_library_exports_every_declared_symbol(pdgb):
 
 
 def test_abi_version(pdgb):
-    assert pdgb.library().pd_abi_version() == 3
+    assert pdgb.library().pd_abi_version() == 4
 
 
 def test_params_file_and_derivation(pdgb, tmp_path):
@@ -142,7 +142,7 @@ def test_invalid_spmv_options_rejected(pdgb, scenes, field, value):
     assert "SpMV options" in str(e.value)
 
 
-@pytest.mark.parametrize("field,value", [("warm_start", 3), ("warm_start", -1), ("history_size", 9)])
+@pytest.mark.parametrize("field,value", [("warm_start", 4), ("warm_start", -1), ("history_size", 9)])
 def test_invalid_warm_start_rejected(pdgb, scenes, field, value):
     sc = scenes.reference_block(n_side=3)
     setattr(sc.opt, field, value)
