@@ -407,8 +407,27 @@ pd_status pd_dataio_saved_frame(pd_handle* h, size_t* frame);
 /* DataIO::saveState (dataIO.cu:150-175) */
 pd_status pd_dataio_save_state(pd_handle* h, size_t timestep);
 /* DataIO::loadState (dataIO.cu:178-203): into a handle made ready on the same
- * scene (same particles and bonds); the run then continues bit for bit. */
+ * scene (same particles and bonds); the run then continues bit for bit.
+ * Without DATA/STATE/state.<step> it reads the reference's own
+ * STATE/state.<step> (pd_dataio_load_state_reference). */
 pd_status pd_dataio_load_state(pd_handle* h, size_t timestep);
+/* DataIO::saveState (dataIO.cu:123-150) in the reference's own layout, to
+ * STATE/state.<step> under saving_path: savedFrame, then every MemoryManager
+ * array (memory_manager.h:29-90) in enum order with the sizes of
+ * memory_manager.cu:16-178 for the counts of DATA/sim_info.dat (written
+ * first): positions times scaleFactor, bond lists bond-major
+ * (list[j * num_pd_particle + p], live bonds first) with their tops and backup
+ * tops; arrays this library does not keep (SPH, cells) are zeros, and the
+ * system matrix is a hole of its length (the reference rebuilds it every
+ * step). */
+pd_status pd_dataio_save_state_reference(pd_handle* h, size_t timestep);
+/* DataIO::loadState (dataIO.cu:152-198) of a file in the reference's layout,
+ * sized by DATA/sim_info.dat of the same run, into a handle made ready on the
+ * same scene (original positions and activity are checked): positions,
+ * velocities and their backups, stretch limits, bond lists and tops, the CG
+ * solution and savedFrame; pd_time_step and clockScale from sim_info.dat; the
+ * step counter becomes `timestep` (the reference keeps it out of the file). */
+pd_status pd_dataio_load_state_reference(pd_handle* h, size_t timestep);
 
 /* ---- example scene: an OBJ mesh filled with particles (src/examples/scene.cpp) */
 typedef struct pd_scene pd_scene;

@@ -117,6 +117,10 @@ def _load():
         lib.pdo_get_bond_count.argtypes = [C.c_void_p, ip]
         lib.pdo_get_row_ptr.argtypes = [C.c_void_p, P(C.c_long)]
         lib.pdo_get_bond_list.argtypes = [C.c_void_p, ip]
+        for name in ("pdo_get_position_backup", "pdo_get_velocity_backup"):
+            getattr(lib, name).argtypes = [C.c_void_p, dp]
+        lib.pdo_get_top_backup.argtypes = [C.c_void_p, ip]
+        lib.pdo_get_top.argtypes = [C.c_void_p, ip]
         _lib = lib
     return _lib
 
@@ -238,6 +242,20 @@ class OracleSim:
         return out
 
     position = property(lambda self: self._vec4("pdo_get_position"))
+    position_backup = property(lambda self: self._vec4("pdo_get_position_backup"))
+    velocity_backup = property(lambda self: self._vec4("pdo_get_velocity_backup"))
+
+    @property
+    def bond_top(self):
+        out = np.zeros(self.n, np.int32)
+        self.lib.pdo_get_top(self.h, _ip(out))
+        return out
+
+    @property
+    def bond_top_backup(self):
+        out = np.zeros(self.n, np.int32)
+        self.lib.pdo_get_top_backup(self.h, _ip(out))
+        return out
     velocity = property(lambda self: self._vec4("pdo_get_velocity"))
     force = property(lambda self: self._vec4("pdo_get_force"))
     solution = property(lambda self: self._vec4("pdo_get_solution"))

@@ -678,4 +678,10 @@ void pdo_get_row_ptr(const pdo_state* s, long* o) { memcpy(o, s->row_ptr, ((size
 void pdo_get_bond_list(const pdo_state* s, int* o) { if (s->total_bonds) memcpy(o, s->col, (size_t)s->total_bonds * sizeof(int)); }
 
 /* Diagonal 3x3 blocks of the assembled system matrix (row-major, 9 per particle). */
+/* the adaptive scheme's backups (the reference's PD_POSITION_BACKUP,
+ * PD_VELOCITY_BACKUP, PD_BOND_LIST_TOP_BACKUP), the step counters */
+void pdo_get_position_backup(const pdo_state* s, double* o) { memcpy(o, s->pos_bk, 4 * (size_t)s->n * sizeof(double)); }
+void pdo_get_velocity_backup(const pdo_state* s, double* o) { memcpy(o, s->vel_bk, 4 * (size_t)s->n * sizeof(double)); }
+void pdo_get_top_backup(const pdo_state* s, int* o) { memcpy(o, s->top_bk, (size_t)s->n * sizeof(int)); }
+void pdo_get_top(const pdo_state* s, int* o) { memcpy(o, s->top, (size_t)s->n * sizeof(int)); }
 void pdo_get_diag_blocks(const pdo_state* s, double* out) { memcpy(out, s->diag, 9 * (size_t)s->n * sizeof(double)); }

@@ -122,6 +122,10 @@ void pdo_get_bond_list(const pdo_state* s, int* out);      /* rows in current (s
 int  pdo_force_pass(pdo_state* s, int* has_broken);      /* force/break/Jacobian at current state */
 void pdo_apply_A(pdo_state* s, const double* x4, double* y4);  /* y = A x, current assembled A */
 void pdo_get_diag_blocks(const pdo_state* s, double* out9);     /* diagonal blocks of A, 9 per particle */
+void pdo_get_position_backup(const pdo_state* s, double* out4);  /* adaptive scheme's backups */
+void pdo_get_velocity_backup(const pdo_state* s, double* out4);
+void pdo_get_top_backup(const pdo_state* s, int* out);
+void pdo_get_top(const pdo_state* s, int* out);                   /* pd_bond_list_top: live bonds - 1 */
 void pdo_assemble(pdo_state* s);                           /* fill A and b after a force pass */
 
 /* glibc-compatible rand() stream used for s0 (exposed to pin the product's copy). */

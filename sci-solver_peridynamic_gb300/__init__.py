@@ -209,6 +209,8 @@ def library(build_if_missing: bool = True):
         "pd_dataio_saved_frame": (st, [vp, P(C.c_size_t)]),
         "pd_dataio_save_state": (st, [vp, C.c_size_t]),
         "pd_dataio_load_state": (st, [vp, C.c_size_t]),
+        "pd_dataio_save_state_reference": (st, [vp, C.c_size_t]),
+        "pd_dataio_load_state_reference": (st, [vp, C.c_size_t]),
         "pd_scene_create": (st, [P(SimulationParameters), P(RunningParameters), C.c_int, C.c_uint, P(vp)]),
         "pd_scene_particle_count": (st, [vp, P(C.c_int)]),
         "pd_scene_init_pd_particles": (st, [vp, P(C.c_int32), P(C.c_double), P(C.c_double)]),
@@ -532,6 +534,14 @@ class Simulator:
 
     def dataIO_saveState(self, timestep: int):
         _check(self.lib.pd_dataio_save_state(self.h, int(timestep)), self.h)
+
+    def dataIO_saveStateReference(self, timestep: int):
+        """saveState in the reference's own layout (STATE/state.<step>)."""
+        _check(self.lib.pd_dataio_save_state_reference(self.h, C.c_size_t(timestep)), self.h)
+
+    def dataIO_loadStateReference(self, timestep: int):
+        """loadState of a file in the reference's own layout (STATE/state.<step>)."""
+        _check(self.lib.pd_dataio_load_state_reference(self.h, C.c_size_t(timestep)), self.h)
 
     def dataIO_loadState(self, timestep: int):
         _check(self.lib.pd_dataio_load_state(self.h, int(timestep)), self.h)

@@ -54,6 +54,10 @@ public:
     size_t dataio_saved_frame() const { return saved_frame_; }
     pd_status dataio_save_state(size_t timestep);
     pd_status dataio_load_state(size_t timestep);
+    // the reference's own checkpoint layout (STATE/state.<step>, dataIO.cu:123-198)
+    pd_status dataio_save_state_reference(size_t timestep);
+    pd_status dataio_load_state_reference(size_t timestep);
+    std::string ref_state_path(size_t timestep) const;
 
 private:
     pd_status dataio_write_sim_info();

@@ -230,3 +230,27 @@ def test_struct_mirrors_match_the_c_layout(pdgb):
     assert lib.pd_params_default(C.cast(sbuf, C.POINTER(sim_cls)), C.cast(rbuf, C.POINTER(run_cls))) == 0
     assert bytes(sbuf[C.sizeof(sim_cls):]) == bytes([0xA5] * tail)
     assert bytes(rbuf[C.sizeof(run_cls):]) == bytes([0xA5] * tail)
+
+
+def test_reference_state_layout_restatement(tmp_path):
+    """The restated reference checkpoint layout (tests/golden/ref_state.py):
+    every MemoryManager variable has a size, the PD-only sizes follow
+    memory_manager.cu (528 bond slots, 72-byte Mat3x3 blocks), and a file
+    written with it reads back."""
+    import numpy as np
+    from golden import ref_state
+    n, cells = 10, 7
+    sz = ref_state.sizes(0, n, cells, 0, 0)
+    assert len(sz) == len(ref_state.VARIABLES) == 42
+    assert sz["PD_BOND_LIST"] == 4 * 528 * n and sz["PD_SYSTEM_MATRIX"] == 72 * 528 * n
+    assert sz["SPH_BOUNDARY_POSITION"] == 32 * 8 and sz["PD_CELL_END_INDEX"] == 4 * cells
+    rng = np.random.default_rng(1)
+    pos = np.zeros((n, 4))
+    pos[:, :3] = rng.standard_normal((n, 3))
+    top = np.arange(n, dtype=np.int32)
+    path = tmp_path / "state.1"
+    total = ref_state.write(path, (0, n, cells, 0, 0), 2.5, 7, {"PD_POSITION": pos, "PD_BOND_LIST_TOP": top})
+    d = ref_state.read(path, (0, n, cells, 0, 0), 2.5)
+    assert d["file_size"] == total and d["savedFrame"] == 7
+    np.testing.assert_allclose(d["PD_POSITION"], pos, rtol=1e-15)
+    np.testing.assert_array_equal(d["PD_BOND_LIST_TOP"], top)
