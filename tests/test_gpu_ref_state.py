@@ -44,11 +44,11 @@ def test_reference_layout_holds_the_handles_arrays(pdgb, scenes, tmp_path, preci
     sc = _scene(pdgb, scenes, tmp_path, precision)
     sim = scenes.make_simulator(sc)
     sim.makeReady()
-    sim.advance(25)
+    sim.advance(45)                 # bonds break from step ~40
     sim.dataIO_newFrame()
-    sim.dataIO_saveStateReference(25)
+    sim.dataIO_saveStateReference(45)
     info = _sim_info(tmp_path)
-    path = os.path.join(tmp_path, "STATE", "state.25")
+    path = os.path.join(tmp_path, "STATE", "state.45")
     d = ref_state.read(path, _counts(info), info.scaleFactor)
     assert d["file_size"] == d["expected_size"] and d["savedFrame"] == 1
     n = sc.n
@@ -73,23 +73,23 @@ def test_reference_layout_holds_the_handles_arrays(pdgb, scenes, tmp_path, preci
 
 @pytest.mark.parametrize("precision", [1, 0])
 def test_reference_layout_round_trip(pdgb, scenes, tmp_path, precision):
-    """Save at step 25 in the reference layout, load into a fresh handle
+    """Save at step 45 in the reference layout, load into a fresh handle
     (through pd_dataio_load_state, which falls back to the reference layout),
     continue 20 steps: the uninterrupted run's bond sets and time steps; the
     bond rows come back in the file's order, so positions agree to the
     summation order (FP64 1e-9, mixed as the parity tests)."""
     ref = scenes.make_simulator(_scene(pdgb, scenes, tmp_path, precision))
     ref.makeReady()
-    ref.advance(45)
+    ref.advance(65)
     a = scenes.make_simulator(_scene(pdgb, scenes, tmp_path, precision))
     a.makeReady()
-    a.advance(25)
-    a.dataIO_saveStateReference(25)
+    a.advance(45)
+    a.dataIO_saveStateReference(45)
     a.close()
     b = scenes.make_simulator(_scene(pdgb, scenes, tmp_path, precision))
     b.makeReady()
-    b.dataIO_loadState(25)          # no DATA/STATE/state.25: the reference layout is read
-    assert b.get_current_step() == 25
+    b.dataIO_loadState(45)          # no DATA/STATE/state.45: the reference layout is read
+    assert b.get_current_step() == 45
     b.advance(20)
     assert same_sets(b.alive_sets(), ref.alive_sets())
     assert b.stats().time_step_ticks == ref.stats().time_step_ticks
@@ -100,13 +100,19 @@ def test_reference_layout_round_trip(pdgb, scenes, tmp_path, precision):
 
 @pytest.mark.parametrize("precision", [1, 0])
 def test_oracle_state_in_reference_layout_continues(pdgb, scenes, tmp_path, precision):
-    """The oracle runs 15 steps of a breaking implicit-Euler block; its state
-    is written in the reference's layout (with the run's sim_info.dat); a
-    fresh handle loads it and both continue 15 steps in step."""
-    sc = _scene(pdgb, scenes, tmp_path, precision, integrator=pdgb.IMPLICIT_EULER, adaptive=0)
-    sc.vel[:, 0] *= 2.0   # a faster expansion: bonds break within the run
+    """The oracle runs the breaking Newmark block past step 40 (bonds broken,
+    time step halved), stopping where the adaptive scheme's sub-step count is 0
+    (the reference keeps that count out of its file, and the loader starts it
+    at 0); its state is written in the reference's layout with the run's
+    sim_info.dat; a fresh handle loads it and both continue 15 steps in step."""
+    sc = _scene(pdgb, scenes, tmp_path, precision)
     ora = make_oracle(sc)
-    ora.advance(15)
+    ora.advance(40)
+    k = 40
+    while ora.lib.pdo_substep(ora.h) != 0 and k < 60:
+        ora.advance(1)
+        k += 1
+    assert ora.lib.pdo_substep(ora.h) == 0
     sim = scenes.make_simulator(sc)
     sim.makeReady()
     sim.dataIO_getDataAndWrite()    # DATA/sim_info.dat of this scene
@@ -116,6 +122,7 @@ def test_oracle_state_in_reference_layout_continues(pdgb, scenes, tmp_path, prec
     open(os.path.join(tmp_path, "DATA", "sim_info.dat"), "wb").write(bytes(info))
     n = sc.n
     rp, col, top = ora.row_ptr, ora.bond_list, ora.bond_top
+    assert int((top + 1).sum()) < int(np.diff(rp).sum())   # bonds are broken at the saved step
     bl = np.zeros((ref_state.MAX_BONDS, n), np.int32)
     for p in range(n):
         row = col[rp[p]:rp[p + 1]]
@@ -131,16 +138,15 @@ def test_oracle_state_in_reference_layout_continues(pdgb, scenes, tmp_path, prec
         "PD_SYSTEM_SOLUTION": ora.solution,
     }
     os.makedirs(os.path.join(tmp_path, "STATE"), exist_ok=True)
-    ref_state.write(os.path.join(tmp_path, "STATE", "state.15"), _counts(info), info.scaleFactor, 3, arrays)
-    sim.dataIO_loadStateReference(15)
-    assert sim.get_current_step() == 15 and sim.dataIO_savedFrame() == 3
+    ref_state.write(os.path.join(tmp_path, "STATE", "state.%d" % k), _counts(info), info.scaleFactor, 3, arrays)
+    sim.dataIO_loadStateReference(k)
+    assert sim.get_current_step() == k and sim.dataIO_savedFrame() == 3
     assert same_sets(sim.alive_sets(), ora.alive_sets())
     for _ in range(3):
         sim.advance(5)
         ora.advance(5)
         assert same_sets(sim.alive_sets(), ora.alive_sets())
         assert sim.stats().time_step_ticks == ora.dt_ticks
-    assert sim.stats().bonds_alive < sim.stats().bonds_initial
     assert_positions(sim.get(pdgb.VAR_POSITION), ora.position, sc.pos, precision, "oracle state, reference layout")
 
 
