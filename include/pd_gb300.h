@@ -426,7 +426,10 @@ pd_status pd_dataio_save_state_reference(pd_handle* h, size_t timestep);
  * same scene (original positions and activity are checked): positions,
  * velocities and their backups, stretch limits, bond lists and tops, the CG
  * solution and savedFrame; pd_time_step and clockScale from sim_info.dat; the
- * step counter becomes `timestep` (the reference keeps it out of the file). */
+ * step counter becomes `timestep` and the adaptive scheme's sub-step count 0
+ * (the reference keeps both out of the file, in Simulator members): a state
+ * saved while the halved time step was still in its sub-steps continues with
+ * a fresh count. */
 pd_status pd_dataio_load_state_reference(pd_handle* h, size_t timestep);
 
 /* ---- example scene: an OBJ mesh filled with particles (src/examples/scene.cpp) */

@@ -73,23 +73,29 @@ def test_reference_layout_holds_the_handles_arrays(pdgb, scenes, tmp_path, preci
 
 @pytest.mark.parametrize("precision", [1, 0])
 def test_reference_layout_round_trip(pdgb, scenes, tmp_path, precision):
-    """Save at step 45 in the reference layout, load into a fresh handle
-    (through pd_dataio_load_state, which falls back to the reference layout),
-    continue 20 steps: the uninterrupted run's bond sets and time steps; the
-    bond rows come back in the file's order, so positions agree to the
-    summation order (FP64 1e-9, mixed as the parity tests)."""
-    ref = scenes.make_simulator(_scene(pdgb, scenes, tmp_path, precision))
-    ref.makeReady()
-    ref.advance(65)
+    """Save past step 45 in the reference layout, where the adaptive
+    scheme's sub-step count is 0 (the reference's file does not hold it),
+    load into a fresh handle (through pd_dataio_load_state, which falls back
+    to the reference layout), continue 20 steps: the uninterrupted run's bond
+    sets and time steps; the bond rows come back in the file's order, so
+    positions agree to the summation order (FP64 1e-9, mixed as the parity
+    tests)."""
     a = scenes.make_simulator(_scene(pdgb, scenes, tmp_path, precision))
     a.makeReady()
     a.advance(45)
-    a.dataIO_saveStateReference(45)
+    while a.stats().substep != 0 and a.get_current_step() < 80:
+        a.advance(1)
+    k = a.get_current_step()
+    assert a.stats().substep == 0
+    a.dataIO_saveStateReference(k)
     a.close()
+    ref = scenes.make_simulator(_scene(pdgb, scenes, tmp_path, precision))
+    ref.makeReady()
+    ref.advance(k + 20)
     b = scenes.make_simulator(_scene(pdgb, scenes, tmp_path, precision))
     b.makeReady()
-    b.dataIO_loadState(45)          # no DATA/STATE/state.45: the reference layout is read
-    assert b.get_current_step() == 45
+    b.dataIO_loadState(k)           # no DATA/STATE/state.<k>: the reference layout is read
+    assert b.get_current_step() == k
     b.advance(20)
     assert same_sets(b.alive_sets(), ref.alive_sets())
     assert b.stats().time_step_ticks == ref.stats().time_step_ticks
