@@ -59,10 +59,23 @@ constexpr int kLatHaloPerThread = (kLatHaloMax + kBlock - 1) / kBlock;
 // known at compile time.
 constexpr int kS80 = 80;
 constexpr int kS80Hx = kLatBX + 4, kS80Hy = kLatBY + 4, kS80Hz = 4 + 4;
+struct Stencil80 {
+    int off[kS80];
+};
 __host__ __device__ constexpr bool in_s80(int dx, int dy, int dz)
 {
     return (dx || dy || dz) && dx * dx + dy * dy + dz * dz <= 6 && dx >= -2 && dx <= 2 && dy >= -2 && dy <= 2 &&
            dz >= -2 && dz <= 2;
+}
+__host__ __device__ constexpr Stencil80 make_stencil80()
+{
+    Stencil80 t{};
+    int k = 0;
+    for (int dz = -2; dz <= 2; ++dz)
+        for (int dy = -2; dy <= 2; ++dy)
+            for (int dx = -2; dx <= 2; ++dx)
+                if (in_s80(dx, dy, dz)) t.off[k++] = (dz * kS80Hy + dy) * kS80Hx + dx;
+    return t;
 }
 __host__ __device__ constexpr int count_s80()
 {
@@ -74,37 +87,6 @@ __host__ __device__ constexpr int count_s80()
     return k;
 }
 static_assert(count_s80() == kS80, "the |v|^2 <= 6 stencil has 80 offsets");
-
-// The compile-time product walks the stencil slab by slab in dz: the slabs
-// dz = -2 and +2 share one in-plane pattern (dx^2 + dy^2 <= 2, 9 offsets),
-// dz = -1 and +1 another (<= 5, 21), dz = 0 its own (<= 6 without the origin,
-// 20), so a loop over the two mirrored slabs runs 50 bond bodies instead of 80
-// (a smaller loop body for the instruction cache).  In the 1/d0 table each
-// slab is padded to whole chunks of 4 entries: slabs of 12, 24, 20, 24, 12
-// entries starting at chunks 0, 3, 9, 14, 20 (92 entries in all; padding
-// entries hold 0).
-constexpr int kSlabK = 92;
-// first chunk of 4 table entries of each slab, dz = -2 .. 2
-constexpr int kSlabChunkM2 = 0, kSlabChunkM1 = 3, kSlabChunk0 = 9, kSlabChunkP1 = 14, kSlabChunkP2 = 20;
-struct InPlane {
-    int off[21];
-    int n;
-};
-__host__ __device__ constexpr InPlane make_plane(int r2max, bool skip_origin)
-{
-    InPlane t{};
-    t.n = 0;
-    for (int dy = -2; dy <= 2; ++dy)
-        for (int dx = -2; dx <= 2; ++dx)
-            if (dx * dx + dy * dy <= r2max && !(skip_origin && dx == 0 && dy == 0)) t.off[t.n++] = dy * kS80Hx + dx;
-    return t;
-}
-static_assert(make_plane(2, false).n == 9 && make_plane(5, false).n == 21 && make_plane(6, true).n == 20,
-              "slab sizes of the 80-entry stencil");
-__device__ __forceinline__ float lane_of(const float4& v, int i)
-{
-    return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
-}
 
 // 1/sqrt(x) by the hardware approximation without a denormal path: a live
 // bond's d^2 is far above the FP32 denormal range, and an empty or padding
@@ -304,8 +286,8 @@ __global__ void __launch_bounds__(kBlock) k_lat_ell(DeviceState S, LatticeParams
 // resets the counter for the next launch.  The next brick's 1/d0 block is
 // prefetched to L2 while the current one is computed.
 //
-// FIXED: the 80-entry stencil with its compile-time halo (lp.K == 92 in the
-// slab layout above, halo 36 x 8 x 8).  FUSE (a CG iteration): the direction is updated on the way
+// FIXED: the 80-entry stencil with its compile-time halo (lp.K == 80, halo
+// 36 x 8 x 8).  FUSE (a CG iteration): the direction is updated on the way
 // in, w = r + beta p_prev for every halo site (beta = 0 on the first
 // iteration, which cg_fin_residual sets), and each brick writes its rows' new
 // direction to p_out (p_prev and p_out are different buffers, so blocks that
@@ -326,7 +308,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
     const float sup = (float)P.sup;
     const int hx = FIXED ? kS80Hx : lp.hx, hxy = FIXED ? kS80Hx * kS80Hy : lp.hx * lp.hy;
     const int mx = lp.map_dim[0], mxy = lp.map_dim[0] * lp.map_dim[1];
-    const int K = FIXED ? kSlabK : lp.K;
+    const int K = FIXED ? kS80 : lp.K;
     const float beta = FUSE ? (float)((volatile CgScalars*)cg)->beta : 0.f;
     DotAcc32 acc;
     if (threadIdx.x == 0) {
@@ -405,8 +387,9 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
             // this row's 1/d0 stream: 16 bytes (4 stencil entries) per load
             const float4* __restrict__ e4 = (const float4*)(lp.ell + (size_t)K * start) + l;
             float ax = 0.f, ay = 0.f, az = 0.f;
-            // q: the neighbour's halo index, s: its table entry (2^100 / d0, or 0)
-            const auto bond = [&](int q, float s) {
+            constexpr Stencil80 s80 = make_stencil80();
+            const auto bond = [&](int k, float s) {
+                const int q = c + (FIXED ? s80.off[k] : lp.off[k]);
                 const float4 qa = sA[q], qb = sB[q];
                 const float qwz = sW[q];
                 // (X_q - X_p) + sup (ijk_q - ijk_p): the gather product's bond vector
@@ -423,32 +406,22 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
                 az = fmaf(a1, wz, fmaf(g, zs, az));
             };
             if constexpr (FIXED) {
-                constexpr int kPlaneStep = kS80Hx * kS80Hy;
-                // one slab: its in-plane pattern at dz, table chunks from `chunk`
-                const auto slab = [&](const InPlane& pl, int dz, int chunk) {
-                    const int cz = c + dz * kPlaneStep;
-                    float4 s4[6];
 #pragma unroll
-                    for (int u = 0; u < 6; ++u)
-                        if (4 * u < pl.n) s4[u] = __ldcs(e4 + (size_t)(chunk + u) * rows);
-#pragma unroll
-                    for (int j = 0; j < 21; ++j)
-                        if (j < pl.n) bond(cz + pl.off[j], lane_of(s4[j >> 2], j & 3));
-                };
-                constexpr InPlane p9 = make_plane(2, false), p21 = make_plane(5, false), p20 = make_plane(6, true);
-#pragma unroll 1
-                for (int t = 0; t < 2; ++t) slab(p9, t ? 2 : -2, t ? kSlabChunkP2 : kSlabChunkM2);
-#pragma unroll 1
-                for (int t = 0; t < 2; ++t) slab(p21, t ? 1 : -1, t ? kSlabChunkP1 : kSlabChunkM1);
-                slab(p20, 0, kSlabChunk0);
+                for (int k4 = 0; k4 < kS80 / 4; ++k4) {
+                    const float4 s4 = __ldcs(e4 + (size_t)k4 * rows);
+                    bond(4 * k4, s4.x);
+                    bond(4 * k4 + 1, s4.y);
+                    bond(4 * k4 + 2, s4.z);
+                    bond(4 * k4 + 3, s4.w);
+                }
             } else {
 #pragma unroll 4
                 for (int k4 = 0; k4 < K / 4; ++k4) {
                     const float4 s4 = __ldcs(e4 + (size_t)k4 * rows);
-                    bond(c + lp.off[4 * k4], s4.x);
-                    bond(c + lp.off[4 * k4 + 1], s4.y);
-                    bond(c + lp.off[4 * k4 + 2], s4.z);
-                    bond(c + lp.off[4 * k4 + 3], s4.w);
+                    bond(4 * k4, s4.x);
+                    bond(4 * k4 + 1, s4.y);
+                    bond(4 * k4 + 2, s4.z);
+                    bond(4 * k4 + 3, s4.w);
                 }
             }
             spmv_finish_mixed<1, DOT>(P, S, p, ab, w, ax, ay, az, 0, 0xffffffffu, out, acc);
@@ -613,9 +586,7 @@ cudaError_t lattice_build(int n, double spacing, dbl4* x64, float4* X32, int* pe
             for (int dx = -kLatRmax; dx <= kLatRmax; ++dx)
                 if (tab[((dz + kLatRmax) * kLatTab + (dy + kLatRmax)) * kLatTab + (dx + kLatRmax)] && !in_s80(dx, dy, dz))
                     in80 = false;
-    // padding entries: offset 0 (the row's own site), 1/d0 = 0 (no bond maps to them)
-    const int3 kPad = make_int3(0, 0, 0);
-    for (int dz = -kLatRmax; dz <= kLatRmax; ++dz) {
+    for (int dz = -kLatRmax; dz <= kLatRmax; ++dz)
         for (int dy = -kLatRmax; dy <= kLatRmax; ++dy)
             for (int dx = -kLatRmax; dx <= kLatRmax; ++dx) {
                 const int i = ((dz + kLatRmax) * kLatTab + (dy + kLatRmax)) * kLatTab + (dx + kLatRmax);
@@ -625,13 +596,7 @@ cudaError_t lattice_build(int n, double spacing, dbl4* x64, float4* X32, int* pe
                 sten.push_back(make_int3(dx, dy, dz));
                 R = std::max(R, std::max(std::abs(dx), std::max(std::abs(dy), std::abs(dz))));
             }
-        // the compile-time product's slab layout: each dz slab in whole chunks of 4
-        if (in80 && dz >= -2 && dz <= 2)
-            while (sten.size() % 4) sten.push_back(kPad);
-    }
-    if (in80 && (int)sten.size() != kSlabK) return cudaSuccess;   // (cannot happen: 80 offsets in 5 slabs)
-    while (sten.size() % 4) sten.push_back(kPad);
-    L.K = (int)sten.size();
+    L.K = ((int)sten.size() + 3) / 4 * 4;   // padding entries: offset 0 (the row's own site), 1/d0 = 0
     if (in80) R = 2;
     L.R = R;
     L.fixed = in80 ? 1 : 0;
@@ -641,7 +606,8 @@ cudaError_t lattice_build(int n, double spacing, dbl4* x64, float4* X32, int* pe
     L.hx = L.bx + 2 * R;
     L.hy = L.by + 2 * R;
     L.hz = L.bz + 2 * R;
-    for (int k = 0; k < L.K; ++k) L.off[k] = (sten[k].z * L.hy + sten[k].y) * L.hx + sten[k].x;
+    for (int k = 0; k < L.K; ++k)
+        L.off[k] = k < (int)sten.size() ? (sten[k].z * L.hy + sten[k].y) * L.hx + sten[k].x : 0;
     const long long D[3] = {(long long)ext[3] - ext[0] + 1, (long long)ext[4] - ext[1] + 1,
                             (long long)ext[5] - ext[2] + 1};
     const long long NB[3] = {(D[0] + L.bx - 1) / L.bx, (D[1] + L.by - 1) / L.by, (D[2] + L.bz - 1) / L.bz};
