@@ -432,7 +432,6 @@ pd_status Engine::tune_spmv()
         L_.lat = c.lattice ? &lat_ : nullptr;
         if (c.lattice) {
             lat_.fixed = (c.lattice == 1 && lat_fixed_built_) ? 1 : 0;
-            lat_.grid = std::max(1, std::min(lat_.n_bricks, lattice_spmv_blocks_per_sm(lat_) * sm_count_));
             L_.tiled = 0;
             L_.lanes = 1;
             L_.unroll = 1;

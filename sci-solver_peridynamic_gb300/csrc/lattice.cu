@@ -55,10 +55,10 @@ constexpr int kLatHaloPerThread = (kLatHaloMax + kBlock - 1) / kBlock;
 // The stencil of a horizon of 2.5 spacings (the benchmark's 5 r): every lattice
 // offset with |v|^2 <= 6 (80 offsets, reach 2 per axis), in (dz, dy, dx)
 // order.  Bodies whose bonds all fall in it use a product specialised for it:
-// bricks of 32 x 4 x 2 sites, a 36 x 8 x 6 halo (62 KB: three blocks per SM),
-// and shared-memory offsets known at compile time.
+// bricks of 32 x 4 x 4 sites, a 36 x 8 x 8 halo, and shared-memory offsets
+// known at compile time.
 constexpr int kS80 = 80;
-constexpr int kS80Hx = kLatBX + 4, kS80Hy = kLatBY + 4;
+constexpr int kS80Hx = kLatBX + 4, kS80Hy = kLatBY + 4, kS80Hz = 4 + 4;
 struct Stencil80 {
     int off[kS80];
 };
@@ -293,7 +293,7 @@ __global__ void __launch_bounds__(kBlock) k_lat_ell(DeviceState S, LatticeParams
 // direction to p_out (p_prev and p_out are different buffers, so blocks that
 // still stage halos read the old direction).
 template <bool DOT, bool FIXED, bool FUSE>
-__global__ void __launch_bounds__(kBlock, FIXED ? 3 : 2) k_spmv_lattice(StepParams P, DeviceState S, LatticeParams lp,
+__global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, DeviceState S, LatticeParams lp,
                                                            const float4* __restrict__ in, float4* __restrict__ out,
                                                            ReduceSlot slot, CgScalars* cg, double* dot_out,
                                                            const float4* __restrict__ r_in, float4* __restrict__ p_out)
@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(kBlock, FIXED ? 3 : 2) k_spmv_lattice(StepPara
     if (DOT && cg && ((volatile CgScalars*)cg)->done) return;
     extern __shared__ float4 lat_smem[];
     __shared__ int s_next;
-    const int H = lp.hx * lp.hy * lp.hz;
+    const int H = FIXED ? kS80Hx * kS80Hy * kS80Hz : lp.hx * lp.hy * lp.hz;
     float4* sA = lat_smem;
     float4* sB = sA + H;
     float* sW = (float*)(sB + H);
@@ -474,10 +474,8 @@ int lattice_spmv_blocks_per_sm(const LatticeParams& lp)
     // both variants get the shared-memory attribute: the autotuner may run
     // the general kernel on a stencil the compile-time one also covers
     const size_t smem = lattice_smem_bytes(lp);
-    // both variants get the attribute; the blocks are the variant's in use
     const int general = lattice_blocks<false>(smem);
-    const int fixed = lattice_blocks<true>(smem);
-    return lp.fixed ? fixed : general;
+    return lp.fixed ? std::min(general, lattice_blocks<true>(smem)) : general;
 }
 
 template <bool FIXED>
@@ -604,7 +602,7 @@ cudaError_t lattice_build(int n, double spacing, dbl4* x64, float4* X32, int* pe
     L.fixed = in80 ? 1 : 0;
     L.bx = kLatBX;
     L.by = kLatBY;
-    L.bz = (R <= 2 && !in80) ? 4 : 2;
+    L.bz = R <= 2 ? 4 : 2;
     L.hx = L.bx + 2 * R;
     L.hy = L.by + 2 * R;
     L.hz = L.bz + 2 * R;
