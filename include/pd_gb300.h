@@ -149,7 +149,8 @@ typedef struct pd_solver_options {
      * brick and the product walks each row's stencil of lattice offsets over
      * the brick's halo staged in shared memory (other bodies fall back to
      * 2); 0 = automatic: from 20000 particles, 3 when the body is a lattice
-     * fill, timed against the lanes x unroll shapes of 2 at make_ready.
+     * fill, timed against the lanes x unroll shapes of 2 at make_ready (from
+     * 250000 particles a lattice body takes 3 without timing the others).
      * pd_get_options reports the path in use (1, 2 or 3). */
     int spmv_path;
     /* PD-PD contact (collectPDParticles / collidePDParticles,

@@ -420,7 +420,11 @@ pd_status Engine::tune_spmv()
         }
     }
     if (lat_ok_) {
-        if (opt_.spmv_path == 3) cand.clear();   // asked for: the only candidate
+        // asked for, or a large lattice body (from 250k particles the stencil
+        // product measured well ahead of every gather shape: 186 against
+        // 253 us per product at 1M), where timing the gather shapes and their
+        // bond reorderings would cost make_ready ~45 ms: the stencil only
+        if (opt_.spmv_path == 3 || n_ >= kLatticeOnlyRows) cand.clear();
         cand.push_back({0, 1, 1, 1});
         // the 80-entry stencil also runs on the general kernel (offsets from
         // the launch parameters instead of compile-time constants)

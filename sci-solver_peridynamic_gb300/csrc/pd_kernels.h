@@ -147,6 +147,7 @@ struct DeviceState {
 // marks "no live bond" (no particle there, beyond the horizon, or broken).
 constexpr int kLatMaxK = 160;        // stencil entries at most
 constexpr int kLatticeMinRows = 20000;   // automatic choice: smaller bodies keep the gather product
+constexpr int kLatticeOnlyRows = 250000; // automatic choice: larger lattice bodies time only the stencil variants
 constexpr int kLatRmax = 3;          // largest offset per axis (sites)
 constexpr int kLatTab = 2 * kLatRmax + 1;
 
