@@ -73,6 +73,8 @@ def parse_args(argv=None):
                     help="ellipsoid: CG initial guess, 0 previous solution (the reference's), 2 history projection "
                          "(default; the same steps with guess 0 are timed too and reported as plain_guess)")
     ap.add_argument("--history", type=int, default=0, help="warm start 2: solutions kept (0 = 8)")
+    ap.add_argument("--cg-loop", type=int, default=0, choices=(0, 1),
+                    help="CG loop: 0 = CUDA graph with a device-side while node, 1 = host-checked batches")
     ap.add_argument("--no-plain", action="store_true", help="skip the previous-solution-guess comparison run")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -264,6 +266,7 @@ def run_gb300(args):
     sc.opt.spmv_path = args.spmv_path
     sc.opt.warm_start = args.warm_start
     sc.opt.history_size = args.history
+    sc.opt.cg_loop = args.cg_loop
     sim = scenes.make_simulator(sc, device=local)
     sim.makeReady()
     sim.advance(args.warmup)
@@ -332,8 +335,15 @@ def run_gb300(args):
                                  "history projection: previous solution + Galerkin correction in the span of "
                                  "the last %d solutions" % (sim.params()[2].history_size or 8)),
             "spmv_variant": spmv_variant(sim.params()[2], args),
+            "cg_loop": ("CUDA graph per solve: a while node repeats %d iterations until the device-side test "
+                        "stops it" % (sc.opt.cg_check_interval or 4) if args.cg_loop == 0 else
+                        "host-launched batches, a read-back of the test after each"),
+            "cg_graph_solves": int(st1.cg_graph_solves - st0.cg_graph_solves),
+            "host_syncs_per_step": round((st1.host_syncs - st0.host_syncs) / args.steps, 2),
             "parallelism": "replicas x%d" % world,
-            "l2": "inputs larger than L2 (bond columns + 1/d0 %.0f MB + particle state > 129 MB L2)" % (8 * bonds / 1e6),
+            "l2": ("inputs larger than L2 (1/d0 stencil table %.0f MB + particle state > 129 MB L2)" % (320 * n / 1e6)
+                   if sim.params()[2].spmv_path == 3 else
+                   "inputs larger than L2 (bond columns + 1/d0 %.0f MB + particle state > 129 MB L2)" % (8 * bonds / 1e6)),
         },
         "gpu_launches": int(launches),
         "kernel_time_share": shares,
@@ -355,7 +365,7 @@ def run_gb300(args):
     # the same steps with the reference's initial guess (the previous solution)
     if args.warm_start and not args.no_plain:
         sc0 = scenes.ellipsoid_impact(target_n=args.n, gap=0.0)
-        for f in ("lanes_per_particle", "spmv_unroll", "spmv_path"):
+        for f in ("lanes_per_particle", "spmv_unroll", "spmv_path", "cg_loop", "cg_check_interval"):
             setattr(sc0.opt, f, getattr(sc.opt, f))
         sc0.opt.warm_start = 0
         sim0 = scenes.make_simulator(sc0, device=local)

@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define PD_GB300_ABI_VERSION 4
+#define PD_GB300_ABI_VERSION 5
 
 typedef enum pd_status {
     PD_OK = 0,
@@ -127,7 +127,9 @@ typedef struct pd_solver_options {
     double sphere_stiffness;
     /* performance knobs: 0 = automatic */
     int lanes_per_particle;        /* 4, 8, 16 or 32 lanes cooperate on one bond row of the SpMV */
-    int cg_check_interval;         /* CG iterations launched between convergence read-backs */
+    int cg_check_interval;         /* CG iterations between convergence tests of the loop: the
+                                      graph's while-node body (even, default 4) with cg_loop 0,
+                                      a host batch (default 8) with cg_loop 1 */
     int spmv_unroll;               /* 1, 2 or 4 bonds loaded per lane before computing */
     /* CG initial guess (no reference counterpart for 1, 2 and 3): 0 = the
      * previous solution, as the reference (simulator.cu:745-770); 1 = previous
@@ -166,6 +168,16 @@ typedef struct pd_solver_options {
     double contact_volume;
     /* warm_start = 2: solutions kept for the projection, 1..8; 0 = 8 */
     int history_size;
+    /* how the CG iterations of a step are driven (no reference counterpart:
+     * the reference's CUSP cg loop tests on the host, simulator.cu:735-799):
+     * 0 = a CUDA graph launched once per solve, whose while node repeats
+     * cg_check_interval iterations until the device-side convergence test
+     * stops it -- no host read-back inside the solve; 1 = batches of
+     * iterations launched from the host, each followed by a read-back of the
+     * test.  Both run the same kernels in the same order, so the results are
+     * identical.  Default 0; a device where the graph cannot be built falls
+     * back to 1 (pd_step_stats.cg_graph_solves stays 0). */
+    int cg_loop;
 } pd_solver_options;
 
 /* Export selectors for pd_get. */
@@ -206,6 +218,11 @@ typedef struct pd_step_stats {
                                       (warm_start 2) whose history projection was applied */
     double last_ws_residual_ratio; /* ||r(guess)|| / ||r(previous solution)|| of the last step */
     long long ws_learned_used;     /* warm_start 3: projections that gave the network's column a nonzero weight */
+    long long host_syncs;          /* host waits on the GPU inside pd_advance since pd_make_ready: the
+                                      adaptive time step's test (Newmark-beta or adaptive_integration)
+                                      and the read-back of each solve's result, plus one per host
+                                      batch with cg_loop 1 */
+    long long cg_graph_solves;     /* solves whose iterations ran in the CG graph (cg_loop 0) */
 } pd_step_stats;
 
 /* Device time per kernel class, accumulated with CUDA events on the handle's

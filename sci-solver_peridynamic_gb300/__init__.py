@@ -94,7 +94,7 @@ class SolverOptions(C.Structure):
         ("lanes_per_particle", C.c_int), ("cg_check_interval", C.c_int), ("spmv_unroll", C.c_int),
         ("warm_start", C.c_int), ("spmv_path", C.c_int), ("contact_enabled", C.c_int),
         ("contact_distance", C.c_double), ("contact_stiffness", C.c_double), ("contact_volume", C.c_double),
-        ("history_size", C.c_int),
+        ("history_size", C.c_int), ("cg_loop", C.c_int),
     ]
 
 
@@ -106,7 +106,7 @@ class StepStats(C.Structure):
         ("retries_last_step", C.c_int), ("bonds_initial", C.c_longlong), ("bonds_alive", C.c_longlong),
         ("max_bonds_per_particle", C.c_int), ("clock_scale", C.c_double), ("sim_time", C.c_double),
         ("ws_guesses_kept", C.c_longlong), ("last_ws_residual_ratio", C.c_double),
-        ("ws_learned_used", C.c_longlong),
+        ("ws_learned_used", C.c_longlong), ("host_syncs", C.c_longlong), ("cg_graph_solves", C.c_longlong),
     ]
 
     def as_dict(self):

@@ -74,6 +74,10 @@ pd_status pd_create(const pd_sim_params* sim, const pd_run_params* run, const pd
         g_create_error = "warm_start 0..3, history_size 0..8 (0..7 with warm_start 3)";
         return PD_ERR_INVALID_ARGUMENT;
     }
+    if (o.cg_loop < 0 || o.cg_loop > 1 || o.cg_check_interval < 0) {
+        g_create_error = "cg_loop 0 (graph) or 1 (host batches), cg_check_interval >= 0";
+        return PD_ERR_INVALID_ARGUMENT;
+    }
     if (o.contact_enabled && !(o.contact_distance > 0 && o.contact_volume > 0)) {
         g_create_error = "contact distance and volume must be positive";
         return PD_ERR_INVALID_ARGUMENT;

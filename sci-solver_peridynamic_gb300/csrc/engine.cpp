@@ -879,6 +879,7 @@ pd_status Engine::integrate(bool* advanced)
     if (adaptive) {
         CK(cudaMemcpyAsync(h_flags_, S_.flags, sizeof(int) * 2, cudaMemcpyDeviceToHost, stream_), "read flag");
         CK(cudaStreamSynchronize(stream_), "step sync");
+        ++host_syncs_;
         int rollback = 0;
         pd_adaptive_decide(h_flags_[0], sim_.pd_time_step, opt_.time_step_min, opt_.max_substep, &ticks_, &substep_,
                            &rollback);
@@ -941,64 +942,43 @@ pd_status Engine::solve(const StepParams& P)
             if (s != PD_OK) return s;
         }
     }
-    const int check = opt_.cg_check_interval > 0 ? opt_.cg_check_interval : 8;
-    int batch = predicted_iters_ > 0 ? predicted_iters_ : check;
-    int launched = 0;
-    for (;;) {
-        for (int k = 0; k < batch; ++k) {
-            // profiling times every kMarkStride-th iteration so that the
-            // event records barely perturb the solve they measure; the mean
-            // sampled duration is scaled to the exact launch count
-            const bool sample = (launched % kMarkStride) == 0;
-            if (L_.lattice && d_p2_) {
-                // the direction update p = r + beta p is fused into the
-                // product, which reads the previous direction from one buffer
-                // and writes the new one to the other (buffer 0 = S_.p, set to r
-                // by the residual kernel)
-                void* p_prev = (launched & 1) ? d_p2_ : S_.p;
-                void* p_new = (launched & 1) ? S_.p : d_p2_;
-                if (sample) mark_begin(PD_KC_SPMV, launched);
-                launch_spmv_lattice(true, P, S_, lat_, p_prev, S_.y, ReduceSlot{S_.partials, S_.counters + 1}, S_.sc,
-                                    nullptr, S_.r, p_new, stream_);
-                if (sample) mark_end();
-                DeviceState Sj = S_;
-                Sj.p = p_new;
-                if (sample) mark_begin(PD_KC_CG_VECTOR, launched);
-                launch_cg_axpy(fp64_, P, Sj, L_, stream_);
-                if (sample) mark_end();
-            } else {
-                if (sample) mark_begin(PD_KC_SPMV, launched);
-                launch_spmv(fp64_, true, P, S_, L_, stream_);
-                if (sample) mark_end();
-                if (sample) mark_begin(PD_KC_CG_VECTOR, launched);
-                launch_cg_axpy(fp64_, P, S_, L_, stream_);
-                launch_cg_xpby(fp64_, P, S_, L_, stream_);
-                if (sample) mark_end();
-            }
-            ++launched;
+    // iteration 0 from the host: the sample of the profiled kernel times (a
+    // live launch unless the guess had already converged)
+    cg_iteration(P, 0, 0, true);
+    launches_ += cg_kernels_per_iteration();
+    bool graph = false;
+    if (opt_.cg_loop == 0 && !cg_graph_failed_) {
+        const cudaError_t e = cg_graph_launch(P);
+        if (e == cudaSuccess) {
+            graph = true;
+        } else {
+            // the graph could not be built here: the solve goes on in host-checked batches
+            cudaGetLastError();
+            cg_graph_failed_ = true;
         }
-        launches_ += (L_.lattice && d_p2_ ? 2LL : 3LL) * batch;
-        CK(cudaGetLastError(), "cg launch");
+    }
+    if (graph) {
         CK(cudaMemcpyAsync(h_sc_, S_.sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, stream_), "read cg scalars");
         CK(cudaStreamSynchronize(stream_), "cg sync");
-        if (h_sc_->done) break;
-        if (launched > opt_.cg_max_iterations + 2 * check) {
-            err_ = "cg: iteration count not advancing";
-            return PD_ERR_STATE;
-        }
-        batch = std::max(check, launched / 8);
+        ++host_syncs_;
+        ++cg_graph_solves_;
+        // bodies run: at least one (the while node's first test is the default value 1)
+        const int K = cg_graph_body();
+        const int after0 = std::max(0, h_sc_->iter - 1);
+        const long long bodies = std::max(1, (after0 + K - 1) / K);
+        launches_ += bodies * K * cg_kernels_per_iteration();
+    } else {
+        pd_status s = cg_host_loop(P);
+        if (s != PD_OK) return s;
     }
     last_iters_ = h_sc_->iter;
     last_res_ = h_sc_->rnorm;
     last_tol_ = h_sc_->tol;
     total_iters_ += last_iters_;
     predicted_iters_ = std::max(1, last_iters_);
-    flush_marks(last_iters_);
+    flush_marks(last_iters_, true);
     if (opt_.warm_start == 2 || opt_.warm_start == 3) {
-        if (hist_pending_ratio_) {   // the projected residual's scalars arrived with the loop's syncs
-            last_ws_ratio_ = hist_rz1_ > 0.0 ? std::sqrt(h_sc_hist_->rz / hist_rz1_) : 0.0;
-            hist_pending_ratio_ = false;
-        }
+        hist_collect();
         pd_status s = hist_push();
         if (s != PD_OK) return s;
     }
@@ -1008,6 +988,111 @@ pd_status Engine::solve(const StepParams& P)
     }
     if (!h_sc_->converged) cg_converged_ = false;
     if (ws_features_needed()) return ws_after_cg(P);
+    return PD_OK;
+}
+
+void Engine::cg_iteration(const StepParams& P, int k, cudaGraphConditionalHandle cond, bool sample)
+{
+    // profiling times the host-launched iterations of every kMarkStride-th
+    // index, so that the event records barely perturb the solve they measure;
+    // the mean sampled duration is scaled to the exact launch count
+    sample = sample && profiling_ && cond == 0 && (k % kMarkStride) == 0;
+    if (L_.lattice && d_p2_) {
+        // the direction update p = r + beta p is fused into the product, which
+        // reads the previous direction from one buffer and writes the new one
+        // to the other (buffer 0 = S_.p, set to r by the residual kernel)
+        void* p_prev = (k & 1) ? d_p2_ : S_.p;
+        void* p_new = (k & 1) ? S_.p : d_p2_;
+        if (sample) mark_begin(PD_KC_SPMV, k);
+        launch_spmv_lattice(true, P, S_, lat_, p_prev, S_.y, ReduceSlot{S_.partials, S_.counters + 1}, S_.sc, nullptr,
+                            S_.r, p_new, stream_);
+        if (sample) mark_end();
+        DeviceState Sj = S_;
+        Sj.p = p_new;
+        if (sample) mark_begin(PD_KC_CG_VECTOR, k);
+        launch_cg_axpy(fp64_, P, Sj, L_, stream_, cond);
+        if (sample) mark_end();
+    } else {
+        if (sample) mark_begin(PD_KC_SPMV, k);
+        launch_spmv(fp64_, true, P, S_, L_, stream_);
+        if (sample) mark_end();
+        if (sample) mark_begin(PD_KC_CG_VECTOR, k);
+        launch_cg_axpy(fp64_, P, S_, L_, stream_, cond);
+        launch_cg_xpby(fp64_, P, S_, L_, stream_);
+        if (sample) mark_end();
+    }
+}
+
+// Iterations per while-node body: an even count (the lattice product's
+// direction buffers alternate), 4 unless cg_check_interval asks otherwise.
+int Engine::cg_graph_body() const
+{
+    const int k = opt_.cg_check_interval > 0 ? opt_.cg_check_interval : 4;
+    return std::min(64, (k + 1) & ~1);
+}
+
+// The graph holds one while node; its body is cg_graph_body() iterations
+// captured from the launches of cg_iteration.  Every k_cg_axpy of the body
+// sets the node's condition to "not converged and below the iteration limit"
+// (cg_fin_axpy), or to 0 when the solve had finished before it ran, so the
+// loop ends at most one body after the test that ends the solve: every body
+// that runs holds a live iteration, and the iteration limit sets done.  The
+// operator's constants (StepParams) change every step, so the graph is built
+// and instantiated for each solve, while the GPU still runs the work queued
+// before it.
+cudaError_t Engine::cg_graph_launch(const StepParams& P)
+{
+    const int K = cg_graph_body();
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t x = nullptr;
+    cudaError_t e = cudaGraphCreate(&g, 0);
+    cudaGraphConditionalHandle cond = 0;
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&cond, g, 1u, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = cond;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp);
+    if (e == cudaSuccess) {
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        e = cudaStreamBeginCaptureToGraph(stream_, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            for (int k = 1; k <= K; ++k) cg_iteration(P, k, cond, false);
+            const cudaError_t le = cudaGetLastError();
+            cudaGraph_t captured = nullptr;
+            const cudaError_t ce = cudaStreamEndCapture(stream_, &captured);
+            e = le != cudaSuccess ? le : ce;
+        }
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&x, g, 0);
+    if (e == cudaSuccess) e = cudaGraphLaunch(x, stream_);
+    // an executable graph destroyed while in flight is freed when it completes
+    if (x) cudaGraphExecDestroy(x);
+    if (g) cudaGraphDestroy(g);
+    return e;
+}
+
+pd_status Engine::cg_host_loop(const StepParams& P)
+{
+    const int check = opt_.cg_check_interval > 0 ? opt_.cg_check_interval : 8;
+    int batch = std::max(1, predicted_iters_ - 1);
+    int launched = 1;   // iteration 0 ran from solve()
+    for (;;) {
+        for (int k = 0; k < batch; ++k, ++launched) cg_iteration(P, launched, 0, true);
+        launches_ += (long long)cg_kernels_per_iteration() * batch;
+        CK(cudaGetLastError(), "cg launch");
+        CK(cudaMemcpyAsync(h_sc_, S_.sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, stream_), "read cg scalars");
+        CK(cudaStreamSynchronize(stream_), "cg sync");
+        ++host_syncs_;
+        if (h_sc_->done) break;
+        if (launched > opt_.cg_max_iterations + 2 * check) {
+            err_ = "cg: iteration count not advancing";
+            return PD_ERR_STATE;
+        }
+        batch = std::max(check, launched / 8);
+    }
     return PD_OK;
 }
 
@@ -1035,8 +1120,9 @@ pd_status Engine::hist_prepare()
     CK(cudaMalloc((void**)&d_hpart_, sizeof(double) * (size_t)hist_blocks_ * hist_dots_count(0)),
        "alloc history partials");
     CK(cudaMalloc((void**)&d_hdots_, sizeof(double) * 128), "alloc history dots");
-    CK(cudaMallocHost((void**)&h_hdots_, sizeof(double) * 128), "alloc history dots (host)");
     CK(cudaMallocHost((void**)&h_sc_hist_, sizeof(CgScalars)), "alloc history scalars (host)");
+    CK(cudaMalloc((void**)&d_hsol_, sizeof(HistSolve)), "alloc history solve");
+    CK(cudaMallocHost((void**)&h_hsol_, sizeof(HistSolve)), "alloc history solve (host)");
     hist_reset();
     return PD_OK;
 }
@@ -1049,11 +1135,15 @@ void Engine::hist_free()
     d_hnet_ = nullptr;
     if (d_hpart_) cudaFree(d_hpart_);
     if (d_hdots_) cudaFree(d_hdots_);
-    if (h_hdots_) cudaFreeHost(h_hdots_);
     if (h_sc_hist_) cudaFreeHost(h_sc_hist_);
+    if (d_hsol_) cudaFree(d_hsol_);
+    if (h_hsol_) cudaFreeHost(h_hsol_);
     d_hist_ = d_ahist_ = nullptr;
-    d_hpart_ = d_hdots_ = h_hdots_ = nullptr;
+    d_hpart_ = d_hdots_ = nullptr;
     h_sc_hist_ = nullptr;
+    d_hsol_ = nullptr;
+    h_hsol_ = nullptr;
+    hist_pending_ = false;
     hist_cap_ = 0;
     hist_reset();
 }
@@ -1084,33 +1174,37 @@ pd_status Engine::hist_project(const StepParams& P)
     const int na = hist_dots_count(0);
     launch_hist_dots(fp64_, 0, n_, m, H, W, S_.r, d_hpart_, hist_blocks_, d_hdots_, stream_);
     launch_hist_dots(fp64_, 1, n_, m, H, W, nullptr, d_hpart_, hist_blocks_, d_hdots_ + na, stream_);
-    launches_ += m + 4;
-    CK(cudaGetLastError(), "history products");
-    CK(cudaMemcpyAsync(h_hdots_, d_hdots_, sizeof(double) * (na + hist_dots_count(1)), cudaMemcpyDeviceToHost,
-                       stream_), "read history dots");
-    CK(cudaMemcpyAsync(h_sc_, S_.sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, stream_), "read cg scalars");
-    CK(cudaStreamSynchronize(stream_), "history sync");
-    HistCoef Y{};
     // columns whose part outside the others' span is below sqrt(rel) of the
     // largest norm are rounding noise of the stored precision
     // (measured on a 100k-particle impact: 1e-14 .. 1e-10 within 1 % of iterations; 1e-6 loses the gain)
     const double rel = fp64_ ? 1e-26 : 1e-12;
-    const int used = hist_solve(m, h_hdots_, h_hdots_ + na, h_hdots_ + hist_dots_count(1), rel, Y.y);
-    if (net && Y.y[m - 1] != 0.0) ++ws_net_used_;
-    if (used > 0 && !h_sc_->done) {
-        hist_rz1_ = h_sc_->rz;
-        launch_hist_apply(fp64_, n_, m, H, Y, S_.sol, L_.grid_vec, stream_);
-        launch_spmv(fp64_, false, P, S_, L_, stream_);
-        launch_cg_residual(fp64_, P, S_, L_, stream_);
-        launches_ += 3;
-        CK(cudaMemcpyAsync(h_sc_hist_, S_.sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, stream_),
-           "read projected residual");
-        hist_pending_ratio_ = true;
-        ++ws_kept_;
-    }
+    launch_hist_solve(m, d_hdots_, rel, net ? m - 1 : -1, S_.sc, d_hsol_, stream_);
+    // x1 + H y and its residual (the apply returns at once when no column was
+    // used; the residual is then that of x1 again)
+    launch_hist_apply(fp64_, n_, m, H, d_hsol_, S_.sol, L_.grid_vec, stream_);
+    launch_spmv(fp64_, false, P, S_, L_, stream_);
+    launch_cg_residual(fp64_, P, S_, L_, stream_);
+    launches_ += m + 8;
+    CK(cudaMemcpyAsync(h_hsol_, d_hsol_, sizeof(HistSolve), cudaMemcpyDeviceToHost, stream_), "read history solve");
+    CK(cudaMemcpyAsync(h_sc_hist_, S_.sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, stream_),
+       "read projected residual");
+    hist_pending_ = true;
     mark_end();
     CK(cudaGetLastError(), "history guess");
     return PD_OK;
+}
+
+// After the solve's read-back: whether the projection was applied, its
+// residual relative to the previous solution's, and the network column's use.
+void Engine::hist_collect()
+{
+    if (!hist_pending_) return;
+    hist_pending_ = false;
+    if (h_hsol_->used > 0) {
+        ++ws_kept_;
+        last_ws_ratio_ = h_hsol_->rz1 > 0.0 ? std::sqrt(h_sc_hist_->rz / h_hsol_->rz1) : 0.0;
+    }
+    if (h_hsol_->net_used) ++ws_net_used_;
 }
 
 pd_status Engine::hist_push()
@@ -1156,10 +1250,10 @@ void Engine::mark_end()
 // Accumulates completed marks.  SpMV / CG-vector marks of iterations at or
 // beyond `live_iters` were launches that returned immediately after
 // convergence and are dropped.  live_iters < 0 keeps all.
-void Engine::flush_marks(int live_iters)
+void Engine::flush_marks(int live_iters, bool synced)
 {
     if (marks_.empty()) return;
-    cudaStreamSynchronize(stream_);
+    if (!synced) cudaStreamSynchronize(stream_);
     for (Mark& m : marks_) {
         const bool dead = live_iters >= 0 && m.iter >= live_iters &&
                           (m.kc == PD_KC_SPMV || m.kc == PD_KC_CG_VECTOR);
@@ -1376,6 +1470,8 @@ pd_status Engine::stats(pd_step_stats* s) const
     s->ws_guesses_kept = ws_kept_;
     s->last_ws_residual_ratio = last_ws_ratio_;
     s->ws_learned_used = ws_net_used_;
+    s->host_syncs = host_syncs_;
+    s->cg_graph_solves = cg_graph_solves_;
     if (ready_ && n_ > 0) {
         std::vector<int> c((size_t)n_);
         cudaSetDevice(device_);

@@ -89,6 +89,17 @@ private:
     void* hist_vec(int j) const;
     pd_status integrate(bool* advanced);
     pd_status solve(const StepParams& P);
+    // one CG iteration's launches (iteration k of the solve: on lattice bodies
+    // its parity picks the direction buffers); cond: the CG graph's while
+    // condition when captured into it, else 0
+    void cg_iteration(const StepParams& P, int k, cudaGraphConditionalHandle cond, bool sample);
+    int cg_kernels_per_iteration() const { return (L_.lattice && d_p2_) ? 2 : 3; }
+    int cg_graph_body() const;
+    // iterations 1.. of a solve as one graph launch: a while node repeating
+    // cg_graph_body() iterations until the device-side test stops it
+    cudaError_t cg_graph_launch(const StepParams& P);
+    pd_status cg_host_loop(const StepParams& P);   // the same iterations in host-checked batches
+    void hist_collect();   // the projection's statistics, after the solve's read-back
     template <typename T>
     pd_status download_scatter(const T* dev, T* host_out, size_t count_per, size_t elem_count);
     pd_status ensure_stage(size_t bytes);   // device staging buffer of the exports
@@ -102,7 +113,8 @@ private:
     };
     void mark_begin(int kc, int iter);
     void mark_end();
-    void flush_marks(int live_iters);
+    // synced: every mark was recorded before the latest stream synchronisation
+    void flush_marks(int live_iters, bool synced = false);
     cudaEvent_t take_event();
 
     pd_sim_params sim_;
@@ -156,10 +168,10 @@ private:
     long long ws_net_used_ = 0;   // warm_start 3: projections that gave the network's column a weight
     double* d_hpart_ = nullptr;   // per-block partial sums of a Gram pass
     double* d_hdots_ = nullptr;   // S (36), c (8), G (36)
-    double* h_hdots_ = nullptr;   // pinned copy
     CgScalars* h_sc_hist_ = nullptr;   // pinned: scalars after the projected residual
-    bool hist_pending_ratio_ = false;
-    double hist_rz1_ = 0.0;
+    HistSolve* d_hsol_ = nullptr;      // the m x m solve's result (device)
+    HistSolve* h_hsol_ = nullptr;      // pinned copy, read after the solve
+    bool hist_pending_ = false;        // a projection ran in this solve
     // step state (Simulator members)
     int step_ = 0;
     int substep_ = 0;
@@ -173,6 +185,9 @@ private:
     long long total_iters_ = 0;
     int retries_ = 0;
     int predicted_iters_ = 0;
+    long long host_syncs_ = 0;         // stream synchronisations of the step loop
+    long long cg_graph_solves_ = 0;    // solves whose iterations ran in the CG graph
+    bool cg_graph_failed_ = false;     // the graph could not be built: host-checked batches
     // profiling
     bool profiling_ = false;
     std::vector<cudaEvent_t> event_pool_;

@@ -11,8 +11,9 @@
 // to the same tolerance as always.
 //
 // Per solve: one product A h_j per history vector (the operator changes every
-// step), the small Gram matrices below, a host solve of an m x m system,
-// x += H y, and a fresh residual.  The kernels here are the vector parts.
+// step), the small Gram matrices below, the m x m solve (one thread on the
+// device, so that the solve needs no host read-back), x += H y, and a fresh
+// residual.
 #include <cmath>
 
 #include "pd_device.cuh"
@@ -98,22 +99,42 @@ __global__ void k_hist_sum(const double* partials, int blocks, int na, double* o
     }
 }
 
+// The m x m solve on one thread.  A solve that had already converged from
+// the previous solution keeps it (used = 0).
+__global__ void k_hist_solve(int m, const double* dots, int s_off, int g_off, int c_off, double rel_tol,
+                             int net_col, const CgScalars* sc, HistSolve* out)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    double y[kHistMax];
+    int used = hist_solve(m, dots + s_off, dots + g_off, dots + c_off, rel_tol, y);
+    const volatile CgScalars* v = sc;
+    if (v->done) used = 0;
+    for (int k = 0; k < kHistMax; ++k) out->y[k] = (used > 0 && k < m) ? y[k] : 0.0;
+    out->used = used;
+    out->net_used = (used > 0 && net_col >= 0 && net_col < m && y[net_col] != 0.0) ? 1 : 0;
+    out->rz1 = v->rz;
+}
+
 // x += H y, formed in FP64 (the coefficients of nearly parallel history
 // vectors can be large and of opposite sign)
 template <typename Real>
-__global__ void __launch_bounds__(kBlock) k_hist_apply(int n, int m, HistPtrs H, HistCoef Y, void* x_)
+__global__ void __launch_bounds__(kBlock) k_hist_apply(int n, int m, HistPtrs H, const HistSolve* Y, void* x_)
 {
     using V4 = typename Vec4<Real>::type;
     V4* x = (V4*)x_;
+    if (((const volatile HistSolve*)Y)->used == 0) return;
+    double yk[kHistMax];
+#pragma unroll
+    for (int k = 0; k < kHistMax; ++k) yk[k] = Y->y[k];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         double ax = 0.0, ay = 0.0, az = 0.0;
 #pragma unroll
         for (int k = 0; k < kHistMax; ++k) {
             if (k < m) {
                 const V4 h = ((const V4*)H.v[k])[i];
-                ax = fma(Y.y[k], (double)h.x, ax);
-                ay = fma(Y.y[k], (double)h.y, ay);
-                az = fma(Y.y[k], (double)h.z, az);
+                ax = fma(yk[k], (double)h.x, ax);
+                ay = fma(yk[k], (double)h.y, ay);
+                az = fma(yk[k], (double)h.z, az);
             }
         }
         V4 xi = x[i];
@@ -156,7 +177,14 @@ void launch_hist_dots(bool fp64, int pass, int n, int m, const HistPtrs& H, cons
     k_hist_sum<<<1, 128, 0, st>>>(partials, blocks, hist_dots_count(pass), out);
 }
 
-void launch_hist_apply(bool fp64, int n, int m, const HistPtrs& H, const HistCoef& Y, void* x, int blocks,
+void launch_hist_solve(int m, const double* dots, double rel_tol, int net_col, const CgScalars* sc, HistSolve* out,
+                       cudaStream_t st)
+{
+    const int na = hist_dots_count(0);
+    k_hist_solve<<<1, 32, 0, st>>>(m, dots, 0, na, kPairs, rel_tol, net_col, sc, out);
+}
+
+void launch_hist_apply(bool fp64, int n, int m, const HistPtrs& H, const HistSolve* Y, void* x, int blocks,
                        cudaStream_t st)
 {
     if (fp64) k_hist_apply<double><<<blocks, kBlock, 0, st>>>(n, m, H, Y, x);
@@ -169,14 +197,15 @@ void launch_hist_push(bool fp64, int n, const uint8_t* act, const void* x, void*
     else k_hist_push<float><<<blocks, kBlock, 0, st>>>(n, act, x, dst);
 }
 
-// ---- host side: the m x m solve ------------------------------------------------------
+// ---- the m x m solve (host and device) ------------------------------------------------
 // S = H^T H, G = H^T A H (upper triangles, row-major pairs a <= b), c = H^T r1.
 // A pivoted Cholesky of S selects a well-conditioned subset of the history
 // (columns whose remaining component is below rel_tol of the largest are
 // dropped: in FP32 storage they are rounding noise); in the orthonormal basis
 // Q = H_sel R^-1 the projected system G_Q z = c_Q is solved by Cholesky and
 // y = R^-1 z.  Returns the number of columns used (0: no usable guess).
-int hist_solve(int m, const double* S_up, const double* G_up, const double* c, double rel_tol, double* y)
+__host__ __device__ int hist_solve(int m, const double* S_up, const double* G_up, const double* c, double rel_tol,
+                                   double* y)
 {
     double S[kHistMax][kHistMax], G[kHistMax][kHistMax];
     int e = 0;
@@ -287,7 +316,7 @@ int hist_solve(int m, const double* S_up, const double* G_up, const double* c, d
     for (int i = 0; i < r; ++i) {
         double s = 0.0;
         for (int k = i; k < r; ++k) s += Ri[i][k] * z[k];
-        if (!std::isfinite(s)) {
+        if (!(fabs(s) <= 1.7976931348623157e308)) {   // NaN or infinite
             for (int q = 0; q < m; ++q) y[q] = 0.0;
             return 0;
         }

@@ -178,6 +178,7 @@ extern "C" pd_status pd_solver_options_default(pd_solver_options* o)
     o->sphere_enabled = 0;
     o->lanes_per_particle = 0;
     o->cg_check_interval = 0;
+    o->cg_loop = 0;
     return PD_OK;
 }
 

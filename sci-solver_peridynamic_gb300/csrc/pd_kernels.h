@@ -228,7 +228,9 @@ void launch_spmv(bool fp64, bool dot, const StepParams& P, const DeviceState& S,
 void launch_operator(bool fp64, const StepParams& P, const DeviceState& S, int lanes, int grid, const void* in,
                      void* out, ReduceSlot slot, double* dot_out, cudaStream_t st);
 void launch_cg_residual(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
-void launch_cg_axpy(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
+// cond: the while node's condition handle when launched inside the CG graph, else 0
+void launch_cg_axpy(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st,
+                    cudaGraphConditionalHandle cond = 0);
 void launch_cg_xpby(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
 void launch_update(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
 void launch_refresh(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
@@ -273,16 +275,33 @@ int row_kernel_blocks_per_sm(bool fp64, int lanes, int unroll);
 // ---- history-projection initial guess (history.cu) --------------------------------
 constexpr int kHistMax = 8;                 // history vectors kept at most
 struct HistPtrs { const void* v[kHistMax]; };
-struct HistCoef { double y[kHistMax]; };
+// the m x m solve's result, in device memory: coefficients, columns used
+// (0: no guess), whether the network's column got a nonzero weight, and <r,r>
+// of the previous solution's residual
+struct HistSolve {
+    double y[kHistMax];
+    int used;
+    int net_used;
+    double rz1;
+};
 // entries of a Gram pass: 0 -> S = H^T H (upper) then c = H^T r; 1 -> G = H^T W (upper)
 int hist_dots_count(int pass);
 void launch_hist_dots(bool fp64, int pass, int n, int m, const HistPtrs& H, const HistPtrs& W, const void* r,
                       double* partials, int blocks, double* out, cudaStream_t st);
-void launch_hist_apply(bool fp64, int n, int m, const HistPtrs& H, const HistCoef& Y, void* x, int blocks,
+// one-thread device solve of the dots of launch_hist_dots (both passes, in
+// order, at `dots`); net_col: the network's column, or -1
+void launch_hist_solve(int m, const double* dots, double rel_tol, int net_col, const CgScalars* sc, HistSolve* out,
+                       cudaStream_t st);
+// x += H y where out->used > 0
+void launch_hist_apply(bool fp64, int n, int m, const HistPtrs& H, const HistSolve* Y, void* x, int blocks,
                        cudaStream_t st);
 void launch_hist_push(bool fp64, int n, const uint8_t* act, const void* x, void* dst, int blocks, cudaStream_t st);
-// host: coefficients y of x1 + H y (Galerkin over the well-conditioned part of
-// span H); returns the number of history columns used, 0 for no guess
+// coefficients y of x1 + H y (Galerkin over the well-conditioned part of span
+// H); returns the number of history columns used, 0 for no guess.  Host and
+// device (history.cu); the host build serves the tests.
+#ifdef __CUDACC__
+__host__ __device__
+#endif
 int hist_solve(int m, const double* S_up, const double* G_up, const double* c, double rel_tol, double* y);
 int force_kernel_blocks_per_sm(bool fp64, int lanes);
 void launch_operator_u(bool fp64, const StepParams& P, const DeviceState& S, int lanes, int unroll, int grid,

@@ -114,17 +114,30 @@ __global__ void __launch_bounds__(kBlock) k_cg_residual(StepParams P, DeviceStat
 }
 
 // x += alpha p ; r -= alpha A p ; rz' = <r,r> ; beta = rz'/rz ; test
+//
+// Inside the CG graph (cond != 0) this kernel also sets the while node's
+// condition: its finisher to "not done" after the test, or, when the solve
+// had already finished before the launch, block 0 to 0.  Exactly one thread of
+// each launch sets it: `done` only changes in the finisher, which runs after
+// every block has read it, so all blocks of one launch take the same branch.
 template <bool FP64>
-__global__ void __launch_bounds__(kBlock) k_cg_axpy(StepParams P, DeviceState S, ReduceSlot slot)
+__global__ void __launch_bounds__(kBlock) k_cg_axpy(StepParams P, DeviceState S, ReduceSlot slot,
+                                                   cudaGraphConditionalHandle cond)
 {
     using Real = typename std::conditional<FP64, double, float>::type;
     CgScalars* sc = S.sc;
-    if (((volatile CgScalars*)sc)->done) return;
+    if (((volatile CgScalars*)sc)->done) {
+        if (cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond, 0u);
+        return;
+    }
     const Real alpha = (Real)sc->alpha;
     typename DotAccFor<Real>::type acc;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x)
         axpy_elem<FP64>(S, i, alpha, acc);
-    block_reduce_finish(acc, slot, [sc](double rr) { cg_fin_axpy(sc, rr); });
+    block_reduce_finish(acc, slot, [sc, cond](double rr) {
+        cg_fin_axpy(sc, rr);
+        if (cond) cudaGraphSetConditional(cond, sc->done ? 0u : 1u);
+    });
 }
 
 // p = r + beta p
@@ -325,10 +338,11 @@ void launch_cg_residual(bool fp64, const StepParams& P, const DeviceState& S, co
     else k_cg_residual<false><<<L.grid_vec, kBlock, 0, st>>>(P, S, slot_of(S, 2));
 }
 
-void launch_cg_axpy(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st)
+void launch_cg_axpy(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st,
+                    cudaGraphConditionalHandle cond)
 {
-    if (fp64) k_cg_axpy<true><<<L.grid_vec, kBlock, 0, st>>>(P, S, slot_of(S, 3));
-    else k_cg_axpy<false><<<L.grid_vec, kBlock, 0, st>>>(P, S, slot_of(S, 3));
+    if (fp64) k_cg_axpy<true><<<L.grid_vec, kBlock, 0, st>>>(P, S, slot_of(S, 3), cond);
+    else k_cg_axpy<false><<<L.grid_vec, kBlock, 0, st>>>(P, S, slot_of(S, 3), cond);
 }
 
 void launch_cg_xpby(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st)

@@ -32,7 +32,7 @@ def test_library_exports_every_declared_symbol(pdgb):
 
 
 def test_abi_version(pdgb):
-    assert pdgb.library().pd_abi_version() == 4
+    assert pdgb.library().pd_abi_version() == 5
 
 
 def test_params_file_and_derivation(pdgb, tmp_path):
@@ -150,6 +150,21 @@ def test_invalid_warm_start_rejected(pdgb, scenes, field, value):
         scenes.make_simulator(sc)
     assert e.value.status == 1
     assert "warm_start" in str(e.value)
+
+
+@pytest.mark.parametrize("field,value", [("cg_loop", 2), ("cg_loop", -1), ("cg_check_interval", -3)])
+def test_invalid_cg_loop_rejected(pdgb, scenes, field, value):
+    sc = scenes.reference_block(n_side=3)
+    setattr(sc.opt, field, value)
+    with pytest.raises(pdgb.PdError) as e:
+        scenes.make_simulator(sc)
+    assert e.value.status == 1
+    assert "cg_loop" in str(e.value)
+
+
+def test_solver_option_cg_loop_default(pdgb):
+    """The graph-driven CG loop is the default."""
+    assert pdgb.default_options().cg_loop == 0
 
 
 def test_batch_scene_sizes():
