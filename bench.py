@@ -498,6 +498,7 @@ def _batch_arm(pkg, scenes, lst, local, args, warm_start, params=None):
     k_all = range(len(lst))
     it0 = sum(b.stats(k).total_cg_iterations for k in k_all)
     kept0 = sum(b.stats(k).ws_guesses_kept for k in k_all)
+    skipped0 = sum(b.stats(k).ws_guesses_skipped for k in k_all)
     l0 = b.launch_count()
     sampler = ClockSampler(local)
     sampler.start()
@@ -507,6 +508,7 @@ def _batch_arm(pkg, scenes, lst, local, args, warm_start, params=None):
         "launches": b.launch_count() - l0,
         "iters": sum(b.stats(k).total_cg_iterations for k in k_all) - it0,
         "kept": sum(b.stats(k).ws_guesses_kept for k in k_all) - kept0,
+        "skipped": sum(b.stats(k).ws_guesses_skipped for k in k_all) - skipped0,
         "bonds": sum(b.stats(k).bonds_alive for k in k_all),
         "max_iters": max(b.stats(k).last_cg_iterations for k in k_all),
         "converged": all(b.stats(k).cg_converged for k in k_all),
@@ -578,6 +580,9 @@ def run_batched(args):
                    "cg_iterations_per_step_all_scenes": round(st["iters"] / args.steps, 1),
                    "cg_iterations_last_step_max": int(st["max_iters"]),
                    "learned_guesses_kept": "%d of %d scene-steps" % (st["kept"], args.steps * len(lst)),
+                   "learned_pass_paused": ("%d of %d scene-steps (3 rejected guesses in a row pause a scene's "
+                                           "learned pass; retried every 16 steps)" % (st["skipped"],
+                                                                                      args.steps * len(lst))),
                    "network": "trained on the GPU from %d plain-solver pairs of 4 other scenes in %.1f s "
                               "(loss %.4g)" % (X.shape[0], t_train, loss),
                    "launch_shape": {"lanes": cfg.lanes_per_particle, "unroll": cfg.spmv_unroll,

@@ -223,6 +223,8 @@ typedef struct pd_step_stats {
                                       and the read-back of each solve's result, plus one per host
                                       batch with cg_loop 1 */
     long long cg_graph_solves;     /* solves whose iterations ran in the CG graph (cg_loop 0) */
+    long long ws_guesses_skipped;  /* batch learned warm start: steps whose learned pass was paused
+                                      (3 guesses rejected in a row; retried every 16 steps) */
 } pd_step_stats;
 
 /* Device time per kernel class, accumulated with CUDA events on the handle's

@@ -107,6 +107,7 @@ class StepStats(C.Structure):
         ("max_bonds_per_particle", C.c_int), ("clock_scale", C.c_double), ("sim_time", C.c_double),
         ("ws_guesses_kept", C.c_longlong), ("last_ws_residual_ratio", C.c_double),
         ("ws_learned_used", C.c_longlong), ("host_syncs", C.c_longlong), ("cg_graph_solves", C.c_longlong),
+        ("ws_guesses_skipped", C.c_longlong),
     ]
 
     def as_dict(self):

@@ -526,7 +526,9 @@ pd_status Batch::pull_state()
         for (size_t s = 0; s < ns; ++s) {
             Engine& e = *eng_[s];
             e.ws_kept_ = sc[s].ws_kept;
-            e.last_ws_ratio_ = sc[s].rz_plain > 0 ? std::sqrt(sc[s].rz_learned / sc[s].rz_plain) : 0.0;
+            e.ws_skipped_ = sc[s].ws_skipped;
+            e.last_ws_ratio_ = (sc[s].rz_plain > 0 && !sc[s].ws_skip) ? std::sqrt(sc[s].rz_learned / sc[s].rz_plain)
+                                                                      : 0.0;
         }
     }
     if (sync.error) {

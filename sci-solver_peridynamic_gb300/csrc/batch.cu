@@ -282,25 +282,51 @@ __device__ void spmv_item(const SceneDesc& d, const WorkItem& it, const void* in
 }
 
 // ---- learned warm start (mixed precision) -------------------------------------------
+// A scene whose guard rejected kWsRejectLimit guesses in a row pauses its
+// learned pass (features, guess, guess residual): it starts from the previous
+// solution as without the network, and tries the network again every
+// kWsRetryPeriod steps; one kept guess ends the pause.
+constexpr int kWsRejectLimit = 3;
+constexpr int kWsRetryPeriod = 16;
+
+__device__ __forceinline__ bool ws_paused(const SceneDesc& d) { return ld_volatile(&d.S.sc->ws_skip) != 0; }
+
 // End of k_batch_pre: x1 saved, Jacobi step and the RMS scales, features of
-// every solving scene (written into the batch's feature rows).
+// every solving scene whose learned pass is not paused (written into the
+// batch's feature rows).
 __device__ void ws_features_phases(const BatchArgs& A, ItemList& L)
 {
     constexpr int G = 8;
     const unsigned gmask = group_mask<G>();
     const int lane = threadIdx.x & (G - 1);
     constexpr int gpb = kBlock / G;
+    // this step's pause decision, by the scene's owner thread (the fields are
+    // not touched by the phase still running in other blocks)
+    if (threadIdx.x == 0) {
+        for (int s = blockIdx.x; s < A.n_scenes; s += gridDim.x) {
+            if (!ld_volatile(&A.run[s].solving)) continue;
+            CgScalars* sc = A.scenes[s].S.sc;
+            const int rej = sc->ws_rejects;
+            const int skip = rej >= kWsRejectLimit && (rej % kWsRetryPeriod) != kWsRetryPeriod - 1;
+            sc->ws_skip = skip;
+            if (skip) {
+                sc->ws_rejects = rej + 1;
+                sc->ws_skipped += 1;
+            }
+        }
+    }
     if (!grid_barrier(A.sync)) return;
     for_each_item(A, kSelSolving, L, [&](int i, const WorkItem& it) {
         const SceneDesc& d = A.scenes[it.scene];
         const float4* x = (const float4*)d.S.sol;
         // solution history of the features: x3 <- x2 <- the previous step's
-        // x1, then x1 <- the current guess
+        // x1, then x1 <- the current guess (kept current while paused)
         for (int r = it.lo + threadIdx.x; r < it.hi; r += blockDim.x) {
             d.W.hist3[r] = d.W.hist2[r];
             d.W.hist2[r] = d.W.xsave[r];
             d.W.xsave[r] = x[r];
         }
+        if (ws_paused(d)) return;   // every item of the scene returns: its reduction is not entered
         DotAcc32 acc[3];
         for (int p0 = it.lo; p0 < it.hi; p0 += gpb) {
             const int p = p0 + threadIdx.x / G;
@@ -316,6 +342,7 @@ __device__ void ws_features_phases(const BatchArgs& A, ItemList& L)
     if (!grid_barrier(A.sync)) return;
     for_each_item(A, kSelSolving, L, [&](int, const WorkItem& it) {
         const SceneDesc& d = A.scenes[it.scene];
+        if (ws_paused(d)) return;
         const volatile WsScalars* wsc = d.W.sc;
         const float sx = safe_scale(wsc->sum_x2, wsc->n_free);
         const float sr = safe_scale(wsc->sum_r2, wsc->n_free);
@@ -341,6 +368,7 @@ __device__ void ws_guess_phases(const BatchArgs& A, ItemList& L)
     }
     for_each_item(A, kSelSolving, L, [&](int, const WorkItem& it) {
         const SceneDesc& d = A.scenes[it.scene];
+        if (ws_paused(d)) return;
         const WsScalars* wsc = d.W.sc;
         const float so = safe_scale(wsc->sum_x2, wsc->n_free) + safe_scale(wsc->sum_r2, wsc->n_free);
         const float4* r = (const float4*)d.S.r;
@@ -352,12 +380,14 @@ __device__ void ws_guess_phases(const BatchArgs& A, ItemList& L)
     if (!grid_barrier(A.sync)) return;
     for_each_item(A, kSelSolving, L, [&](int, const WorkItem& it) {
         const SceneDesc& d = A.scenes[it.scene];
+        if (ws_paused(d)) return;
         Acc acc;
         spmv_item<G, false, false, U, kLdCoherent>(d, it, d.S.sol, d.S.y, acc);
     });
     if (!grid_barrier(A.sync)) return;
     for_each_item(A, kSelSolving, L, [&](int i, const WorkItem& it) {
         const SceneDesc& d = A.scenes[it.scene];
+        if (ws_paused(d)) return;
         Acc acc;
         for (int r = it.lo + threadIdx.x; r < it.hi; r += blockDim.x) residual_elem<false>(d.S, r, acc);
         CgScalars* sc = d.S.sc;
@@ -373,7 +403,7 @@ __device__ void ws_guess_phases(const BatchArgs& A, ItemList& L)
     if (!grid_barrier(A.sync)) return;
     for_each_item(A, kSelSolving, L, [&](int, const WorkItem& it) {
         const SceneDesc& d = A.scenes[it.scene];
-        if (!ld_volatile(&d.S.sc->ws_revert)) return;
+        if (ws_paused(d) || !ld_volatile(&d.S.sc->ws_revert)) return;
         float4* x = (float4*)d.S.sol;
         float4* r = (float4*)d.S.r;
         float4* pv = (float4*)d.S.p;

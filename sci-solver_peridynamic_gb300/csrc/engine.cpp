@@ -1470,6 +1470,7 @@ pd_status Engine::stats(pd_step_stats* s) const
     s->ws_guesses_kept = ws_kept_;
     s->last_ws_residual_ratio = last_ws_ratio_;
     s->ws_learned_used = ws_net_used_;
+    s->ws_guesses_skipped = ws_skipped_;
     s->host_syncs = host_syncs_;
     s->cg_graph_solves = cg_graph_solves_;
     if (ready_ && n_ > 0) {

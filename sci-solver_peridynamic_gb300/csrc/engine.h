@@ -160,6 +160,7 @@ private:
     unsigned long long ws_rng_ = 88172645463325252ull;
     double last_ws_ratio_ = 0.0;
     long long ws_kept_ = 0;
+    long long ws_skipped_ = 0;    // batch scenes: steps whose learned pass was paused
     // history projection
     int hist_cap_ = 0, hist_m_ = 0, hist_next_ = 0, hist_blocks_ = 0;
     void* d_hist_ = nullptr;      // hist_cap_ vectors of n entries: accepted solutions, Dirichlet rows 0

@@ -46,6 +46,9 @@ struct CgScalars {
     double rz_learned;     // <r, r> of the learned guess
     int ws_revert;         // 1: the learned guess was worse and was replaced
     int ws_kept;           // learned guesses kept so far
+    int ws_rejects;        // batch: consecutive rejected guesses (and paused steps since)
+    int ws_skip;           // batch: 1 while this step's learned pass is paused
+    int ws_skipped;        // batch: steps whose learned pass was paused
 };
 
 // Partial-sum scratch of a reducing launch: one double per block and an

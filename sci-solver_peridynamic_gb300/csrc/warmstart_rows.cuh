@@ -172,8 +172,9 @@ __device__ __forceinline__ void ws_apply_elem(const DeviceState& S, const float*
 __device__ __forceinline__ void ws_decide(CgScalars* sc)
 {
     sc->rz_learned = sc->rz;
-    if (sc->rz > sc->rz_plain) {
+    if (!(sc->rz <= sc->rz_plain)) {   // worse, or not a number: back to the previous solution
         sc->ws_revert = 1;
+        sc->ws_rejects += 1;
         sc->rz = sc->rz_plain;
         sc->rnorm = sqrt(sc->rz_plain);
         sc->done = 0;
@@ -186,6 +187,7 @@ __device__ __forceinline__ void ws_decide(CgScalars* sc)
         }
     } else {
         sc->ws_revert = 0;
+        sc->ws_rejects = 0;
         sc->ws_kept += 1;
     }
 }

@@ -211,3 +211,34 @@ def test_batch_warm_start_needs_mixed_precision(pdgb, scenes):
     with pytest.raises(pdgb.PdError) as e:
         pdgb.Batch(0, o)
     assert e.value.status == 1
+
+
+def test_batch_pauses_the_learned_pass_of_rejecting_scenes(pdgb, scenes):
+    """A network whose guesses the guard rejects: after 3 rejections in a row
+    a scene pauses its learned pass (retrying every 16 steps), and starts
+    from the previous solution exactly as the batch without the network --
+    positions bit for bit.  Over 40 solves an always-rejecting scene is
+    paused in 35 (steps 4-15, 17-31, 33-40)."""
+    n_par = pdgb.library().pd_mlp_param_count()
+    params = np.random.default_rng(3).normal(0.0, 0.5, n_par).astype(np.float32)
+    lst = [scenes.impact_body(300, "block", coeff=5.0, speed=5.0, seed=1, precision=0, steps=40),
+           scenes.impact_body(400, "ball", coeff=6.0, speed=8.0, seed=2, precision=0, steps=40),
+           scenes.cube_lattice(n_side=8, seed=1)]
+    b = _batch(pdgb, scenes, lst, warm_start=1)
+    b.ws_set_params(params)
+    plain = _batch(pdgb, scenes, lst, warm_start=0, lanes_per_particle=b.config().lanes_per_particle,
+                   spmv_unroll=b.config().spmv_unroll, item_rows=b.config().item_rows)
+    b.advance(40)
+    plain.advance(40)
+    rejecting = 0
+    for k in range(len(lst)):
+        st = b.stats(k)
+        assert st.current_step == 40 and st.cg_converged == 1
+        if st.ws_guesses_kept == 0:
+            rejecting += 1
+            assert st.ws_guesses_skipped == 35, f"scene {k}"
+            np.testing.assert_array_equal(b.get(k, pdgb.VAR_POSITION), plain.get(k, pdgb.VAR_POSITION))
+            assert st.total_cg_iterations == plain.stats(k).total_cg_iterations
+        else:
+            assert st.ws_guesses_skipped < 35
+    assert rejecting > 0, "the random network's guesses are rejected"
