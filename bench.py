@@ -75,6 +75,8 @@ def parse_args(argv=None):
     ap.add_argument("--history", type=int, default=0, help="warm start 2: solutions kept (0 = 8)")
     ap.add_argument("--cg-loop", type=int, default=0, choices=(0, 1),
                     help="CG loop: 0 = CUDA graph with a device-side while node, 1 = host-checked batches")
+    ap.add_argument("--precond", type=int, default=0, choices=(0, 1, 2),
+                    help="CG preconditioner: 0 none (the reference's), 1 diagonal, 2 3x3 diagonal blocks")
     ap.add_argument("--no-plain", action="store_true", help="skip the previous-solution-guess comparison run")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -267,6 +269,7 @@ def run_gb300(args):
     sc.opt.warm_start = args.warm_start
     sc.opt.history_size = args.history
     sc.opt.cg_loop = args.cg_loop
+    sc.opt.preconditioner = args.precond
     sim = scenes.make_simulator(sc, device=local)
     sim.makeReady()
     sim.advance(args.warmup)
@@ -339,6 +342,8 @@ def run_gb300(args):
                         "stops it" % (sc.opt.cg_check_interval or 4) if args.cg_loop == 0 else
                         "host-launched batches, a read-back of the test after each"),
             "cg_graph_solves": int(st1.cg_graph_solves - st0.cg_graph_solves),
+            "cg_preconditioner": ("none (the reference's plain CG)", "inverse diagonal",
+                                  "inverse 3x3 diagonal blocks")[args.precond],
             "host_syncs_per_step": round((st1.host_syncs - st0.host_syncs) / args.steps, 2),
             "parallelism": "replicas x%d" % world,
             "l2": ("inputs larger than L2 (1/d0 stencil table %.0f MB + particle state > 129 MB L2)" % (320 * n / 1e6)
@@ -365,7 +370,7 @@ def run_gb300(args):
     # the same steps with the reference's initial guess (the previous solution)
     if args.warm_start and not args.no_plain:
         sc0 = scenes.ellipsoid_impact(target_n=args.n, gap=0.0)
-        for f in ("lanes_per_particle", "spmv_unroll", "spmv_path", "cg_loop", "cg_check_interval"):
+        for f in ("lanes_per_particle", "spmv_unroll", "spmv_path", "cg_loop", "cg_check_interval", "preconditioner"):
             setattr(sc0.opt, f, getattr(sc.opt, f))
         sc0.opt.warm_start = 0
         sim0 = scenes.make_simulator(sc0, device=local)

@@ -178,6 +178,14 @@ typedef struct pd_solver_options {
      * identical.  Default 0; a device where the graph cannot be built falls
      * back to 1 (pd_step_stats.cg_graph_solves stays 0). */
     int cg_loop;
+    /* CG preconditioner (the reference's cusp::precond::diagonal is
+     * commented out, simulator.cu:767-769, so it runs plain CG): 0 = none, as
+     * the reference; 1 = the inverse diagonal of A (Jacobi); 2 = the inverse
+     * 3x3 diagonal blocks of A (block Jacobi; a block that is not positive
+     * definite takes 1's rule).  The stopping test stays ||r|| <= tol ||b||,
+     * so the tolerance means the same.  Single handles only (a batch scene
+     * with a preconditioner is rejected). */
+    int preconditioner;
 } pd_solver_options;
 
 /* Export selectors for pd_get. */

@@ -73,7 +73,7 @@ class PdoParams(C.Structure):
         ("sphere_c0", C.c_double * 3), ("sphere_v", C.c_double * 3),
         ("sphere_radius", C.c_double), ("sphere_k", C.c_double),
         ("contact_on", C.c_int), ("contact_dist", C.c_double), ("contact_k", C.c_double),
-        ("contact_vol", C.c_double),
+        ("contact_vol", C.c_double), ("precond", C.c_int),
     ]
 
 

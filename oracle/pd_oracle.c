@@ -498,9 +498,52 @@ static double dot4n(pdo_state* s, const double* a, const double* b)
 
 static int is_dirichlet(int a) { return a == PDO_INVISIBLE || a == PDO_CLAMPED || a == PDO_PRESCRIBED; }
 
+/* Inverse of a symmetric 3x3 diagonal block D (xx yy zz xy xz yz): the
+ * block's inverse by adjugate over determinant where it is positive definite
+ * (mode 2), else -- and for mode 1 -- the inverse of its diagonal, 1 / mass
+ * for a non-positive entry.  The preconditioner option of the GPU path
+ * (an extension: the reference's diagonal preconditioner is commented out,
+ * simulator.cu:767-769). */
+static void pc_invert(int mode, double mass, const double D[6], double M[6])
+{
+    const double a = D[0], b = D[1], c = D[2], d = D[3], e = D[4], f = D[5];
+    if (mode == 2) {
+        const double c00 = b * c - f * f, c11 = a * c - e * e, c22 = a * b - d * d;
+        const double c01 = e * f - d * c, c02 = d * f - b * e, c12 = d * e - a * f;
+        const double det = a * c00 + d * c01 + e * c02;
+        if (a > 0.0 && c22 > 0.0 && det > 0.0) {
+            const double id = 1.0 / det;
+            M[0] = c00 * id; M[1] = c11 * id; M[2] = c22 * id;
+            M[3] = c01 * id; M[4] = c02 * id; M[5] = c12 * id;
+            return;
+        }
+    }
+    const double im = 1.0 / mass;
+    M[0] = a > 0.0 ? 1.0 / a : im;
+    M[1] = b > 0.0 ? 1.0 / b : im;
+    M[2] = c > 0.0 ? 1.0 / c : im;
+    M[3] = M[4] = M[5] = 0.0;
+}
+
+/* z = M r per particle (Dirichlet rows: r is 0 there) */
+static void pc_apply(const pdo_state* s, const double* M, const double* r, double* z)
+{
+    #pragma omp parallel for schedule(static)
+    for (int i = 0; i < s->n; ++i) {
+        const double* m = M + 6 * (size_t)i;
+        const double* ri = r + 4 * i;
+        z[4 * i + 0] = m[0] * ri[0] + m[3] * ri[1] + m[4] * ri[2];
+        z[4 * i + 1] = m[3] * ri[0] + m[1] * ri[1] + m[5] * ri[2];
+        z[4 * i + 2] = m[4] * ri[0] + m[5] * ri[1] + m[2] * ri[2];
+        z[4 * i + 3] = 0.0;
+    }
+}
+
 /* CUSP krylov::cg with identity preconditioner and default_monitor(b, maxit, reltol)
  * (called at src/core/simulator.cu:760-770), restated; Dirichlet rows
- * (extension) are handled by projection.  Returns 1 if converged. */
+ * (extension) are handled by projection.  With P.precond (extension) the
+ * same loop preconditioned: rho = <r, z>, z = M r, p = z + beta p, the test
+ * still on ||r||.  Returns 1 if converged. */
 static int solve_cg(pdo_state* s)
 {
     const pdo_params* P = &s->P;
@@ -531,13 +574,27 @@ static int solve_cg(pdo_state* s)
     if (has_d)
         for (int i = 0; i < n; ++i)
             if (is_dirichlet(s->act[i])) r[4 * i] = r[4 * i + 1] = r[4 * i + 2] = r[4 * i + 3] = 0.0;
-    memcpy(p, r, 4 * (size_t)n * sizeof(double));
-    double rz = dot4n(s, r, r);
+    /* preconditioner: inverse diagonal blocks of the assembled matrix */
+    double *M = NULL, *z = r;
+    if (P->precond) {
+        M = (double*)xcalloc(6 * (size_t)n, sizeof(double));
+        z = (double*)xcalloc(4 * (size_t)n, sizeof(double));
+        for (int i = 0; i < n; ++i) {
+            if (is_dirichlet(s->act[i])) continue;
+            const double* A = s->diag + 9 * (size_t)i;
+            const double D[6] = {A[0], A[4], A[8], A[1], A[2], A[5]};
+            pc_invert(P->precond, P->mass, D, M + 6 * (size_t)i);
+        }
+        pc_apply(s, M, r, z);
+    }
+    memcpy(p, z, 4 * (size_t)n * sizeof(double));
+    double rr = dot4n(s, r, r);
+    double rz = P->precond ? dot4n(s, r, z) : rr;
     int it = 0;
     int conv = 0;
     double rnorm = 0.0;
     for (;;) {
-        rnorm = sqrt(rz);   /* nrm2(r); z = r, so <r,z> is the same fixed-order sum */
+        rnorm = sqrt(rr);   /* nrm2(r); without a preconditioner z = r, so <r,z> is the same fixed-order sum */
         if (rnorm <= tol) { conv = 1; break; }
         if (it >= P->cg_max_iter) break;
         pdo_apply_A(s, p, y);
@@ -548,10 +605,20 @@ static int solve_cg(pdo_state* s)
         for (long i = 0; i < 4L * n; ++i) x[i] = alpha * p[i] + x[i];
         for (long i = 0; i < 4L * n; ++i) r[i] = -alpha * y[i] + r[i];
         const double rz_old = rz;
-        rz = dot4n(s, r, r);
+        rr = dot4n(s, r, r);
+        if (P->precond) {
+            pc_apply(s, M, r, z);
+            rz = dot4n(s, r, z);
+        } else {
+            rz = rr;
+        }
         const double beta = rz / rz_old;
-        for (long i = 0; i < 4L * n; ++i) p[i] = 1.0 * r[i] + beta * p[i];
+        for (long i = 0; i < 4L * n; ++i) p[i] = 1.0 * z[i] + beta * p[i];
         ++it;
+    }
+    if (P->precond) {
+        free(M);
+        free(z);
     }
     s->cg_iters = it;
     s->cg_res = rnorm;

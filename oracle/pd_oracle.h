@@ -70,6 +70,10 @@ typedef struct pdo_params {
     double contact_dist;     /* FCELL * PERIDYNAMICS_MIN_DISTANCE */
     double contact_k;        /* Kc */
     double contact_vol;      /* PD_V */
+    /* CG preconditioner (extension; the reference's cusp::precond::diagonal
+     * is commented out at simulator.cu:767-769): 0 none, 1 inverse diagonal,
+     * 2 inverse 3x3 diagonal blocks of the assembled matrix */
+    int    precond;
 } pdo_params;
 
 typedef struct pdo_state pdo_state;

@@ -94,7 +94,7 @@ class SolverOptions(C.Structure):
         ("lanes_per_particle", C.c_int), ("cg_check_interval", C.c_int), ("spmv_unroll", C.c_int),
         ("warm_start", C.c_int), ("spmv_path", C.c_int), ("contact_enabled", C.c_int),
         ("contact_distance", C.c_double), ("contact_stiffness", C.c_double), ("contact_volume", C.c_double),
-        ("history_size", C.c_int), ("cg_loop", C.c_int),
+        ("history_size", C.c_int), ("cg_loop", C.c_int), ("preconditioner", C.c_int),
     ]
 
 

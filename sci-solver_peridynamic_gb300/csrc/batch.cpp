@@ -166,8 +166,12 @@ pd_status Batch::add_scene(const pd_sim_params& sim, const pd_run_params& run, c
         err_ = "PD-PD contact is not available in batches";
         return PD_ERR_INVALID_ARGUMENT;
     }
-    if (opt.warm_start == 2) {
-        err_ = "the history-projection guess (warm_start 2) is not available in batches";
+    if (opt.warm_start == 2 || opt.warm_start == 3) {
+        err_ = "the history-projection guess (warm_start 2 and 3) is not available in batches";
+        return PD_ERR_INVALID_ARGUMENT;
+    }
+    if (opt.preconditioner != 0) {
+        err_ = "the preconditioned CG is not available in batches";
         return PD_ERR_INVALID_ARGUMENT;
     }
     pd_run_params r = run;

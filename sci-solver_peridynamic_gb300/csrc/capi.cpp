@@ -78,6 +78,10 @@ pd_status pd_create(const pd_sim_params* sim, const pd_run_params* run, const pd
         g_create_error = "cg_loop 0 (graph) or 1 (host batches), cg_check_interval >= 0";
         return PD_ERR_INVALID_ARGUMENT;
     }
+    if (o.preconditioner < 0 || o.preconditioner > 2) {
+        g_create_error = "preconditioner 0 (none), 1 (diagonal) or 2 (3x3 blocks)";
+        return PD_ERR_INVALID_ARGUMENT;
+    }
     if (o.contact_enabled && !(o.contact_distance > 0 && o.contact_volume > 0)) {
         g_create_error = "contact distance and volume must be positive";
         return PD_ERR_INVALID_ARGUMENT;

@@ -135,8 +135,8 @@ void Engine::free_all()
     hist_free();
     void* ptrs[] = {S_.act, S_.x64, S_.v64, S_.X64, S_.x64_bk, S_.v64_bk, S_.st, S_.ost, S_.nst, S_.row_ptr,
                     S_.cnt, S_.cnt_bk, S_.col, S_.X32, S_.u32, S_.xs4, S_.inv_d0, S_.jac, S_.jdiag, S_.force, S_.rhs, S_.sol,
-                    S_.r, S_.p, S_.y, S_.sc, S_.partials, S_.counters, S_.flags, S_.lidx, S_.d0sq, S_.lim, S_.xlo4, d_perm_,
-                    d_stage_};
+                    S_.r, S_.p, S_.y, S_.z, S_.pc, S_.sc, S_.partials, S_.counters, S_.flags, S_.lidx, S_.d0sq, S_.lim,
+                    S_.xlo4, d_perm_, d_stage_};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     free_tiles(S_);
@@ -188,6 +188,11 @@ pd_status Engine::allocate()
         CK(cudaMemsetAsync(*v, 0, r4 * (n ? n : 1), stream_), "memset vector");
     }
     if (fp64_) CK(dalloc(&S_.jdiag, 6 * n), "alloc jdiag");
+    if (opt_.preconditioner) {   // z and the inverse diagonal blocks (two Real4 per particle)
+        CK(cudaMalloc(&S_.z, r4 * (n ? n : 1)), "alloc z");
+        CK(cudaMemsetAsync(S_.z, 0, r4 * (n ? n : 1), stream_), "memset z");
+        CK(cudaMalloc(&S_.pc, 2 * r4 * (n ? n : 1)), "alloc preconditioner");
+    }
     CK(dalloc(&S_.sc, 1), "alloc scalars");
     CK(dalloc(&S_.partials, 4 * (size_t)kMaxPartials), "alloc partials");
     CK(dalloc(&S_.counters, 8), "alloc counters");
@@ -942,6 +947,12 @@ pd_status Engine::solve(const StepParams& P)
             if (s != PD_OK) return s;
         }
     }
+    if (opt_.preconditioner) {
+        // M from this step's operator, then z = M r and p = z for the final guess
+        launch_pc_build(fp64_, opt_.preconditioner, P, S_, L_, stream_);
+        launch_pcg_start(fp64_, P, S_, L_, stream_);
+        launches_ += 2;
+    }
     // iteration 0 from the host: the sample of the profiled kernel times (a
     // live launch unless the guess had already converged)
     cg_iteration(P, 0, 0, true);
@@ -1001,24 +1012,33 @@ void Engine::cg_iteration(const StepParams& P, int k, cudaGraphConditionalHandle
         // the direction update p = r + beta p is fused into the product, which
         // reads the previous direction from one buffer and writes the new one
         // to the other (buffer 0 = S_.p, set to r by the residual kernel)
+        // (preconditioned: p = z + beta p, from the z buffer)
         void* p_prev = (k & 1) ? d_p2_ : S_.p;
         void* p_new = (k & 1) ? S_.p : d_p2_;
         if (sample) mark_begin(PD_KC_SPMV, k);
         launch_spmv_lattice(true, P, S_, lat_, p_prev, S_.y, ReduceSlot{S_.partials, S_.counters + 1}, S_.sc, nullptr,
-                            S_.r, p_new, stream_);
+                            opt_.preconditioner ? S_.z : S_.r, p_new, stream_);
         if (sample) mark_end();
         DeviceState Sj = S_;
         Sj.p = p_new;
         if (sample) mark_begin(PD_KC_CG_VECTOR, k);
-        launch_cg_axpy(fp64_, P, Sj, L_, stream_, cond);
+        if (opt_.preconditioner) launch_cg_axpy_pc(fp64_, P, Sj, L_, stream_, cond);
+        else launch_cg_axpy(fp64_, P, Sj, L_, stream_, cond);
         if (sample) mark_end();
     } else {
         if (sample) mark_begin(PD_KC_SPMV, k);
         launch_spmv(fp64_, true, P, S_, L_, stream_);
         if (sample) mark_end();
         if (sample) mark_begin(PD_KC_CG_VECTOR, k);
-        launch_cg_axpy(fp64_, P, S_, L_, stream_, cond);
-        launch_cg_xpby(fp64_, P, S_, L_, stream_);
+        if (opt_.preconditioner) {
+            launch_cg_axpy_pc(fp64_, P, S_, L_, stream_, cond);
+            DeviceState Sz = S_;   // p = z + beta p
+            Sz.r = S_.z;
+            launch_cg_xpby(fp64_, P, Sz, L_, stream_);
+        } else {
+            launch_cg_axpy(fp64_, P, S_, L_, stream_, cond);
+            launch_cg_xpby(fp64_, P, S_, L_, stream_);
+        }
         if (sample) mark_end();
     }
 }

@@ -179,6 +179,7 @@ extern "C" pd_status pd_solver_options_default(pd_solver_options* o)
     o->lanes_per_particle = 0;
     o->cg_check_interval = 0;
     o->cg_loop = 0;
+    o->preconditioner = 0;
     return PD_OK;
 }
 

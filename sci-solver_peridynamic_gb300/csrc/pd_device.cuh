@@ -191,4 +191,62 @@ __device__ __forceinline__ void block_reduce_finish(Acc acc, ReduceSlot slot, Fi
     }
 }
 
+// Two sums at once (block partials of the second in partials_b), the same
+// fixed order as block_reduce_finish; fin(total_a, total_b) runs once.
+template <typename Acc, typename Fin>
+__device__ __forceinline__ void block_reduce_finish2(Acc a, Acc b, ReduceSlot slot, double* partials_b, Fin fin)
+{
+    __shared__ double sums_a[kBlock / 32], sums_b[kBlock / 32];
+    __shared__ bool is_last;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    __syncthreads();
+    const double wa = warp_total(a), wb = warp_total(b);
+    if (lane == 0) {
+        sums_a[warp] = wa;
+        sums_b[warp] = wb;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double ta = 0.0, tb = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+            ta += sums_a[i];
+            tb += sums_b[i];
+        }
+        slot.partials[blockIdx.x] = ta;
+        partials_b[blockIdx.x] = tb;
+        __threadfence();
+        const unsigned prev = atomicAdd(slot.counter, 1u);
+        is_last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    double ta = 0.0, tb = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+        ta += ((volatile double*)slot.partials)[i];
+        tb += ((volatile double*)partials_b)[i];
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        ta += __shfl_xor_sync(0xffffffffu, ta, off);
+        tb += __shfl_xor_sync(0xffffffffu, tb, off);
+    }
+    __syncthreads();
+    if (lane == 0) {
+        sums_a[warp] = ta;
+        sums_b[warp] = tb;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double total_a = 0.0, total_b = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+            total_a += sums_a[i];
+            total_b += sums_b[i];
+        }
+        *slot.counter = 0u;
+        fin(total_a, total_b);
+    }
+}
+
 }  // namespace pdgb

@@ -42,6 +42,7 @@ struct CgScalars {
     int done;
     int converged;
     int max_iter;
+    double rr;             // preconditioned CG: <r, r> of the stopping test (rz is then <r, z>)
     double rz_plain;       // <r, r> of the previous-solution guess (learned warm start)
     double rz_learned;     // <r, r> of the learned guess
     int ws_revert;         // 1: the learned guess was worse and was replaced
@@ -132,6 +133,9 @@ struct DeviceState {
     void* r;           // Real4
     void* p;           // Real4
     void* y;           // Real4
+    void* z;           // Real4: preconditioned residual M^-1 r (preconditioner on)
+    void* pc;          // Real4 x 2 per particle: M^-1, the inverse diagonal block of A
+                       // (m00 m11 m22 m01 | m02 m12 0 0)
     CgScalars* sc;
     double* partials;
     unsigned int* counters;  // 8 reduction counters
@@ -231,6 +235,17 @@ void launch_spmv(bool fp64, bool dot, const StepParams& P, const DeviceState& S,
 void launch_operator(bool fp64, const StepParams& P, const DeviceState& S, int lanes, int grid, const void* in,
                      void* out, ReduceSlot slot, double* dot_out, cudaStream_t st);
 void launch_cg_residual(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
+// Preconditioned CG (no reference counterpart in use: the reference's
+// cusp::precond::diagonal is commented out, simulator.cu:767-769): mode 1 =
+// inverse diagonal of A, 2 = inverse 3x3 diagonal blocks; the stopping test
+// stays on the unpreconditioned ||r||.
+void launch_pc_build(bool fp64, int mode, const StepParams& P, const DeviceState& S, const LaunchCfg& L,
+                     cudaStream_t st);
+// z = M^-1 r, p = z, rz = <r, z>, rr = <r, r> (after the residual of the guess)
+void launch_pcg_start(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st);
+// x += alpha p ; r -= alpha A p ; z = M^-1 r ; rr, rz ; beta = rz'/rz ; test
+void launch_cg_axpy_pc(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st,
+                       cudaGraphConditionalHandle cond = 0);
 // cond: the while node's condition handle when launched inside the CG graph, else 0
 void launch_cg_axpy(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st,
                     cudaGraphConditionalHandle cond = 0);

@@ -152,6 +152,119 @@ __global__ void __launch_bounds__(kBlock) k_cg_xpby(StepParams P, DeviceState S)
         xpby_elem<FP64>(S, i, beta);
 }
 
+// ---- preconditioned CG -----------------------------------------------------------
+// FP64: D = m I + t2 jdiag (the bond Jacobians' sum and the contact term, as
+// the product uses them); one thread per particle.
+__global__ void __launch_bounds__(kBlock) k_pc_build64(StepParams P, DeviceState S, int mode)
+{
+    dbl4* pc = (dbl4*)S.pc;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x) {
+        double M[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        if (!is_dirichlet(S.act[i] & kActMask)) {
+            const double* J = S.jdiag + 6ll * i;
+            const double D[6] = {P.mass + P.t2 * J[0], P.mass + P.t2 * J[1], P.mass + P.t2 * J[2],
+                                 P.t2 * J[3], P.t2 * J[4], P.t2 * J[5]};
+            pc_invert(mode, P.mass, D, M);
+        }
+        pc[2 * i] = make_dbl4(M[0], M[1], M[2], M[3]);
+        pc[2 * i + 1] = make_dbl4(M[4], M[5], 0.0, 0.0);
+    }
+}
+
+// Mixed precision: D = m I + t2 (c sum_q [(1/d0 - 1/d) I + xi xi^T / d^3] + k n n^T)
+// over the particle's live bonds (the product's bond term, from the same
+// supercell positions), G lanes per particle.
+template <int G>
+__global__ void __launch_bounds__(kBlock) k_pc_build32(StepParams P, DeviceState S, int mode)
+{
+    const unsigned gmask = group_mask<G>();
+    const int lane = threadIdx.x & (G - 1);
+    const int groups = gridDim.x * (kBlock / G);
+    float4* pc = (float4*)S.pc;
+    const float sup = (float)P.sup;
+    for (int p = blockIdx.x * (kBlock / G) + threadIdx.x / G; p < P.n; p += groups) {
+        const uint8_t ab = S.act[p];
+        if (is_dirichlet(ab & kActMask)) {
+            if (lane == 0) {
+                pc[2 * p] = make_float4(0.f, 0.f, 0.f, 0.f);
+                pc[2 * p + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            continue;
+        }
+        const float4 xp4 = S.xs4[p];
+        const int wp = __float_as_int(xp4.w);
+        const int rs = S.row_ptr[p];
+        const int cn = S.cnt[p];
+        float sa = 0.f, sxx = 0.f, syy = 0.f, szz = 0.f, sxy = 0.f, sxz = 0.f, syz = 0.f;
+        for (int j = lane; j < cn; j += G) {
+            const int q = S.col[rs + j];
+            const float4 Xq = S.xs4[q];
+            float cx, cy, cz;
+            supercell_delta(__float_as_int(Xq.w), wp, sup, cx, cy, cz);
+            const float xs = (Xq.x - xp4.x) + cx, ys = (Xq.y - xp4.y) + cy, zs = (Xq.z - xp4.z) + cz;
+            const float inv_d = rsqrtf(fmaf(xs, xs, fmaf(ys, ys, zs * zs)));
+            const float i3 = inv_d * inv_d * inv_d;
+            sa += S.inv_d0[rs + j] - inv_d;
+            sxx = fmaf(xs * xs, i3, sxx); syy = fmaf(ys * ys, i3, syy); szz = fmaf(zs * zs, i3, szz);
+            sxy = fmaf(xs * ys, i3, sxy); sxz = fmaf(xs * zs, i3, sxz); syz = fmaf(ys * zs, i3, syz);
+        }
+        sa = group_sum<G>(sa, gmask);
+        sxx = group_sum<G>(sxx, gmask); syy = group_sum<G>(syy, gmask); szz = group_sum<G>(szz, gmask);
+        sxy = group_sum<G>(sxy, gmask); sxz = group_sum<G>(sxz, gmask); syz = group_sum<G>(syz, gmask);
+        if (lane != 0) continue;
+        const double c = P.bond_coeff, t2 = P.t2, m = P.mass;
+        double D[6] = {m + t2 * c * ((double)sa + sxx), m + t2 * c * ((double)sa + syy),
+                       m + t2 * c * ((double)sa + szz), t2 * c * sxy, t2 * c * sxz, t2 * c * syz};
+        if (ab & kActContact) {
+            const float4 Xp = S.X32[p];
+            const float4 Up = S.u32[p];
+            const double dx = (double)(Xp.x + Up.x) - P.sphere_c_local[0];
+            const double dy = (double)(Xp.y + Up.y) - P.sphere_c_local[1];
+            const double dz = (double)(Xp.z + Up.z) - P.sphere_c_local[2];
+            const double inv = 1.0 / sqrt(dx * dx + dy * dy + dz * dz);
+            const double nx = dx * inv, ny = dy * inv, nz = dz * inv, k = t2 * P.sphere_k;
+            D[0] += k * nx * nx; D[1] += k * ny * ny; D[2] += k * nz * nz;
+            D[3] += k * nx * ny; D[4] += k * nx * nz; D[5] += k * ny * nz;
+        }
+        double M[6];
+        pc_invert(mode, m, D, M);
+        pc[2 * p] = make_float4((float)M[0], (float)M[1], (float)M[2], (float)M[3]);
+        pc[2 * p + 1] = make_float4((float)M[4], (float)M[5], 0.f, 0.f);
+    }
+}
+
+template <bool FP64>
+__global__ void __launch_bounds__(kBlock) k_pcg_start(StepParams P, DeviceState S, ReduceSlot slot, double* partials_b)
+{
+    using Real = typename std::conditional<FP64, double, float>::type;
+    typename DotAccFor<Real>::type rr, rz;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x)
+        pcg_start_elem<FP64>(S, i, rr, rz);
+    CgScalars* sc = S.sc;
+    block_reduce_finish2(rr, rz, slot, partials_b, [sc](double a, double b) { cg_fin_pcg_start(sc, a, b); });
+}
+
+// as k_cg_axpy (the graph's condition included), with z = M r and <r, z>
+template <bool FP64>
+__global__ void __launch_bounds__(kBlock) k_cg_axpy_pc(StepParams P, DeviceState S, ReduceSlot slot,
+                                                      double* partials_b, cudaGraphConditionalHandle cond)
+{
+    using Real = typename std::conditional<FP64, double, float>::type;
+    CgScalars* sc = S.sc;
+    if (((volatile CgScalars*)sc)->done) {
+        if (cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond, 0u);
+        return;
+    }
+    const Real alpha = (Real)sc->alpha;
+    typename DotAccFor<Real>::type rr, rz;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x)
+        axpy_pc_elem<FP64>(S, i, alpha, rr, rz);
+    block_reduce_finish2(rr, rz, slot, partials_b, [sc, cond](double a, double b) {
+        cg_fin_axpy_pc(sc, a, b);
+        if (cond) cudaGraphSetConditional(cond, sc->done ? 0u : 1u);
+    });
+}
+
 // ---- position / velocity update ------------------------------------------------
 template <bool FP64>
 __global__ void __launch_bounds__(kBlock) k_update(StepParams P, DeviceState S)
@@ -343,6 +456,26 @@ void launch_cg_axpy(bool fp64, const StepParams& P, const DeviceState& S, const 
 {
     if (fp64) k_cg_axpy<true><<<L.grid_vec, kBlock, 0, st>>>(P, S, slot_of(S, 3), cond);
     else k_cg_axpy<false><<<L.grid_vec, kBlock, 0, st>>>(P, S, slot_of(S, 3), cond);
+}
+
+void launch_pc_build(bool fp64, int mode, const StepParams& P, const DeviceState& S, const LaunchCfg& L,
+                     cudaStream_t st)
+{
+    if (fp64) k_pc_build64<<<L.grid_vec, kBlock, 0, st>>>(P, S, mode);
+    else k_pc_build32<8><<<L.grid_vec, kBlock, 0, st>>>(P, S, mode);
+}
+
+void launch_pcg_start(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st)
+{
+    if (fp64) k_pcg_start<true><<<L.grid_vec, kBlock, 0, st>>>(P, S, slot_of(S, 2), S.partials + kMaxPartials);
+    else k_pcg_start<false><<<L.grid_vec, kBlock, 0, st>>>(P, S, slot_of(S, 2), S.partials + kMaxPartials);
+}
+
+void launch_cg_axpy_pc(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st,
+                       cudaGraphConditionalHandle cond)
+{
+    if (fp64) k_cg_axpy_pc<true><<<L.grid_vec, kBlock, 0, st>>>(P, S, slot_of(S, 3), S.partials + kMaxPartials, cond);
+    else k_cg_axpy_pc<false><<<L.grid_vec, kBlock, 0, st>>>(P, S, slot_of(S, 3), S.partials + kMaxPartials, cond);
 }
 
 void launch_cg_xpby(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st)

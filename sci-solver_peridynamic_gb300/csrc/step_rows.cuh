@@ -834,6 +834,108 @@ __device__ __forceinline__ void cg_fin_axpy(CgScalars* sc, double rr)
     }
 }
 
+// ---- preconditioner ---------------------------------------------------------------
+// M = D^-1 from the symmetric diagonal block D = (xx yy zz xy xz yz) of A:
+// mode 2 inverts the block (adjugate over determinant) where it is positive
+// definite, mode 1 -- and mode 2 elsewhere -- inverts its diagonal; a
+// non-positive diagonal entry takes 1 / mass.
+__device__ __forceinline__ void pc_invert(int mode, double mass, const double (&D)[6], double (&M)[6])
+{
+    const double a = D[0], b = D[1], c = D[2], d = D[3], e = D[4], f = D[5];
+    if (mode == 2) {
+        const double c00 = b * c - f * f, c11 = a * c - e * e, c22 = a * b - d * d;
+        const double c01 = e * f - d * c, c02 = d * f - b * e, c12 = d * e - a * f;
+        const double det = a * c00 + d * c01 + e * c02;
+        if (a > 0.0 && c22 > 0.0 && det > 0.0) {
+            const double id = 1.0 / det;
+            M[0] = c00 * id; M[1] = c11 * id; M[2] = c22 * id;
+            M[3] = c01 * id; M[4] = c02 * id; M[5] = c12 * id;
+            return;
+        }
+    }
+    const double im = 1.0 / mass;
+    M[0] = a > 0.0 ? 1.0 / a : im;
+    M[1] = b > 0.0 ? 1.0 / b : im;
+    M[2] = c > 0.0 ? 1.0 / c : im;
+    M[3] = M[4] = M[5] = 0.0;
+}
+
+template <typename V4>
+__device__ __forceinline__ V4 pc_apply(const V4* __restrict__ pc, int i, const V4& r)
+{
+    const V4 m0 = pc[2 * i], m1 = pc[2 * i + 1];
+    V4 z;
+    z.x = m0.x * r.x + m0.w * r.y + m1.x * r.z;
+    z.y = m0.w * r.x + m0.y * r.y + m1.y * r.z;
+    z.z = m1.x * r.x + m1.y * r.y + m0.z * r.z;
+    z.w = 0;
+    return z;
+}
+
+// z = M r, p = z; rr += <r, r>, rz += <r, z>
+template <bool FP64, typename Acc>
+__device__ __forceinline__ void pcg_start_elem(const DeviceState& S, int i, Acc& rr, Acc& rz)
+{
+    using Real = typename std::conditional<FP64, double, float>::type;
+    using V4 = typename Vec4<Real>::type;
+    const V4 ri = ((const V4*)S.r)[i];
+    const V4 zi = pc_apply((const V4*)S.pc, i, ri);
+    ((V4*)S.z)[i] = zi;
+    ((V4*)S.p)[i] = zi;
+    rr.fma(ri.x, ri.x); rr.fma(ri.y, ri.y); rr.fma(ri.z, ri.z);
+    rz.fma(ri.x, zi.x); rz.fma(ri.y, zi.y); rz.fma(ri.z, zi.z);
+}
+
+// x += alpha p ; r -= alpha A p ; z = M r ; rr += <r, r>, rz += <r, z>
+template <bool FP64, typename Real, typename Acc>
+__device__ __forceinline__ void axpy_pc_elem(const DeviceState& S, int i, Real alpha, Acc& rr, Acc& rz)
+{
+    using V4 = typename Vec4<Real>::type;
+    V4* x = (V4*)S.sol;
+    V4* r = (V4*)S.r;
+    const V4 pi = ((const V4*)S.p)[i], yi = ((const V4*)S.y)[i];
+    V4 xi = x[i], ri = r[i];
+    xi.x += alpha * pi.x; xi.y += alpha * pi.y; xi.z += alpha * pi.z;
+    ri.x -= alpha * yi.x; ri.y -= alpha * yi.y; ri.z -= alpha * yi.z;
+    x[i] = xi;
+    r[i] = ri;
+    const V4 zi = pc_apply((const V4*)S.pc, i, ri);
+    ((V4*)S.z)[i] = zi;
+    rr.fma(ri.x, ri.x); rr.fma(ri.y, ri.y); rr.fma(ri.z, ri.z);
+    rz.fma(ri.x, zi.x); rz.fma(ri.y, zi.y); rz.fma(ri.z, zi.z);
+}
+
+// rho = <r, z> for the direction, ||r|| for the test (as the plain CG)
+__device__ __forceinline__ void cg_fin_pcg_start(CgScalars* sc, double rr, double rz)
+{
+    sc->rr = rr;
+    sc->rz = rz;
+    sc->beta = 0.0;
+    sc->rnorm = sqrt(rr);
+    if (sc->rnorm <= sc->tol) {
+        sc->done = 1;
+        sc->converged = 1;
+    } else if (sc->iter >= sc->max_iter) {
+        sc->done = 1;
+    }
+}
+
+__device__ __forceinline__ void cg_fin_axpy_pc(CgScalars* sc, double rr, double rz)
+{
+    const double rz_old = sc->rz;
+    sc->rr = rr;
+    sc->rz = rz;
+    sc->beta = rz / rz_old;
+    sc->iter += 1;
+    sc->rnorm = sqrt(rr);
+    if (sc->rnorm <= sc->tol) {
+        sc->done = 1;
+        sc->converged = 1;
+    } else if (sc->iter >= sc->max_iter) {
+        sc->done = 1;
+    }
+}
+
 // ---- position / velocity update ------------------------------------------------
 // box reflection of updatePDPosition* (implicit_euler.cuh:116-168), FP64, same order
 __device__ __forceinline__ void reflect(const StepParams& P, double& np, double& nv, int k)

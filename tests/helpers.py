@@ -44,6 +44,7 @@ def oracle_params(scene):
     p.contact_dist = opt.contact_distance
     p.contact_k = opt.contact_stiffness
     p.contact_vol = opt.contact_volume
+    p.precond = opt.preconditioner
     return p
 
 

@@ -152,6 +152,16 @@ def test_invalid_warm_start_rejected(pdgb, scenes, field, value):
     assert "warm_start" in str(e.value)
 
 
+@pytest.mark.parametrize("field,value", [("preconditioner", 3), ("preconditioner", -1)])
+def test_invalid_preconditioner_rejected(pdgb, scenes, field, value):
+    sc = scenes.reference_block(n_side=3)
+    setattr(sc.opt, field, value)
+    with pytest.raises(pdgb.PdError) as e:
+        scenes.make_simulator(sc)
+    assert e.value.status == 1
+    assert "preconditioner" in str(e.value)
+
+
 @pytest.mark.parametrize("field,value", [("cg_loop", 2), ("cg_loop", -1), ("cg_check_interval", -3)])
 def test_invalid_cg_loop_rejected(pdgb, scenes, field, value):
     sc = scenes.reference_block(n_side=3)
