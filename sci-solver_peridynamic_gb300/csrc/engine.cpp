@@ -362,6 +362,10 @@ pd_status Engine::make_ready()
     if (!fp64_ && n > 0) {   // supercell positions of the initial state (read by the SpMV)
         launch_refresh(fp64_, step_params(), S_, L_, stream_);
         ++launches_;
+        if (lat_ok_) {   // and the lattice product's deviations (its candidates are timed next)
+            launch_lattice_delta(S_, lat_, sup_, stream_);
+            ++launches_;
+        }
     }
     s = tune_spmv();
     if (s != PD_OK) return s;
@@ -878,7 +882,7 @@ pd_status Engine::integrate(bool* advanced)
     mark_begin(PD_KC_FORCE, -1);
     launch_force(fp64_, Pf, S_, L_, stream_);
     mark_end();
-    launches_ += fp64_ ? 1 : 2;   // mixed: the supercell words, then the pass
+    launches_ += fp64_ ? 1 : (L_.lattice ? 3 : 2);   // mixed: the supercell words (+ lattice deviations), the pass
     lattice_resync(false);        // only where the pass broke a bond (read on the device)
     const bool adaptive = run_.integrator == PD_NEWMARK_BETA || run_.adaptive_integration != 0;
     if (adaptive) {
@@ -894,7 +898,7 @@ pd_status Engine::integrate(bool* advanced)
             CK(cudaMemcpyAsync(S_.x64, S_.x64_bk, sizeof(dbl4) * N, cudaMemcpyDeviceToDevice, stream_), "restore x");
             CK(cudaMemcpyAsync(S_.v64, S_.v64_bk, sizeof(dbl4) * N, cudaMemcpyDeviceToDevice, stream_), "restore v");
             launch_refresh(fp64_, Pf, S_, L_, stream_);
-            ++launches_;
+            launches_ += L_.lattice ? 2 : 1;
             lattice_resync(true);   // the restored live sets
             return PD_OK;
         }

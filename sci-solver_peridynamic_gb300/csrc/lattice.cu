@@ -10,7 +10,7 @@
 // small stencil (80 offsets for a horizon of 2.5 spacings).  The slots are
 // renumbered brick by brick (bricks of 32 x 4 x bz sites, x fastest), and the
 // product runs one brick per block iteration: the block stages the halo of
-// the brick's sites (the neighbours' supercell positions and their entries of
+// the brick's sites (each particle's deviation from its site and its entry of
 // w) in shared memory, then each thread walks its row's stencil.  Rows of a
 // warp are x-consecutive sites, so the neighbours at one stencil entry are
 // x-consecutive shared-memory words (no bank conflicts), and the only per-bond
@@ -18,10 +18,11 @@
 // (stored scaled by 2^100, see kLatScale).
 //
 // The per-bond arithmetic is the gather product's (step_rows.cuh,
-// mixed_bond_chunk): the bond vector is rebuilt from the same supercell words,
-// the Jacobian applied to w_p - w_q is
+// mixed_bond_chunk): the Jacobian applied to w_p - w_q is
 //   c [ (1/d0 - 1/d) (w_p - w_q) + (xi . (w_p - w_q)) xi / d^3 ],
-// and only the order of the per-row sum differs.
+// with the bond vector xi = h v_k + (d_q - d_p) from the stencil offset v_k
+// and the two deviations d from the lattice sites (per step, FP64 rounded
+// once to FP32 within half a supercell), in pairs of FP32 lanes (f32x2).
 #include <algorithm>
 #include <climits>
 #include <cmath>
@@ -41,15 +42,16 @@ namespace {
 
 constexpr int kLatBX = 32;
 constexpr int kLatBY = 4;
-constexpr float kLatEmpty = 1.0e4f;   // supercell offset of an empty site (any far, finite position)
+constexpr float kLatEmpty = 1.0e4f;   // deviation of an empty site (any far, finite position)
 // The table holds 2^100 / d0: then min(1/d, entry) is 1/d for a live bond (its
 // entry is near 1e31 or more) and 0 for "no bond" (entry 0), one instruction,
 // and 1/d0 - 1/d = fma(entry, 2^-100, -1/d) is exact scaling by a power of two.
 constexpr float kLatScale = 1.2676506002282294e30f;     // 2^100
 constexpr float kLatUnscale = 7.888609052210118e-31f;   // 2^-100
-// the largest halo: R = 3, bricks of 32 x 4 x 2 sites -> 38 x 10 x 8 sites of 36 bytes
+// the largest halo: R = 3, bricks of 32 x 4 x 2 sites -> 38 x 10 x 8 sites of 24 bytes
 constexpr int kLatHaloMax = 38 * 10 * 8;
-constexpr int kLatSmemMax = kLatHaloMax * 36;
+constexpr int kLatSiteBytes = sizeof(float4) + sizeof(float2);
+constexpr int kLatSmemMax = kLatHaloMax * kLatSiteBytes;
 constexpr int kLatHaloPerThread = (kLatHaloMax + kBlock - 1) / kBlock;
 
 // The stencil of a horizon of 2.5 spacings (the benchmark's 5 r): every lattice
@@ -61,6 +63,7 @@ constexpr int kS80 = 80;
 constexpr int kS80Hx = kLatBX + 4, kS80Hy = kLatBY + 4, kS80Hz = 4 + 4;
 struct Stencil80 {
     int off[kS80];
+    int dx[kS80], dy[kS80], dz[kS80];
 };
 __host__ __device__ constexpr bool in_s80(int dx, int dy, int dz)
 {
@@ -74,7 +77,13 @@ __host__ __device__ constexpr Stencil80 make_stencil80()
     for (int dz = -2; dz <= 2; ++dz)
         for (int dy = -2; dy <= 2; ++dy)
             for (int dx = -2; dx <= 2; ++dx)
-                if (in_s80(dx, dy, dz)) t.off[k++] = (dz * kS80Hy + dy) * kS80Hx + dx;
+                if (in_s80(dx, dy, dz)) {
+                    t.off[k] = (dz * kS80Hy + dy) * kS80Hx + dx;
+                    t.dx[k] = dx;
+                    t.dy[k] = dy;
+                    t.dz[k] = dz;
+                    ++k;
+                }
     return t;
 }
 __host__ __device__ constexpr int count_s80()
@@ -277,9 +286,39 @@ __global__ void __launch_bounds__(kBlock) k_lat_ell(DeviceState S, LatticeParams
     }
 }
 
+// ---- deviations from the lattice sites ------------------------------------------------
+// dl[i] = (d, n): x - (org + h site) = d + sup n per axis with n = rint(. / sup)
+// (FP64, exact: sup is a power of two), d rounded once to FP32; n packed in
+// 10 bits per axis (+512).  |n| stays below 512 for displacements below
+// 500 supercells; larger ones are clamped (the deviation then loses digits).
+__global__ void __launch_bounds__(kBlock) k_lat_delta(const dbl4* __restrict__ x64, int n, LatticeParams lp,
+                                                      double sup, float4* __restrict__ dl)
+{
+    const double inv_sup = 1.0 / sup;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const dbl4 x = x64[i];
+        const int4 s = lp.site[i];
+        const double dev[3] = {x.x - (lp.org[0] + lp.h * s.x), x.y - (lp.org[1] + lp.h * s.y),
+                               x.z - (lp.org[2] + lp.h * s.z)};
+        float d[3];
+        int packed = 0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const double m = fmin(fmax(rint(dev[k] * inv_sup), -511.0), 511.0);
+            d[k] = (float)(dev[k] - m * sup);
+            packed |= ((int)m + 512) << (10 * k);
+        }
+        dl[i] = make_float4(d[0], d[1], d[2], __int_as_float(packed));
+    }
+}
+
 // ---- the product -----------------------------------------------------------------------
-// Shared memory per halo site: A = (supercell offset x, y, z, sup * i),
-// B = (sup * j, sup * k, w.x, w.y), W = w.z (36 bytes).
+// Shared memory per halo site: A = (d.x, d.y, w.x, w.y), B = (d.z, w.z)
+// (24 bytes), d the site particle's deviation re-referenced to the brick:
+// d + sup (n - n_brick), n_brick the wrap counts of the brick's first slot
+// (within a brick's halo they differ by at most one for any strain a bond
+// survives, so |d| stays within 1.5 sup).  Entry k's bond vector is then
+// xi = h v_k + (d_q - d_p), formed in FP32 pairs with the differences of w.
 //
 // Blocks take bricks from a counter (lp.sched[0]) in brick order, so that
 // bricks of uneven fill balance over the blocks; the last block to finish
@@ -292,8 +331,15 @@ __global__ void __launch_bounds__(kBlock) k_lat_ell(DeviceState S, LatticeParams
 // iteration, which cg_fin_residual sets), and each brick writes its rows' new
 // direction to p_out (p_prev and p_out are different buffers, so blocks that
 // still stage halos read the old direction).
+__device__ __forceinline__ float wrap_delta(int nq, int nb, int shift, float sup)
+{
+    return sup * small_int_to_float(((nq >> shift) & 1023) - ((nb >> shift) & 1023));
+}
+
+// Three blocks per SM (80 registers, a 55 KB halo each): at 1M particles 173 us
+// per product against 184 at two blocks (128 registers) and 178 at four (64).
 template <bool DOT, bool FIXED, bool FUSE>
-__global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, DeviceState S, LatticeParams lp,
+__global__ void __launch_bounds__(kBlock, 3) k_spmv_lattice(StepParams P, DeviceState S, LatticeParams lp,
                                                            const float4* __restrict__ in, float4* __restrict__ out,
                                                            ReduceSlot slot, CgScalars* cg, double* dot_out,
                                                            const float4* __restrict__ r_in, float4* __restrict__ p_out)
@@ -303,13 +349,13 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
     __shared__ int s_next;
     const int H = FIXED ? kS80Hx * kS80Hy * kS80Hz : lp.hx * lp.hy * lp.hz;
     float4* sA = lat_smem;
-    float4* sB = sA + H;
-    float* sW = (float*)(sB + H);
+    float2* sB = (float2*)(sA + H);
     const float sup = (float)P.sup;
     const int hx = FIXED ? kS80Hx : lp.hx, hxy = FIXED ? kS80Hx * kS80Hy : lp.hx * lp.hy;
     const int mx = lp.map_dim[0], mxy = lp.map_dim[0] * lp.map_dim[1];
     const int K = FIXED ? kS80 : lp.K;
     const float beta = FUSE ? (float)((volatile CgScalars*)cg)->beta : 0.f;
+    const float2 m1 = make_float2(-1.f, -1.f);
     DotAcc32 acc;
     if (threadIdx.x == 0) {
         s_next = (int)atomicAdd(&lp.sched[0], 1u);
@@ -324,8 +370,9 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
         const int corner = lp.brick_corner[b];
         const int start = lp.brick_start[b];
         const int rows = lp.brick_start[b + 1] - start;
+        const int nb = __float_as_int(__ldg(&lp.dl[start].w));
         // the map entries of this thread's halo sites first (independent
-        // loads), then their positions and w entries
+        // loads), then their deviations and w entries
         int qs[kLatHaloPerThread];
 #pragma unroll
         for (int t = 0; t < kLatHaloPerThread; ++t) {
@@ -344,10 +391,10 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
             const int h = threadIdx.x + t * kBlock;
             if (h >= H) continue;
             const int q = qs[t];
-            float4 a = make_float4(kLatEmpty, kLatEmpty, kLatEmpty, 0.f), bb = make_float4(0.f, 0.f, 0.f, 0.f);
-            float wz = 0.f;
+            float4 a = make_float4(kLatEmpty, kLatEmpty, 0.f, 0.f);
+            float2 bb = make_float2(kLatEmpty, 0.f);
             if (q >= 0) {
-                const float4 x = __ldg(S.xs4 + q);
+                const float4 dq = __ldg(lp.dl + q);
                 float4 w = __ldg(in + q);
                 if (FUSE) {   // xpby_elem: p = r + beta p
                     const float4 r = __ldg(r_in + q);
@@ -355,15 +402,12 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
                     w.y = r.y + beta * w.y;
                     w.z = r.z + beta * w.z;
                 }
-                const int wq = __float_as_int(x.w);
-                a = make_float4(x.x, x.y, x.z, sup * small_int_to_float(wq & 1023));
-                bb = make_float4(sup * small_int_to_float((wq >> 10) & 1023), sup * small_int_to_float((wq >> 20) & 1023),
-                                 w.x, w.y);
-                wz = w.z;
+                const int nq = __float_as_int(dq.w);
+                a = make_float4(dq.x + wrap_delta(nq, nb, 0, sup), dq.y + wrap_delta(nq, nb, 10, sup), w.x, w.y);
+                bb = make_float2(dq.z + wrap_delta(nq, nb, 20, sup), w.z);
             }
             sA[h] = a;
             sB[h] = bb;
-            sW[h] = wz;
         }
         __syncthreads();   // halo staged; every thread has read s_next
         if (threadIdx.x == 0) {
@@ -377,34 +421,49 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
             const int p = start + l;
             const uint8_t ab = S.act[p];
             const int c = lp.row_local[p];
-            const float4 pa = sA[c], pb = sB[c];
-            const float4 w = make_float4(pb.z, pb.w, sW[c], 0.f);
+            const float4 pa = sA[c];
+            const float2 pb = sB[c];
+            const float4 w = make_float4(pa.z, pa.w, pb.y, 0.f);
             if (FUSE) p_out[p] = w;
             if (is_dirichlet(ab & kActMask)) {
                 out[p] = make_float4(0.f, 0.f, 0.f, 0.f);
                 continue;
             }
+            const float2 pd = make_float2(pa.x, pa.y), pw = make_float2(pa.z, pa.w);
             // this row's 1/d0 stream: 16 bytes (4 stencil entries) per load
             const float4* __restrict__ e4 = (const float4*)(lp.ell + (size_t)K * start) + l;
-            float ax = 0.f, ay = 0.f, az = 0.f;
+            // sums of a1 (w_q - w_p) + g xi with g = xi . (w_q - w_p) / d^3: the
+            // row's term with the sign of w_q - w_p, negated at the end
+            float2 sxy = make_float2(0.f, 0.f);
+            float sz = 0.f;
             constexpr Stencil80 s80 = make_stencil80();
             const auto bond = [&](int k, float s) {
                 const int q = c + (FIXED ? s80.off[k] : lp.off[k]);
-                const float4 qa = sA[q], qb = sB[q];
-                const float qwz = sW[q];
-                // (X_q - X_p) + sup (ijk_q - ijk_p): the gather product's bond vector
-                const float xs = (qa.x - pa.x) + (qa.w - pa.w);
-                const float ys = (qa.y - pa.y) + (qb.x - pb.x);
-                const float zs = (qa.z - pa.z) + (qb.y - pb.y);
-                const float wx = w.x - qb.z, wy = w.y - qb.w, wz = w.z - qwz;
-                float inv_d = rsqrt_ftz(fmaf(xs, xs, fmaf(ys, ys, zs * zs)));
+                const float4 qa = sA[q];
+                const float2 qb = sB[q];
+                float2 xy = __ffma2_rn(pd, m1, make_float2(qa.x, qa.y));    // d_q - d_p
+                const float2 wxy = __ffma2_rn(pw, m1, make_float2(qa.z, qa.w));   // w_q - w_p
+                const float2 zz = __ffma2_rn(pb, m1, qb);                        // (d_q - d_p, w_q - w_p).z
+                float zs = zz.x;
+                if (FIXED) {   // h v_k: compile-time zeros drop out
+                    if (s80.dx[k] != 0) xy.x += lp.cx[k];
+                    if (s80.dy[k] != 0) xy.y += lp.cy[k];
+                    if (s80.dz[k] != 0) zs += lp.cz[k];
+                } else {
+                    xy.x += lp.cx[k];
+                    xy.y += lp.cy[k];
+                    zs += lp.cz[k];
+                }
+                const float2 sq = __fmul2_rn(xy, xy);
+                float inv_d = rsqrt_ftz(fmaf(zs, zs, sq.x + sq.y));
                 inv_d = fminf(inv_d, s);   // no live bond (s = 0): the term vanishes
                 const float a1 = fmaf(s, kLatUnscale, -inv_d);
-                const float g = fmaf(xs, wx, fmaf(ys, wy, zs * wz)) * (inv_d * inv_d * inv_d);
-                ax = fmaf(a1, wx, fmaf(g, xs, ax));
-                ay = fmaf(a1, wy, fmaf(g, ys, ay));
-                az = fmaf(a1, wz, fmaf(g, zs, az));
+                const float2 t = __fmul2_rn(xy, wxy);
+                const float g = fmaf(zs, zz.y, t.x + t.y) * (inv_d * inv_d * inv_d);
+                sxy = __ffma2_rn(make_float2(a1, a1), wxy, __ffma2_rn(make_float2(g, g), xy, sxy));
+                sz = fmaf(a1, zz.y, fmaf(g, zs, sz));
             };
+            // (loading each table chunk one chunk ahead measured slower: 181 against 173 us)
             if constexpr (FIXED) {
 #pragma unroll
                 for (int k4 = 0; k4 < kS80 / 4; ++k4) {
@@ -424,7 +483,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
                     bond(4 * k4 + 3, s4.w);
                 }
             }
-            spmv_finish_mixed<1, DOT>(P, S, p, ab, w, ax, ay, az, 0, 0xffffffffu, out, acc);
+            spmv_finish_mixed<1, DOT>(P, S, p, ab, w, -sxy.x, -sxy.y, -sz, 0, 0xffffffffu, out, acc);
         }
         __syncthreads();   // the rows are done with the halo; s_next is visible
         b = s_next;
@@ -449,7 +508,12 @@ __global__ void __launch_bounds__(kBlock, 2) k_spmv_lattice(StepParams P, Device
 
 size_t lattice_smem_bytes(const LatticeParams& lp)
 {
-    return (size_t)lp.hx * lp.hy * lp.hz * (2 * sizeof(float4) + sizeof(float));
+    return (size_t)lp.hx * lp.hy * lp.hz * kLatSiteBytes;
+}
+
+void launch_lattice_delta(const DeviceState& S, const LatticeParams& lp, double sup, cudaStream_t st)
+{
+    if (S.n > 0 && lp.dl) k_lat_delta<<<blocks_for(S.n), kBlock, 0, st>>>(S.x64, S.n, lp, sup, lp.dl);
 }
 
 template <bool FIXED>
@@ -521,6 +585,7 @@ void lattice_free(LatticeBuffers* lb)
     cudaFree(lb->map);
     cudaFree(lb->offk);
     cudaFree(lb->ell);
+    cudaFree(lb->dl);
     cudaFree(lb->sched);
     *lb = LatticeBuffers{};
 }
@@ -606,8 +671,18 @@ cudaError_t lattice_build(int n, double spacing, dbl4* x64, float4* X32, int* pe
     L.hx = L.bx + 2 * R;
     L.hy = L.by + 2 * R;
     L.hz = L.bz + 2 * R;
-    for (int k = 0; k < L.K; ++k)
-        L.off[k] = k < (int)sten.size() ? (sten[k].z * L.hy + sten[k].y) * L.hx + sten[k].x : 0;
+    for (int k = 0; k < L.K; ++k) {
+        const int3 v = k < (int)sten.size() ? sten[k] : make_int3(0, 0, 0);
+        L.off[k] = (v.z * L.hy + v.y) * L.hx + v.x;
+        L.cx[k] = (float)(spacing * v.x);
+        L.cy[k] = (float)(spacing * v.y);
+        L.cz[k] = (float)(spacing * v.z);
+    }
+    // site s (from the minimum site) lies at anchor + h (s + min)
+    L.h = spacing;
+    L.org[0] = anchor.x + spacing * ext[0];
+    L.org[1] = anchor.y + spacing * ext[1];
+    L.org[2] = anchor.z + spacing * ext[2];
     const long long D[3] = {(long long)ext[3] - ext[0] + 1, (long long)ext[4] - ext[1] + 1,
                             (long long)ext[5] - ext[2] + 1};
     const long long NB[3] = {(D[0] + L.bx - 1) / L.bx, (D[1] + L.by - 1) / L.by, (D[2] + L.bz - 1) / L.bz};
@@ -683,6 +758,8 @@ cudaError_t lattice_build(int n, double spacing, dbl4* x64, float4* X32, int* pe
     LT_TRY(cudaMalloc(&t.lb.map, sizeof(int) * (size_t)map_size));
     LT_TRY(cudaMalloc(&t.lb.offk, sizeof(int) * offk.size()));
     LT_TRY(cudaMalloc(&t.lb.ell, sizeof(float) * (size_t)L.K * (size_t)n));
+    LT_TRY(cudaMalloc(&t.lb.dl, sizeof(float4) * (size_t)n));
+    LT_TRY(cudaMemsetAsync(t.lb.dl, 0, sizeof(float4) * (size_t)n, st));
     LT_TRY(cudaMalloc(&t.lb.sched, sizeof(unsigned) * 2));
     LT_TRY(cudaMemsetAsync(t.lb.sched, 0, sizeof(unsigned) * 2, st));
     LT_TRY(cudaMemcpyAsync(t.lb.brick_start, bstart.data(), sizeof(int) * bstart.size(), cudaMemcpyHostToDevice, st));
@@ -702,6 +779,7 @@ cudaError_t lattice_build(int n, double spacing, dbl4* x64, float4* X32, int* pe
     L.map = t.lb.map;
     L.offk = t.lb.offk;
     L.ell = t.lb.ell;
+    L.dl = t.lb.dl;
     L.sched = t.lb.sched;
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);

@@ -177,7 +177,12 @@ struct LatticeParams {
     unsigned* sched;          // [0] next brick, [1] blocks finished (zero between launches)
     float* ell;               // K per row, brick-major, in chunks of 4 entries:
                               // [K * start_b + (k / 4) * 4 rows_b + 4 l + k % 4]
+    float4* dl;               // n, per step: the particle's deviation from its site, x - (org + h site)
+                              // = d + sup n (|d| <= sup / 2 per axis): (d.x, d.y, d.z, packed n + 512)
+    double org[3];            // position of site (0, 0, 0)
+    double h;                 // lattice spacing
     int off[kLatMaxK];        // halo index offset of each stencil entry
+    float cx[kLatMaxK], cy[kLatMaxK], cz[kLatMaxK];   // h * (lattice offset) of each stencil entry
 };
 
 struct LatticeBuffers {       // device allocations owned by the engine
@@ -189,6 +194,7 @@ struct LatticeBuffers {       // device allocations owned by the engine
     int* map = nullptr;
     int* offk = nullptr;
     float* ell = nullptr;
+    float4* dl = nullptr;
     unsigned* sched = nullptr;
 };
 
@@ -222,6 +228,9 @@ void launch_lattice_ell(const DeviceState& S, const LatticeParams& lp, int force
 void launch_spmv_lattice(bool dot, const StepParams& P, const DeviceState& S, const LatticeParams& lp,
                          const void* in, void* out, ReduceSlot slot, CgScalars* cg, double* dot_out,
                          const void* r_in, void* p_out, cudaStream_t st);
+// lp.dl from the positions x64 (with the supercell edge sup): after every
+// change of the positions the product's operator is taken at
+void launch_lattice_delta(const DeviceState& S, const LatticeParams& lp, double sup, cudaStream_t st);
 int lattice_spmv_blocks_per_sm(const LatticeParams& lp);
 size_t lattice_smem_bytes(const LatticeParams& lp);
 void lattice_free(LatticeBuffers* lb);

@@ -372,6 +372,8 @@ static void force_g(bool fp64, const StepParams& P, const DeviceState& S, int gr
 void launch_force(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st)
 {
     if (!fp64 && P.n > 0) k_supercell_words<<<L.grid_vec, kBlock, 0, st>>>(P, S);
+    // the lattice product's deviations from the same positions
+    if (!fp64 && L.lattice && L.lat) launch_lattice_delta(S, *L.lat, P.sup, st);
     switch (L.force_lanes) {
     case 4: force_g<4>(fp64, P, S, L.grid_force, st); break;
     case 16: force_g<16>(fp64, P, S, L.grid_force, st); break;
@@ -492,8 +494,8 @@ void launch_update(bool fp64, const StepParams& P, const DeviceState& S, const L
 
 void launch_refresh(bool fp64, const StepParams& P, const DeviceState& S, const LaunchCfg& L, cudaStream_t st)
 {
-    (void)fp64;
     k_refresh<<<L.grid_vec, kBlock, 0, st>>>(P, S);
+    if (!fp64 && L.lattice && L.lat) launch_lattice_delta(S, *L.lat, P.sup, st);
 }
 
 template <int G, int U>
