@@ -109,17 +109,6 @@ __device__ __forceinline__ float rsqrt_ftz(float x)
     return y;
 }
 
-// L2 prefetch of [p, p + bytes) (16-byte aligned, bytes a multiple of 16) in
-// pieces of at most 16 KB, all issued by the calling thread
-__device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes)
-{
-    constexpr unsigned kPiece = 16384;
-    for (unsigned off = 0; off < bytes; off += kPiece) {
-        const unsigned len = bytes - off < kPiece ? bytes - off : kPiece;
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"((const char*)p + off), "r"(len) : "memory");
-    }
-}
-
 int blocks_for(long long n) { return (int)std::max<long long>(1, std::min<long long>((n + kBlock - 1) / kBlock, 8192)); }
 
 // ---- detection ------------------------------------------------------------------------
@@ -322,8 +311,9 @@ __global__ void __launch_bounds__(kBlock) k_lat_delta(const dbl4* __restrict__ x
 //
 // Blocks take bricks from a counter (lp.sched[0]) in brick order, so that
 // bricks of uneven fill balance over the blocks; the last block to finish
-// resets the counter for the next launch.  The next brick's 1/d0 block is
-// prefetched to L2 while the current one is computed.
+// resets the counter for the next launch.  (An L2 prefetch of the next
+// brick's 1/d0 block, issued when the brick is taken, measured 3 % slower at
+// three blocks per SM; ordering the bricks by row count made no difference.)
 //
 // FIXED: the 80-entry stencil with its compile-time halo (lp.K == 80, halo
 // 36 x 8 x 8).  FUSE (a CG iteration): the direction is updated on the way
@@ -359,10 +349,6 @@ __global__ void __launch_bounds__(kBlock, 3) k_spmv_lattice(StepParams P, Device
     DotAcc32 acc;
     if (threadIdx.x == 0) {
         s_next = (int)atomicAdd(&lp.sched[0], 1u);
-        if (s_next < lp.n_bricks) {
-            const int s0 = lp.brick_start[s_next], s1 = lp.brick_start[s_next + 1];
-            prefetch_l2(lp.ell + (size_t)K * s0, (unsigned)(sizeof(float) * K * (s1 - s0)));
-        }
     }
     __syncthreads();
     int b = s_next;
@@ -412,10 +398,6 @@ __global__ void __launch_bounds__(kBlock, 3) k_spmv_lattice(StepParams P, Device
         __syncthreads();   // halo staged; every thread has read s_next
         if (threadIdx.x == 0) {
             s_next = (int)atomicAdd(&lp.sched[0], 1u);
-            if (s_next < lp.n_bricks) {
-                const int s0 = lp.brick_start[s_next], s1 = lp.brick_start[s_next + 1];
-                prefetch_l2(lp.ell + (size_t)K * s0, (unsigned)(sizeof(float) * K * (s1 - s0)));
-            }
         }
         for (int l = threadIdx.x; l < rows; l += blockDim.x) {
             const int p = start + l;
@@ -474,7 +456,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_spmv_lattice(StepParams P, Device
                     bond(4 * k4 + 3, s4.w);
                 }
             } else {
-#pragma unroll 4
+#pragma unroll 10   // 160 us at 1M against 163 (5), 168 (4), 171 (2) and 174 (20)
                 for (int k4 = 0; k4 < K / 4; ++k4) {
                     const float4 s4 = __ldcs(e4 + (size_t)k4 * rows);
                     bond(4 * k4, s4.x);
