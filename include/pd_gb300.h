@@ -460,6 +460,24 @@ pd_status pd_dataio_save_state_reference(pd_handle* h, size_t timestep);
  * a fresh count. */
 pd_status pd_dataio_load_state_reference(pd_handle* h, size_t timestep);
 
+/* SPH <-> PD collision: the reference's collideDifferentParticles
+ * (src/core/simulator.cuh:1590-1733, called after the PD step at
+ * simulator.cu:1188-1206), for SPH particles the caller simulates itself
+ * (this library has no SPH model).  sph_pos4 / sph_vel4: double[4 * n_sph]
+ * host arrays in internal units, updated in place.  Every SPH particle whose
+ * cell of the grid of sim (cell_size from boundary_min, num_cell_x/y/z) is
+ * inside the grid and that has a PD particle closer than sph_particle_radius +
+ * pd_particle_radius in the 27 cells around it is moved to that distance from
+ * the nearest one, and the two exchange velocity: normal parts to the
+ * mass-weighted mean, tangential parts mixed by (1 - slip) (slip = the
+ * reference's sph_pd_slip, 1.0 by default).  The PD particle's velocity is
+ * set on the handle (several SPH particles on one PD particle: the one of
+ * the smallest index).  The PD positions and velocities are the handle's at
+ * the call; the reference uses copies sorted at the start of its step and
+ * reads the PD velocity from a wrong index.  collided (may be NULL): SPH
+ * particles corrected. */
+pd_status pd_sph_collide(pd_handle* h, double* sph_pos4, double* sph_vel4, int n_sph, double slip, int* collided);
+
 /* ---- example scene: an OBJ mesh filled with particles (src/examples/scene.cpp) */
 typedef struct pd_scene pd_scene;
 /* Scene(simParams, runningParams, arrangement) (scene.cpp:18-135): reads

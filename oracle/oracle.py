@@ -101,6 +101,9 @@ def _load():
         lib.pdo_assemble.argtypes = [C.c_void_p]
         lib.pdo_apply_A.argtypes = [C.c_void_p, dp, dp]
         lib.pdo_sample_stretch.argtypes = [C.c_int, C.c_double, dp]
+        lib.pdo_sph_collide.argtypes = [C.c_void_p, dp, C.c_double, ip, C.c_double, C.c_double, C.c_double, dp, dp,
+                                        C.c_int]
+        lib.pdo_sph_collide.restype = C.c_int
         for name in ("pdo_current_step", "pdo_cg_converged", "pdo_last_cg_iters", "pdo_dt_ticks",
                      "pdo_substep", "pdo_retries_last_step"):
             getattr(lib, name).argtypes = [C.c_void_p]
@@ -287,6 +290,15 @@ class OracleSim:
         """List of sorted live-neighbour arrays, one per particle."""
         rp, col, cnt = self.row_ptr, self.bond_list, self.bond_count
         return [np.sort(col[rp[i]:rp[i] + cnt[i]]) for i in range(self.n)]
+
+    def sph_collide(self, lo, cell, n, r_sph, m_sph, slip, pos, vel):
+        """SPH <-> PD collision of (k, 4) float64 SPH arrays (updated in place)
+        on the grid (lo, cell, n); returns the SPH particles corrected."""
+        lo = np.ascontiguousarray(lo, dtype=np.float64)
+        n = np.ascontiguousarray(n, dtype=np.int32)
+        assert pos.dtype == np.float64 and pos.flags.c_contiguous and vel.dtype == np.float64 and vel.flags.c_contiguous
+        return self.lib.pdo_sph_collide(self.h, _dp(lo), float(cell), _ip(n), float(r_sph), float(m_sph),
+                                        float(slip), _dp(pos), _dp(vel), len(pos))
 
     step = property(lambda self: self.lib.pdo_current_step(self.h))
     cg_converged = property(lambda self: bool(self.lib.pdo_cg_converged(self.h)))

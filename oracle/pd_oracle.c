@@ -752,3 +752,93 @@ void pdo_get_velocity_backup(const pdo_state* s, double* o) { memcpy(o, s->vel_b
 void pdo_get_top_backup(const pdo_state* s, int* o) { memcpy(o, s->top_bk, (size_t)s->n * sizeof(int)); }
 void pdo_get_top(const pdo_state* s, int* o) { memcpy(o, s->top, (size_t)s->n * sizeof(int)); }
 void pdo_get_diag_blocks(const pdo_state* s, double* out) { memcpy(out, s->diag, 9 * (size_t)s->n * sizeof(double)); }
+
+/* ---- SPH <-> PD collision ------------------------------------------------------------
+ * collideDifferentParticles (src/core/simulator.cuh:1590-1733) restated with
+ * the GPU path's semantics: calcGridPos / calcGridHash (simulator.cuh:61-87)
+ * for both particle kinds, the nearest PD particle of the 27 cells around the
+ * SPH particle's cell closer than r_sph + r_pd (ties: the smallest PD index),
+ * the reference's position correction and velocity exchange in its operation
+ * order (the distance divisor rounded to float as its fmaxf), the PD velocity
+ * read from the nearest particle (the reference reads a wrong index) and
+ * written by the SPH particle of the smallest index. */
+static int sph_cell(const double lo[3], double cell, const int n[3], const double* p, int c[3])
+{
+    for (int k = 0; k < 3; ++k) c[k] = (int)floor((p[k] - lo[k]) / cell);
+    if (c[0] < 0 || c[1] < 0 || c[2] < 0 || c[0] >= n[0] || c[1] >= n[1] || c[2] >= n[2]) return -1;
+    return (c[2] * n[1] + c[1]) * n[0] + c[0];
+}
+
+int pdo_sph_collide(pdo_state* s, const double lo[3], double cell, const int n[3], double r_sph, double m_sph,
+                    double slip, double* pos4, double* vel4, int n_sph)
+{
+    const int np = s->n;
+    const double min_dist = r_sph + s->P.radius, mi = m_sph, mj = s->P.mass;
+    int* pcell = (int*)xcalloc(3 * (size_t)np + 1, sizeof(int));
+    int* pin = (int*)xcalloc((size_t)np + 1, sizeof(int));
+    int* winner = (int*)xcalloc((size_t)np + 1, sizeof(int));
+    int* hit = (int*)xcalloc((size_t)n_sph + 1, sizeof(int));
+    double* vnew = (double*)xcalloc(3 * (size_t)n_sph + 1, sizeof(double));
+    for (int j = 0; j < np; ++j) {
+        pin[j] = sph_cell(lo, cell, n, s->pos + 4 * (size_t)j, pcell + 3 * (size_t)j) >= 0;
+        winner[j] = -1;
+    }
+    int count = 0;
+    for (int i = 0; i < n_sph; ++i) {
+        hit[i] = -1;
+        double* pi = pos4 + 4 * (size_t)i;
+        int c[3];
+        if (sph_cell(lo, cell, n, pi, c) < 0) continue;
+        double best = min_dist;
+        int bj = -1;
+        for (int j = 0; j < np; ++j) {
+            if (!pin[j]) continue;
+            const int* cj = pcell + 3 * (size_t)j;
+            if (abs(cj[0] - c[0]) > 1 || abs(cj[1] - c[1]) > 1 || abs(cj[2] - c[2]) > 1) continue;
+            const double* pj = s->pos + 4 * (size_t)j;
+            const double ex = pj[0] - pi[0], ey = pj[1] - pi[1], ez = pj[2] - pi[2];
+            const double d = sqrt(ex * ex + ey * ey + ez * ez);
+            if (d < best || (d == best && bj >= 0 && j < bj)) {
+                best = d;
+                bj = j;
+            }
+        }
+        if (bj < 0) continue;
+        const double* pj = s->pos + 4 * (size_t)bj;
+        const double* vj = s->vel + 4 * (size_t)bj;
+        double* vi = vel4 + 4 * (size_t)i;
+        const double D = (double)ref_fmaxf((float)best, (float)SMALL_D);
+        const double e[3] = {(pj[0] - pi[0]) / D, (pj[1] - pi[1]) / D, (pj[2] - pi[2]) / D};
+        const double di = e[0] * vi[0] + e[1] * vi[1] + e[2] * vi[2];
+        const double dj = e[0] * vj[0] + e[1] * vj[1] + e[2] * vj[2];
+        const double mm = mi + mj;
+        const double ci = mi + mj * slip, cj = mj + mi * slip;
+        const double ti = mj * (1.0 - slip), tj = mi * (1.0 - slip);
+        double xo[3], vo[3];
+        for (int k = 0; k < 3; ++k) {
+            xo[k] = pj[k] - min_dist * e[k];
+            const double vin = e[k] * di, vit = vi[k] - vin;
+            const double vjn = e[k] * dj, vjt = vj[k] - vjn;
+            const double vn2 = (mi * vin + mj * vjn) / mm;
+            const double vit2 = (ci * vit + ti * vjt) / mm;
+            const double vjt2 = (cj * vjt + tj * vit) / mm;
+            vo[k] = vn2 + vit2;
+            vnew[3 * (size_t)i + k] = vn2 + vjt2;
+        }
+        for (int k = 0; k < 3; ++k) {
+            pi[k] = xo[k];
+            vi[k] = vo[k];
+        }
+        hit[i] = bj;
+        if (winner[bj] < 0) winner[bj] = i;
+        ++count;
+    }
+    for (int i = 0; i < n_sph; ++i) {
+        const int j = hit[i];
+        if (j < 0 || winner[j] != i) continue;
+        for (int k = 0; k < 3; ++k) s->vel[4 * (size_t)j + k] = vnew[3 * (size_t)i + k];
+        s->vel[4 * (size_t)j + 3] = 0.0;
+    }
+    free(pcell); free(pin); free(winner); free(hit); free(vnew);
+    return count;
+}

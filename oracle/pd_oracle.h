@@ -131,6 +131,13 @@ void pdo_get_velocity_backup(const pdo_state* s, double* out4);
 void pdo_get_top_backup(const pdo_state* s, int* out);
 void pdo_get_top(const pdo_state* s, int* out);                   /* pd_bond_list_top: live bonds - 1 */
 void pdo_assemble(pdo_state* s);                           /* fill A and b after a force pass */
+/* SPH <-> PD collision (collideDifferentParticles, simulator.cuh:1590-1733)
+ * of n_sph caller SPH particles (pos4 / vel4 updated) against the current PD
+ * state, on the grid (lo, cell, n) with the distance r_sph + P.radius; the
+ * PD velocity of a particle hit is set from the SPH particle of the smallest
+ * index.  Returns the SPH particles corrected. */
+int pdo_sph_collide(pdo_state* s, const double lo[3], double cell, const int n[3], double r_sph, double m_sph,
+                    double slip, double* pos4, double* vel4, int n_sph);
 
 /* glibc-compatible rand() stream used for s0 (exposed to pin the product's copy). */
 void pdo_sample_stretch(int n, double s0, double* out);

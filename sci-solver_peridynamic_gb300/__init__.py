@@ -212,6 +212,7 @@ def library(build_if_missing: bool = True):
         "pd_dataio_load_state": (st, [vp, C.c_size_t]),
         "pd_dataio_save_state_reference": (st, [vp, C.c_size_t]),
         "pd_dataio_load_state_reference": (st, [vp, C.c_size_t]),
+        "pd_sph_collide": (st, [vp, P(C.c_double), P(C.c_double), C.c_int, C.c_double, P(C.c_int)]),
         "pd_scene_create": (st, [P(SimulationParameters), P(RunningParameters), C.c_int, C.c_uint, P(vp)]),
         "pd_scene_particle_count": (st, [vp, P(C.c_int)]),
         "pd_scene_init_pd_particles": (st, [vp, P(C.c_int32), P(C.c_double), P(C.c_double)]),
@@ -555,6 +556,25 @@ class Simulator:
 
     def synchronize(self):
         _check(self.lib.pd_synchronize(self.h), self.h)
+
+    def sph_collide(self, sph_pos, sph_vel, slip: float = 1.0) -> int:
+        """SPH <-> PD collision (collideDifferentParticles) of the caller's SPH
+        particles: (n, 4) float64 arrays of positions and velocities in
+        internal units, corrected in place; the PD velocities of the handle
+        are updated.  Returns the number of SPH particles corrected."""
+        pos = np.ascontiguousarray(sph_pos, dtype=np.float64)
+        vel = np.ascontiguousarray(sph_vel, dtype=np.float64)
+        if pos.shape != vel.shape or pos.ndim != 2 or pos.shape[1] != 4:
+            raise ValueError("sph_pos and sph_vel must be (n, 4) float64 arrays")
+        c = C.c_int()
+        _check(self.lib.pd_sph_collide(self.h, pos.ctypes.data_as(C.POINTER(C.c_double)),
+                                       vel.ctypes.data_as(C.POINTER(C.c_double)), pos.shape[0], float(slip),
+                                       C.byref(c)), self.h)
+        if pos is not sph_pos:
+            sph_pos[...] = pos
+        if vel is not sph_vel:
+            sph_vel[...] = vel
+        return c.value
 
     def launch_count(self) -> int:
         v = C.c_longlong()

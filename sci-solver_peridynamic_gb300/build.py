@@ -27,7 +27,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["step.cu", "bonds.cu", "noalloc.cu", "mlp.cu", "mlp_tc.cu", "warmstart.cu", "batch.cu", "tiles.cu", "mesh_fill.cu", "contact.cu", "history.cu", "lattice.cu"]
+CU_SOURCES = ["step.cu", "bonds.cu", "noalloc.cu", "mlp.cu", "mlp_tc.cu", "warmstart.cu", "batch.cu", "tiles.cu", "mesh_fill.cu", "contact.cu", "history.cu", "lattice.cu", "sph_coupling.cu"]
 # per-file nvcc flags (none at present)
 CU_EXTRA = {}
 CPP_SOURCES = ["engine.cpp", "capi.cpp", "params.cpp", "batch.cpp", "dataio.cpp", "scene.cpp"]

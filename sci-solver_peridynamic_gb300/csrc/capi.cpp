@@ -279,4 +279,10 @@ pd_status pd_synchronize(pd_handle* h)
     return h->eng->synchronize();
 }
 
+pd_status pd_sph_collide(pd_handle* h, double* sph_pos4, double* sph_vel4, int n_sph, double slip, int* collided)
+{
+    ENG(h);
+    return h->eng->sph_collide(sph_pos4, sph_vel4, n_sph, slip, collided);
+}
+
 }  // extern "C"

@@ -141,6 +141,7 @@ void Engine::free_all()
         if (p) cudaFree(p);
     free_tiles(S_);
     lattice_free(&latb_);
+    sph_buffers_free(&sph_);
     lat_ = LatticeParams{};
     lat_ok_ = false;
     lat_fixed_built_ = false;
@@ -1507,6 +1508,50 @@ pd_status Engine::stats(pd_step_stats* s) const
             s->bonds_alive = a;
         }
     }
+    return PD_OK;
+}
+
+// SPH <-> PD collision on the reference's grid (sim_.cell_size from
+// boundary_min, num_cell_x/y/z) with the distance r_sph + r_pd
+// (sph_pd_min_distance, parameters.cu:420-421); sph_coupling.cu.
+pd_status Engine::sph_collide(double* pos4, double* vel4, int n_sph, double slip, int* collided)
+{
+    if (!ready_) {
+        err_ = "sph_collide: make_ready has not run";
+        return PD_ERR_NOT_READY;
+    }
+    if (n_sph < 0 || (n_sph > 0 && (!pos4 || !vel4)) || !std::isfinite(slip)) return PD_ERR_INVALID_ARGUMENT;
+    if (sim_.num_cell_x <= 0 || sim_.num_cell_y <= 0 || sim_.num_cell_z <= 0 || !(sim_.cell_size > 0)) {
+        err_ = "sph_collide: the simulation parameters define no grid";
+        return PD_ERR_INVALID_ARGUMENT;
+    }
+    CK(cudaSetDevice(device_), "cudaSetDevice");
+    const SphGrid g{{sim_.boundary_min_x, sim_.boundary_min_y, sim_.boundary_min_z}, sim_.cell_size,
+                    {sim_.num_cell_x, sim_.num_cell_y, sim_.num_cell_z}};
+    const size_t bytes = sizeof(double4) * (size_t)std::max(n_sph, 1);
+    for (auto pc : {std::make_pair(&sph_.pos, &sph_.pos_cap), std::make_pair(&sph_.vel, &sph_.vel_cap)}) {
+        if (*pc.second < bytes) {
+            if (*pc.first) cudaFree(*pc.first);
+            *pc.first = nullptr;
+            *pc.second = 0;
+            CK(cudaMalloc((void**)pc.first, bytes), "alloc sph arrays");
+            *pc.second = bytes;
+        }
+    }
+    if (n_sph > 0) {
+        CK(cudaMemcpyAsync(sph_.pos, pos4, sizeof(double4) * (size_t)n_sph, cudaMemcpyHostToDevice, stream_), "upload sph");
+        CK(cudaMemcpyAsync(sph_.vel, vel4, sizeof(double4) * (size_t)n_sph, cudaMemcpyHostToDevice, stream_), "upload sph");
+    }
+    int c = 0;
+    CK(sph_pd_collide(S_, d_perm_, g, sim_.sph_particle_radius + sim_.pd_particle_radius, sim_.sph_particle_mass,
+                      sim_.pd_particle_mass, slip, n_sph, sph_.pos, sph_.vel, &sph_, &c, stream_), "sph collide");
+    launches_ += 4 + (n_sph > 0 ? 2 : 0);
+    if (n_sph > 0) {
+        CK(cudaMemcpyAsync(pos4, sph_.pos, sizeof(double4) * (size_t)n_sph, cudaMemcpyDeviceToHost, stream_), "download sph");
+        CK(cudaMemcpyAsync(vel4, sph_.vel, sizeof(double4) * (size_t)n_sph, cudaMemcpyDeviceToHost, stream_), "download sph");
+        CK(cudaStreamSynchronize(stream_), "sph sync");
+    }
+    if (collided) *collided = c;
     return PD_OK;
 }
 

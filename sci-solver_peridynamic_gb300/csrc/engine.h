@@ -58,6 +58,8 @@ public:
     pd_status dataio_save_state_reference(size_t timestep);
     pd_status dataio_load_state_reference(size_t timestep);
     std::string ref_state_path(size_t timestep) const;
+    // SPH <-> PD collision (collideDifferentParticles) with the caller's SPH particles
+    pd_status sph_collide(double* pos4, double* vel4, int n_sph, double slip, int* collided);
 
 private:
     pd_status dataio_write_sim_info();
@@ -207,6 +209,7 @@ private:
     void* d_p2_ = nullptr;             // second CG direction buffer of the lattice product's fused update
     bool batch_member_ = false;        // set by Batch: its scenes keep the builder's slot order
     ContactBuffers contact_{};         // PD-PD contact hash (when enabled)
+    SphBuffers sph_{};                 // SPH <-> PD collision scratch
     size_t saved_frame_ = 0;           // DataIO::savedFrame
     bool wrote_sim_info_ = false;      // DataIO::writtenSimulationParameter
     std::string err_;

@@ -299,6 +299,31 @@ cudaError_t launch_contact(bool fp64, const DeviceState& S, int n, const Contact
 // Max resident blocks per SM of the SpMV / force kernels (for grid sizing).
 int row_kernel_blocks_per_sm(bool fp64, int lanes, int unroll);
 
+// ---- SPH <-> PD collision (sph_coupling.cu) ------------------------------------------
+struct SphGrid {              // the reference's uniform grid (calcGridPos, simulator.cuh:61-87)
+    double lo[3];             // boundary_min
+    double cell;              // cell_size
+    int n[3];                 // num_cell_x, y, z
+};
+struct SphBuffers {           // device scratch of the collision, grown to the largest call
+    unsigned* key = nullptr; size_t key_cap = 0;
+    int* sorted = nullptr; size_t sorted_cap = 0;
+    int* winner = nullptr; size_t winner_cap = 0;
+    int* start = nullptr; size_t start_cap = 0;
+    int* end = nullptr; size_t end_cap = 0;
+    int* hit = nullptr; size_t hit_cap = 0;
+    double4* vnew = nullptr; size_t vnew_cap = 0;
+    int* count = nullptr; size_t count_cap = 0;
+    double4* pos = nullptr; size_t pos_cap = 0;   // the caller's SPH arrays on the device
+    double4* vel = nullptr; size_t vel_cap = 0;
+};
+// d_pos / d_vel: the SPH particles (caller order), corrected in place; the
+// PD velocities S.v64 of the particles hit; collided = SPH particles corrected
+cudaError_t sph_pd_collide(const DeviceState& S, const int* perm, const SphGrid& g, double min_dist, double m_sph,
+                           double m_pd, double slip, int n_sph, double4* d_pos, double4* d_vel, SphBuffers* b,
+                           int* collided, cudaStream_t st);
+void sph_buffers_free(SphBuffers* b);
+
 // ---- history-projection initial guess (history.cu) --------------------------------
 constexpr int kHistMax = 8;                 // history vectors kept at most
 struct HistPtrs { const void* v[kHistMax]; };
