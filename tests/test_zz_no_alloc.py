@@ -4,6 +4,8 @@ library pointers into its own pool, or a time-critical loop that must not
 allocate).  Its output must equal pd_apply_operator's on the same view and
 vectors, on two calls in a row (the static scratch is reused and keeps the
 previous call's contents).  This file is collected last on purpose."""
+import gc
+
 import numpy as np
 import pytest
 
@@ -86,11 +88,15 @@ def test_noalloc_allocates_nothing(pdgb, scenes):
     torch.cuda.synchronize()
     pdgb.apply_operator_noalloc(v, x.data_ptr(), y.data_ptr(), dot.data_ptr(), stream)
     sim.synchronize()
+    # tensors of earlier tests still waiting for the cycle collector would
+    # otherwise be released in the middle of the measurement
+    gc.collect()
     free0, _ = torch.cuda.mem_get_info()
     torch_bytes0 = torch.cuda.memory_allocated()
     for _ in range(20):
         pdgb.apply_operator_noalloc(v, x.data_ptr(), y.data_ptr(), dot.data_ptr(), stream)
     sim.synchronize()
+    gc.collect()
     free1, _ = torch.cuda.mem_get_info()
     assert free1 == free0
     assert torch.cuda.memory_allocated() == torch_bytes0
