@@ -40,7 +40,7 @@ struct SceneRun {
     int substep;
     int ticks;
     int retries;           // rollbacks in the current step
-    int active;            // force pass pending in this round
+    int active;            // force pass pending in this pass of the rollback loop
     int restore;           // 1: restore from the backup, 2: take the backup
     int solving;           // solve + update in this step
     int cg_converged;      // every CG solve so far converged (Simulator::CGConvergence)
