@@ -1528,7 +1528,7 @@ pd_status Engine::sph_collide(double* pos4, double* vel4, int n_sph, double slip
     CK(cudaSetDevice(device_), "cudaSetDevice");
     const SphGrid g{{sim_.boundary_min_x, sim_.boundary_min_y, sim_.boundary_min_z}, sim_.cell_size,
                     {sim_.num_cell_x, sim_.num_cell_y, sim_.num_cell_z}};
-    const size_t bytes = sizeof(double4) * (size_t)std::max(n_sph, 1);
+    const size_t bytes = sizeof(dbl4) * (size_t)std::max(n_sph, 1);
     for (auto pc : {std::make_pair(&sph_.pos, &sph_.pos_cap), std::make_pair(&sph_.vel, &sph_.vel_cap)}) {
         if (*pc.second < bytes) {
             if (*pc.first) cudaFree(*pc.first);
@@ -1539,16 +1539,16 @@ pd_status Engine::sph_collide(double* pos4, double* vel4, int n_sph, double slip
         }
     }
     if (n_sph > 0) {
-        CK(cudaMemcpyAsync(sph_.pos, pos4, sizeof(double4) * (size_t)n_sph, cudaMemcpyHostToDevice, stream_), "upload sph");
-        CK(cudaMemcpyAsync(sph_.vel, vel4, sizeof(double4) * (size_t)n_sph, cudaMemcpyHostToDevice, stream_), "upload sph");
+        CK(cudaMemcpyAsync(sph_.pos, pos4, sizeof(dbl4) * (size_t)n_sph, cudaMemcpyHostToDevice, stream_), "upload sph");
+        CK(cudaMemcpyAsync(sph_.vel, vel4, sizeof(dbl4) * (size_t)n_sph, cudaMemcpyHostToDevice, stream_), "upload sph");
     }
     int c = 0;
     CK(sph_pd_collide(S_, d_perm_, g, sim_.sph_particle_radius + sim_.pd_particle_radius, sim_.sph_particle_mass,
                       sim_.pd_particle_mass, slip, n_sph, sph_.pos, sph_.vel, &sph_, &c, stream_), "sph collide");
     launches_ += 4 + (n_sph > 0 ? 2 : 0);
     if (n_sph > 0) {
-        CK(cudaMemcpyAsync(pos4, sph_.pos, sizeof(double4) * (size_t)n_sph, cudaMemcpyDeviceToHost, stream_), "download sph");
-        CK(cudaMemcpyAsync(vel4, sph_.vel, sizeof(double4) * (size_t)n_sph, cudaMemcpyDeviceToHost, stream_), "download sph");
+        CK(cudaMemcpyAsync(pos4, sph_.pos, sizeof(dbl4) * (size_t)n_sph, cudaMemcpyDeviceToHost, stream_), "download sph");
+        CK(cudaMemcpyAsync(vel4, sph_.vel, sizeof(dbl4) * (size_t)n_sph, cudaMemcpyDeviceToHost, stream_), "download sph");
         CK(cudaStreamSynchronize(stream_), "sph sync");
     }
     if (collided) *collided = c;

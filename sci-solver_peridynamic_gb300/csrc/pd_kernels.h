@@ -312,15 +312,15 @@ struct SphBuffers {           // device scratch of the collision, grown to the l
     int* start = nullptr; size_t start_cap = 0;
     int* end = nullptr; size_t end_cap = 0;
     int* hit = nullptr; size_t hit_cap = 0;
-    double4* vnew = nullptr; size_t vnew_cap = 0;
+    dbl4* vnew = nullptr; size_t vnew_cap = 0;
     int* count = nullptr; size_t count_cap = 0;
-    double4* pos = nullptr; size_t pos_cap = 0;   // the caller's SPH arrays on the device
-    double4* vel = nullptr; size_t vel_cap = 0;
+    dbl4* pos = nullptr; size_t pos_cap = 0;   // the caller's SPH arrays on the device
+    dbl4* vel = nullptr; size_t vel_cap = 0;
 };
 // d_pos / d_vel: the SPH particles (caller order), corrected in place; the
 // PD velocities S.v64 of the particles hit; collided = SPH particles corrected
 cudaError_t sph_pd_collide(const DeviceState& S, const int* perm, const SphGrid& g, double min_dist, double m_sph,
-                           double m_pd, double slip, int n_sph, double4* d_pos, double4* d_vel, SphBuffers* b,
+                           double m_pd, double slip, int n_sph, dbl4* d_pos, dbl4* d_vel, SphBuffers* b,
                            int* collided, cudaStream_t st);
 void sph_buffers_free(SphBuffers* b);
 

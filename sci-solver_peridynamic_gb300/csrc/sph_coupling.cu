@@ -88,10 +88,10 @@ struct SphCollideArgs {
     const int* sorted; // slots by cell
     const int* start;  // per cell, -1 empty
     const int* end;
-    double4* pos;      // SPH positions (caller order), updated
-    double4* vel;      // SPH velocities, updated
+    dbl4* pos;      // SPH positions (caller order), updated
+    dbl4* vel;      // SPH velocities, updated
     int* hit;          // per SPH particle: PD slot, or -1
-    double4* vnew;     // per SPH particle: the PD particle's new velocity
+    dbl4* vnew;     // per SPH particle: the PD particle's new velocity
     int* winner;       // per PD slot: smallest SPH index that hit it (INT_MAX: none)
     int* count;        // SPH particles corrected
 };
@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(kBlock) k_sph_collide(SphCollideArgs a)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n_sph; i += gridDim.x * blockDim.x) {
         a.hit[i] = -1;
-        const double4 pi = a.pos[i];
+        const dbl4 pi = a.pos[i];
         int c[3];
         if (grid_cell(a.g, pi.x, pi.y, pi.z, c) < 0) continue;
         double best = a.min_dist;
@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(kBlock) k_sph_collide(SphCollideArgs a)
         const double D = (double)fmaxf((float)best, (float)kSmall);
         const double e[3] = {ddiv(dsub(pj.x, pi.x), D), ddiv(dsub(pj.y, pi.y), D), ddiv(dsub(pj.z, pi.z), D)};
         const double pjv[3] = {pj.x, pj.y, pj.z};
-        const double4 vi4 = a.vel[i];
+        const dbl4 vi4 = a.vel[i];
         const dbl4 vj4 = a.v64[bj];
         const double vi[3] = {vi4.x, vi4.y, vi4.z}, vj[3] = {vj4.x, vj4.y, vj4.z};
         const double di = dadd(dadd(dmul(e[0], vi[0]), dmul(e[1], vi[1])), dmul(e[2], vi[2]));
@@ -151,9 +151,9 @@ __global__ void __launch_bounds__(kBlock) k_sph_collide(SphCollideArgs a)
             vo[k] = dadd(vn2, vit2);
             wo[k] = dadd(vn2, vjt2);
         }
-        a.pos[i] = make_double4(xo[0], xo[1], xo[2], pi.w);
-        a.vel[i] = make_double4(vo[0], vo[1], vo[2], vi4.w);
-        a.vnew[i] = make_double4(wo[0], wo[1], wo[2], 0.0);
+        a.pos[i] = make_dbl4(xo[0], xo[1], xo[2], pi.w);
+        a.vel[i] = make_dbl4(vo[0], vo[1], vo[2], vi4.w);
+        a.vnew[i] = make_dbl4(wo[0], wo[1], wo[2], 0.0);
         a.hit[i] = bj;
         atomicMin(a.winner + bj, i);
         atomicAdd(a.count, 1);
@@ -161,13 +161,13 @@ __global__ void __launch_bounds__(kBlock) k_sph_collide(SphCollideArgs a)
 }
 
 __global__ void __launch_bounds__(kBlock) k_sph_apply(int n_sph, const int* __restrict__ hit,
-                                                      const int* __restrict__ winner, const double4* __restrict__ vnew,
+                                                      const int* __restrict__ winner, const dbl4* __restrict__ vnew,
                                                       dbl4* __restrict__ v64)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_sph; i += gridDim.x * blockDim.x) {
         const int j = hit[i];
         if (j < 0 || winner[j] != i) continue;
-        const double4 w = vnew[i];
+        const dbl4 w = vnew[i];
         v64[j] = make_dbl4(w.x, w.y, w.z, 0.0);
     }
 }
@@ -177,7 +177,7 @@ int grid_blocks(long long n) { return (int)std::max<long long>(1, std::min<long 
 }  // namespace
 
 cudaError_t sph_pd_collide(const DeviceState& S, const int* perm, const SphGrid& g, double min_dist, double m_sph,
-                           double m_pd, double slip, int n_sph, double4* d_pos, double4* d_vel, SphBuffers* b,
+                           double m_pd, double slip, int n_sph, dbl4* d_pos, dbl4* d_vel, SphBuffers* b,
                            int* collided, cudaStream_t st)
 {
     const int n = S.n;
@@ -201,7 +201,7 @@ cudaError_t sph_pd_collide(const DeviceState& S, const int* perm, const SphGrid&
     if ((e = grow((void**)&b->start, &b->start_cap, sizeof(int) * (size_t)cells)) != cudaSuccess) return e;
     if ((e = grow((void**)&b->end, &b->end_cap, sizeof(int) * (size_t)cells)) != cudaSuccess) return e;
     if ((e = grow((void**)&b->hit, &b->hit_cap, sizeof(int) * ns)) != cudaSuccess) return e;
-    if ((e = grow((void**)&b->vnew, &b->vnew_cap, sizeof(double4) * ns)) != cudaSuccess) return e;
+    if ((e = grow((void**)&b->vnew, &b->vnew_cap, sizeof(dbl4) * ns)) != cudaSuccess) return e;
     if ((e = grow((void**)&b->count, &b->count_cap, sizeof(int))) != cudaSuccess) return e;
     int bits = 1;
     while (bits < 32 && (1ULL << bits) <= (unsigned long long)cells) ++bits;
