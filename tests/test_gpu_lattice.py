@@ -143,3 +143,37 @@ def test_lattice_checkpoint_restart_bitwise(pdgb, scenes, tmp_path):
     b.advance(20)
     assert np.array_equal(a.get(pdgb.VAR_POSITION), b.get(pdgb.VAR_POSITION))
     assert same_sets(a.alive_sets(), b.alive_sets())
+
+
+def test_lattice_operator_after_a_translation_of_several_supercells(pdgb, scenes):
+    """A free lattice block flying at 60 m/s per axis for 40 steps moves 0.24
+    m per axis, about four supercells: every particle's deviation from its
+    site wraps (d + sup n with n != 0), and the stencil product must still
+    equal the gather product (whose supercell words wrap the same way) and
+    the oracle's assembled matrix; the run keeps the oracle's positions."""
+    ys = {}
+    for path in (3, 2):
+        sc = scenes.impact_body(1728, "block", coeff=5.0, speed=0.0, seed=3, steps=40)
+        sc.act[:] = pdgb.ACTIVE
+        sc.vel[:, :3] = 60.0
+        sc.opt.gravity[:] = (0.0, 0.0, 0.0)
+        sc.opt.spmv_path = path
+        sim = scenes.make_simulator(sc)
+        sim.makeReady()
+        sim.advance(40)
+        assert sim.params()[2].spmv_path == path
+        x = sim.get(pdgb.VAR_POSITION)[:, :3]
+        assert np.all(x - sc.pos[:, :3] > 0.2), "the body moved by several supercells"
+        rng = np.random.default_rng(7)
+        v = np.zeros((sc.n, 4))
+        v[:, :3] = rng.standard_normal((sc.n, 3))
+        ys[path] = apply_on_device(pdgb, sim, v) + (sim,)
+    (y3, d3, x3, s3), (y2, d2, x2, _) = ys[3], ys[2]
+    scale = np.abs(y2[:, :3]).max()
+    assert np.abs(y3[:, :3] - y2[:, :3]).max() <= 2e-6 * scale
+    ora = make_oracle(sc)
+    ora.advance(40)
+    y_ref = ora.apply_A(x3)
+    assert np.abs(y3[:, :3] - y_ref[:, :3]).max() <= 2e-5 * np.abs(y_ref[:, :3]).max()
+    assert same_sets(s3.alive_sets(), ora.alive_sets())
+    assert_positions(s3.get(pdgb.VAR_POSITION), ora.position, sc.pos, 0, "lattice block after translation")
