@@ -1142,9 +1142,10 @@ pd_status Engine::hist_prepare()
         CK(cudaMalloc(&d_hnet_, vec), "alloc learned column");
         CK(cudaMemsetAsync(d_hnet_, 0, vec, stream_), "memset learned column");
     }
-    CK(cudaMalloc((void**)&d_hpart_, sizeof(double) * (size_t)hist_blocks_ * hist_dots_count(0)),
-       "alloc history partials");
-    CK(cudaMalloc((void**)&d_hdots_, sizeof(double) * 128), "alloc history dots");
+    const size_t npart = (size_t)hist_blocks_ * (hist_dots_count(0) + hist_dots_count(1));
+    CK(cudaMalloc((void**)&d_hpart_, sizeof(double) * npart), "alloc history partials");
+    CK(cudaMallocHost((void**)&h_hpart_, sizeof(double) * npart), "alloc history partials (host)");
+    CK(cudaMallocHost((void**)&h_sc_pre_, sizeof(CgScalars)), "alloc history scalars (host)");
     CK(cudaMallocHost((void**)&h_sc_hist_, sizeof(CgScalars)), "alloc history scalars (host)");
     CK(cudaMalloc((void**)&d_hsol_, sizeof(HistSolve)), "alloc history solve");
     CK(cudaMallocHost((void**)&h_hsol_, sizeof(HistSolve)), "alloc history solve (host)");
@@ -1159,12 +1160,15 @@ void Engine::hist_free()
     if (d_hnet_) cudaFree(d_hnet_);
     d_hnet_ = nullptr;
     if (d_hpart_) cudaFree(d_hpart_);
-    if (d_hdots_) cudaFree(d_hdots_);
     if (h_sc_hist_) cudaFreeHost(h_sc_hist_);
     if (d_hsol_) cudaFree(d_hsol_);
     if (h_hsol_) cudaFreeHost(h_hsol_);
+    if (h_hpart_) cudaFreeHost(h_hpart_);
+    if (h_sc_pre_) cudaFreeHost(h_sc_pre_);
+    h_hpart_ = nullptr;
+    h_sc_pre_ = nullptr;
     d_hist_ = d_ahist_ = nullptr;
-    d_hpart_ = d_hdots_ = nullptr;
+    d_hpart_ = nullptr;
     h_sc_hist_ = nullptr;
     d_hsol_ = nullptr;
     h_hsol_ = nullptr;
@@ -1196,21 +1200,30 @@ pd_status Engine::hist_project(const StepParams& P)
     // products with this step's operator (counter 4 of the reduction scratch is unused without a dot)
     const ReduceSlot slot{S_.partials, S_.counters + 4};
     for (int j = 0; j < m; ++j) apply_op(P, H.v[j], (void*)W.v[j], slot, nullptr);
-    const int na = hist_dots_count(0);
-    launch_hist_dots(fp64_, 0, n_, m, H, W, S_.r, d_hpart_, hist_blocks_, d_hdots_, stream_);
-    launch_hist_dots(fp64_, 1, n_, m, H, W, nullptr, d_hpart_, hist_blocks_, d_hdots_ + na, stream_);
+    // the block partials of both Gram passes
+    const int na0 = hist_dots_count(0), na1 = hist_dots_count(1);
+    launch_hist_dots(fp64_, 0, n_, m, H, W, S_.r, d_hpart_, hist_blocks_, nullptr, stream_);
+    launch_hist_dots(fp64_, 1, n_, m, H, W, nullptr, d_hpart_ + (size_t)hist_blocks_ * na0, hist_blocks_, nullptr,
+                     stream_);
+    // the m x m solve on the host, in stream order: partials and scalars to
+    // pinned memory, the callback, its result back to the device (the GPU
+    // waits for the round trip; the calling thread does not)
+    CK(cudaMemcpyAsync(h_hpart_, d_hpart_, sizeof(double) * (size_t)hist_blocks_ * (na0 + na1),
+                       cudaMemcpyDeviceToHost, stream_), "read history partials");
+    CK(cudaMemcpyAsync(h_sc_pre_, S_.sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, stream_), "read cg scalars");
     // columns whose part outside the others' span is below sqrt(rel) of the
     // largest norm are rounding noise of the stored precision
     // (measured on a 100k-particle impact: 1e-14 .. 1e-10 within 1 % of iterations; 1e-6 loses the gain)
-    const double rel = fp64_ ? 1e-26 : 1e-12;
-    launch_hist_solve(m, d_hdots_, rel, net ? m - 1 : -1, S_.sc, d_hsol_, stream_);
+    hist_cb_ = HistHostSolve{m, hist_blocks_, net ? m - 1 : -1, fp64_ ? 1e-26 : 1e-12, h_hpart_, h_sc_pre_, h_hsol_};
+    CK(cudaLaunchHostFunc(stream_, [](void* a) { hist_host_solve(*(const HistHostSolve*)a); }, &hist_cb_),
+       "history solve callback");
+    CK(cudaMemcpyAsync(d_hsol_, h_hsol_, sizeof(HistSolve), cudaMemcpyHostToDevice, stream_), "upload history solve");
     // x1 + H y and its residual (the apply returns at once when no column was
     // used; the residual is then that of x1 again)
     launch_hist_apply(fp64_, n_, m, H, d_hsol_, S_.sol, L_.grid_vec, stream_);
     launch_spmv(fp64_, false, P, S_, L_, stream_);
     launch_cg_residual(fp64_, P, S_, L_, stream_);
-    launches_ += m + 8;
-    CK(cudaMemcpyAsync(h_hsol_, d_hsol_, sizeof(HistSolve), cudaMemcpyDeviceToHost, stream_), "read history solve");
+    launches_ += m + 5;
     CK(cudaMemcpyAsync(h_sc_hist_, S_.sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, stream_),
        "read projected residual");
     hist_pending_ = true;

@@ -170,10 +170,12 @@ private:
     void* d_hnet_ = nullptr;      // warm_start 3: the network's correction (the projection's last column)
     long long ws_net_used_ = 0;   // warm_start 3: projections that gave the network's column a weight
     double* d_hpart_ = nullptr;   // per-block partial sums of a Gram pass
-    double* d_hdots_ = nullptr;   // S (36), c (8), G (36)
     CgScalars* h_sc_hist_ = nullptr;   // pinned: scalars after the projected residual
     HistSolve* d_hsol_ = nullptr;      // the m x m solve's result (device)
-    HistSolve* h_hsol_ = nullptr;      // pinned copy, read after the solve
+    HistSolve* h_hsol_ = nullptr;      // pinned: written by the host callback, copied to d_hsol_
+    double* h_hpart_ = nullptr;        // pinned: block partials of both Gram passes
+    CgScalars* h_sc_pre_ = nullptr;    // pinned: scalars of the previous solution's residual
+    HistHostSolve hist_cb_{};          // arguments of the callback (alive until it ran)
     bool hist_pending_ = false;        // a projection ran in this solve
     // step state (Simulator members)
     int step_ = 0;

@@ -11,9 +11,10 @@
 // to the same tolerance as always.
 //
 // Per solve: one product A h_j per history vector (the operator changes every
-// step), the small Gram matrices below, the m x m solve (one thread on the
-// device, so that the solve needs no host read-back), x += H y, and a fresh
-// residual.
+// step), the block partials of the small Gram matrices below, the m x m solve
+// on the host in a stream callback (the partials summed there in block order;
+// the calling thread does not wait, and one FP64 thread on the device took
+// 0.5-0.9 ms for it), x += H y, and a fresh residual.
 #include <cmath>
 
 #include "pd_device.cuh"
@@ -99,22 +100,6 @@ __global__ void k_hist_sum(const double* partials, int blocks, int na, double* o
     }
 }
 
-// The m x m solve on one thread.  A solve that had already converged from
-// the previous solution keeps it (used = 0).
-__global__ void k_hist_solve(int m, const double* dots, int s_off, int g_off, int c_off, double rel_tol,
-                             int net_col, const CgScalars* sc, HistSolve* out)
-{
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
-    double y[kHistMax];
-    int used = hist_solve(m, dots + s_off, dots + g_off, dots + c_off, rel_tol, y);
-    const volatile CgScalars* v = sc;
-    if (v->done) used = 0;
-    for (int k = 0; k < kHistMax; ++k) out->y[k] = (used > 0 && k < m) ? y[k] : 0.0;
-    out->used = used;
-    out->net_used = (used > 0 && net_col >= 0 && net_col < m && y[net_col] != 0.0) ? 1 : 0;
-    out->rz1 = v->rz;
-}
-
 // x += H y, formed in FP64 (the coefficients of nearly parallel history
 // vectors can be large and of opposite sign)
 template <typename Real>
@@ -174,14 +159,33 @@ void launch_hist_dots(bool fp64, int pass, int n, int m, const HistPtrs& H, cons
         if (fp64) k_hist_dots<double, 1><<<blocks, kBlock, 0, st>>>(n, m, H, W, r, partials);
         else k_hist_dots<float, 1><<<blocks, kBlock, 0, st>>>(n, m, H, W, r, partials);
     }
-    k_hist_sum<<<1, 128, 0, st>>>(partials, blocks, hist_dots_count(pass), out);
+    if (out) k_hist_sum<<<1, 128, 0, st>>>(partials, blocks, hist_dots_count(pass), out);
 }
 
-void launch_hist_solve(int m, const double* dots, double rel_tol, int net_col, const CgScalars* sc, HistSolve* out,
-                       cudaStream_t st)
+void hist_host_solve(const HistHostSolve& a)
 {
-    const int na = hist_dots_count(0);
-    k_hist_solve<<<1, 32, 0, st>>>(m, dots, 0, na, kPairs, rel_tol, net_col, sc, out);
+    const int na0 = hist_dots_count(0), na1 = hist_dots_count(1);
+    double dots[kPairs + kHistMax + kPairs];
+    const double* p0 = a.partials;
+    const double* p1 = a.partials + (size_t)a.blocks * na0;
+    for (int k = 0; k < na0; ++k) {   // block order, as k_hist_sum
+        double v = 0.0;
+        for (int b = 0; b < a.blocks; ++b) v += p0[(size_t)b * na0 + k];
+        dots[k] = v;
+    }
+    for (int k = 0; k < na1; ++k) {
+        double v = 0.0;
+        for (int b = 0; b < a.blocks; ++b) v += p1[(size_t)b * na1 + k];
+        dots[na0 + k] = v;
+    }
+    double y[kHistMax];
+    int used = hist_solve(a.m, dots, dots + na0, dots + kPairs, a.rel_tol, y);
+    // a solve that had already converged from the previous solution keeps it
+    if (a.sc->done) used = 0;
+    for (int k = 0; k < kHistMax; ++k) a.out->y[k] = (used > 0 && k < a.m) ? y[k] : 0.0;
+    a.out->used = used;
+    a.out->net_used = (used > 0 && a.net_col >= 0 && a.net_col < a.m && y[a.net_col] != 0.0) ? 1 : 0;
+    a.out->rz1 = a.sc->rz;
 }
 
 void launch_hist_apply(bool fp64, int n, int m, const HistPtrs& H, const HistSolve* Y, void* x, int blocks,
@@ -197,15 +201,14 @@ void launch_hist_push(bool fp64, int n, const uint8_t* act, const void* x, void*
     else k_hist_push<float><<<blocks, kBlock, 0, st>>>(n, act, x, dst);
 }
 
-// ---- the m x m solve (host and device) ------------------------------------------------
+// ---- the m x m solve (host) ------------------------------------------------------------
 // S = H^T H, G = H^T A H (upper triangles, row-major pairs a <= b), c = H^T r1.
 // A pivoted Cholesky of S selects a well-conditioned subset of the history
 // (columns whose remaining component is below rel_tol of the largest are
 // dropped: in FP32 storage they are rounding noise); in the orthonormal basis
 // Q = H_sel R^-1 the projected system G_Q z = c_Q is solved by Cholesky and
 // y = R^-1 z.  Returns the number of columns used (0: no usable guess).
-__host__ __device__ int hist_solve(int m, const double* S_up, const double* G_up, const double* c, double rel_tol,
-                                   double* y)
+int hist_solve(int m, const double* S_up, const double* G_up, const double* c, double rel_tol, double* y)
 {
     double S[kHistMax][kHistMax], G[kHistMax][kHistMax];
     int e = 0;

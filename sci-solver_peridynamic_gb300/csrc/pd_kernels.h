@@ -338,22 +338,29 @@ struct HistSolve {
 };
 // entries of a Gram pass: 0 -> S = H^T H (upper) then c = H^T r; 1 -> G = H^T W (upper)
 int hist_dots_count(int pass);
+// out = nullptr: the block partials only (blocks x hist_dots_count(pass), row per block)
 void launch_hist_dots(bool fp64, int pass, int n, int m, const HistPtrs& H, const HistPtrs& W, const void* r,
                       double* partials, int blocks, double* out, cudaStream_t st);
-// one-thread device solve of the dots of launch_hist_dots (both passes, in
-// order, at `dots`); net_col: the network's column, or -1
-void launch_hist_solve(int m, const double* dots, double rel_tol, int net_col, const CgScalars* sc, HistSolve* out,
-                       cudaStream_t st);
+// the m x m solve on the host (a stream callback): the block partials of both
+// Gram passes (blocks x hist_dots_count(0), then blocks x hist_dots_count(1))
+// summed in block order, the scalars of x1's residual, the result
+struct HistHostSolve {
+    int m;
+    int blocks;
+    int net_col;              // the network's column, or -1
+    double rel_tol;
+    const double* partials;   // pinned
+    const CgScalars* sc;      // pinned
+    HistSolve* out;           // pinned
+};
+void hist_host_solve(const HistHostSolve& a);
 // x += H y where out->used > 0
 void launch_hist_apply(bool fp64, int n, int m, const HistPtrs& H, const HistSolve* Y, void* x, int blocks,
                        cudaStream_t st);
 void launch_hist_push(bool fp64, int n, const uint8_t* act, const void* x, void* dst, int blocks, cudaStream_t st);
 // coefficients y of x1 + H y (Galerkin over the well-conditioned part of span
-// H); returns the number of history columns used, 0 for no guess.  Host and
-// device (history.cu); the host build serves the tests.
-#ifdef __CUDACC__
-__host__ __device__
-#endif
+// H); returns the number of history columns used, 0 for no guess (host,
+// history.cu).
 int hist_solve(int m, const double* S_up, const double* G_up, const double* c, double rel_tol, double* y);
 int force_kernel_blocks_per_sm(bool fp64, int lanes);
 void launch_operator_u(bool fp64, const StepParams& P, const DeviceState& S, int lanes, int unroll, int grid,
