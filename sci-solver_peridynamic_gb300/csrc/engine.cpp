@@ -1202,9 +1202,8 @@ pd_status Engine::hist_project(const StepParams& P)
     for (int j = 0; j < m; ++j) apply_op(P, H.v[j], (void*)W.v[j], slot, nullptr);
     // the block partials of both Gram passes
     const int na0 = hist_dots_count(0), na1 = hist_dots_count(1);
-    launch_hist_dots(fp64_, 0, n_, m, H, W, S_.r, d_hpart_, hist_blocks_, nullptr, stream_);
-    launch_hist_dots(fp64_, 1, n_, m, H, W, nullptr, d_hpart_ + (size_t)hist_blocks_ * na0, hist_blocks_, nullptr,
-                     stream_);
+    launch_hist_dots(fp64_, 0, n_, m, H, W, S_.r, d_hpart_, hist_blocks_, stream_);
+    launch_hist_dots(fp64_, 1, n_, m, H, W, nullptr, d_hpart_ + (size_t)hist_blocks_ * na0, hist_blocks_, stream_);
     // the m x m solve on the host, in stream order: partials and scalars to
     // pinned memory, the callback, its result back to the device (the GPU
     // waits for the round trip; the calling thread does not)

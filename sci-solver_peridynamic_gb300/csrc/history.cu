@@ -90,16 +90,6 @@ __global__ void __launch_bounds__(kBlock) k_hist_dots(int n, int m, HistPtrs H, 
     }
 }
 
-// out[k] = sum over blocks of partials[b][k], in block order (deterministic)
-__global__ void k_hist_sum(const double* partials, int blocks, int na, double* out)
-{
-    for (int k = threadIdx.x; k < na; k += blockDim.x) {
-        double v = 0.0;
-        for (int b = 0; b < blocks; ++b) v += partials[(size_t)b * na + k];
-        out[k] = v;
-    }
-}
-
 // x += H y, formed in FP64 (the coefficients of nearly parallel history
 // vectors can be large and of opposite sign)
 template <typename Real>
@@ -150,7 +140,7 @@ __global__ void __launch_bounds__(kBlock) k_hist_push(int n, const uint8_t* act,
 int hist_dots_count(int pass) { return pass == 0 ? kPairs + kHistMax : kPairs; }
 
 void launch_hist_dots(bool fp64, int pass, int n, int m, const HistPtrs& H, const HistPtrs& W, const void* r,
-                      double* partials, int blocks, double* out, cudaStream_t st)
+                      double* partials, int blocks, cudaStream_t st)
 {
     if (pass == 0) {
         if (fp64) k_hist_dots<double, 0><<<blocks, kBlock, 0, st>>>(n, m, H, W, r, partials);
@@ -159,7 +149,6 @@ void launch_hist_dots(bool fp64, int pass, int n, int m, const HistPtrs& H, cons
         if (fp64) k_hist_dots<double, 1><<<blocks, kBlock, 0, st>>>(n, m, H, W, r, partials);
         else k_hist_dots<float, 1><<<blocks, kBlock, 0, st>>>(n, m, H, W, r, partials);
     }
-    if (out) k_hist_sum<<<1, 128, 0, st>>>(partials, blocks, hist_dots_count(pass), out);
 }
 
 void hist_host_solve(const HistHostSolve& a)
@@ -168,7 +157,7 @@ void hist_host_solve(const HistHostSolve& a)
     double dots[kPairs + kHistMax + kPairs];
     const double* p0 = a.partials;
     const double* p1 = a.partials + (size_t)a.blocks * na0;
-    for (int k = 0; k < na0; ++k) {   // block order, as k_hist_sum
+    for (int k = 0; k < na0; ++k) {   // block order
         double v = 0.0;
         for (int b = 0; b < a.blocks; ++b) v += p0[(size_t)b * na0 + k];
         dots[k] = v;

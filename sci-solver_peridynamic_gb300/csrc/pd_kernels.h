@@ -338,9 +338,9 @@ struct HistSolve {
 };
 // entries of a Gram pass: 0 -> S = H^T H (upper) then c = H^T r; 1 -> G = H^T W (upper)
 int hist_dots_count(int pass);
-// out = nullptr: the block partials only (blocks x hist_dots_count(pass), row per block)
+// the block partials of a Gram pass (blocks x hist_dots_count(pass), a row per block)
 void launch_hist_dots(bool fp64, int pass, int n, int m, const HistPtrs& H, const HistPtrs& W, const void* r,
-                      double* partials, int blocks, double* out, cudaStream_t st);
+                      double* partials, int blocks, cudaStream_t st);
 // the m x m solve on the host (a stream callback): the block partials of both
 // Gram passes (blocks x hist_dots_count(0), then blocks x hist_dots_count(1))
 // summed in block order, the scalars of x1's residual, the result
